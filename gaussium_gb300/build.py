@@ -1,0 +1,145 @@
+"""Build the CUDA library ``libgaussium_gb300.so`` in-tree for sm_103a.
+
+Steps: run the class generator (csrc/gen_eri.py) and the Boys-table generator
+(csrc/boys_table_gen.c, compiled with gcc) into ``_build/gen``, write one translation unit
+per angular-momentum class, compile all of them in parallel with nvcc
+(``-gencode arch=compute_103a,code=sm_103a``) and link them with the C-ABI file
+``csrc/capi.cu``.  Objects are rebuilt only when their inputs change.
+"""
+import concurrent.futures as cf
+import hashlib
+import json
+import os
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+GEN = os.path.join(BUILD, "gen")
+LIB = os.path.join(PKG, "libgaussium_gb300.so")
+HOSTCHECK = os.path.join(BUILD, "libhostcheck.so")
+LMAX = 2
+# Classes whose one-thread-per-quartet kernel is built (all up to L = 6); the two largest
+# classes need the cooperative kernel and are built separately.
+THREAD_LMAX_TOTAL = 6
+
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                  "--expt-relaxed-constexpr", "-I", CSRC, "-I", GEN]
+
+
+def _run(cmd, **kw):
+    r = subprocess.run(cmd, capture_output=True, text=True, **kw)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r
+
+
+def _digest(paths, extra=""):
+    h = hashlib.sha256(extra.encode())
+    for p in paths:
+        with open(p, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def classes():
+    sys.path.insert(0, CSRC)
+    try:
+        import gen_eri
+    finally:
+        sys.path.pop(0)
+    return gen_eri.canonical_classes(LMAX)
+
+
+def generate():
+    os.makedirs(GEN, exist_ok=True)
+    _run([sys.executable, os.path.join(CSRC, "gen_eri.py"), GEN, str(LMAX)])
+    table = os.path.join(GEN, "boys_table.h")
+    gen_src = os.path.join(CSRC, "boys_table_gen.c")
+    exe = os.path.join(BUILD, "boys_table_gen")
+    if not os.path.exists(table) or os.path.getmtime(table) < os.path.getmtime(gen_src):
+        _run(["gcc", "-O2", "-o", exe, gen_src, "-lm"])
+        _run([exe, table])
+    units = []
+    built = [c for c in classes() if sum(c) <= THREAD_LMAX_TOTAL]
+    lst = "// written by build.py\n#pragma once\n#define GS_FOR_EACH_BUILT(X) " + " ".join(
+        "X(%d, %d, %d, %d)" % c for c in built) + "\n"
+    path = os.path.join(GEN, "gs_built_classes.h")
+    if not os.path.exists(path) or open(path).read() != lst:
+        with open(path, "w") as f:
+            f.write(lst)
+    for cls in built:
+        tag = "".join(map(str, cls))
+        path = os.path.join(GEN, f"eri_k_{tag}.cu")
+        code = ('#include "eri_kernels.cuh"\n#include "eri_class_%s.h"\n'
+                'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
+                '    return gs::launch_class<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
+                % (tag, tag, *cls))
+        if not os.path.exists(path) or open(path).read() != code:
+            with open(path, "w") as f:
+                f.write(code)
+        units.append((path, os.path.join(GEN, f"eri_class_{tag}.h")))
+    return units
+
+
+def _compile(src, deps, obj):
+    common = [os.path.join(CSRC, n) for n in ("eri_common.cuh", "eri_kernels.cuh", "gs_args.h")]
+    common.append(os.path.join(GEN, "boys_table.h"))
+    key = _digest([src] + deps + common, " ".join(NVFLAGS))
+    stamp = obj + ".key"
+    if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
+        return obj, False
+    _run([NVCC] + NVFLAGS + ["-c", src, "-o", obj])
+    with open(stamp, "w") as f:
+        f.write(key)
+    return obj, True
+
+
+def build(jobs=None, verbose=False):
+    units = generate()
+    objs = []
+    todo = [(src, [hdr], os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")) for src, hdr in units]
+    todo.append((os.path.join(CSRC, "capi.cu"), [os.path.join(GEN, "gs_built_classes.h")],
+                 os.path.join(BUILD, "capi.o")))
+    jobs = jobs or max(1, os.cpu_count() or 1)
+    changed = False
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        futs = [ex.submit(_compile, *t) for t in todo]
+        for f in futs:
+            obj, did = f.result()
+            objs.append(obj)
+            changed |= did
+    if changed or not os.path.exists(LIB):
+        tmp = LIB + ".tmp%d" % os.getpid()
+        _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def build_hostcheck():
+    """CPU build of the generated recursions (tests only)."""
+    generate()
+    src = os.path.join(CSRC, "hostcheck.cpp")
+    deps = [src, os.path.join(CSRC, "eri_common.cuh"), os.path.join(GEN, "eri_classes.h")]
+    key = _digest(deps + [os.path.join(GEN, f"eri_class_{''.join(map(str, c))}.h") for c in classes()])
+    stamp = HOSTCHECK + ".key"
+    if os.path.exists(HOSTCHECK) and os.path.exists(stamp) and open(stamp).read() == key:
+        return HOSTCHECK
+    tmp = HOSTCHECK + ".tmp%d" % os.getpid()
+    _run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-I", CSRC, "-I", GEN, "-o", tmp, src])
+    os.replace(tmp, HOSTCHECK)
+    with open(stamp, "w") as f:
+        f.write(key)
+    return HOSTCHECK
+
+
+def opcount():
+    with open(os.path.join(GEN, "opcount.json")) as f:
+        return json.load(f)
+
+
+if __name__ == "__main__":
+    print(build())

@@ -1,0 +1,199 @@
+// C ABI of the GB300 ERI / Fock-build engine (declared in include/gaussium_gb300.h).
+// Every entry point takes device pointers the caller owns, a cudaStream_t passed as
+// void*, and returns a status code (0 = success); nothing here allocates device memory.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "eri_common.cuh"
+#include "gs_args.h"
+#include "gs_built_classes.h"
+
+#define GS_DECL(A, B, C, D) int gs_launch_##A##B##C##D(int, int, const void*, cudaStream_t);
+GS_FOR_EACH_BUILT(GS_DECL)
+#undef GS_DECL
+
+namespace {
+
+typedef int (*launch_fn)(int, int, const void*, cudaStream_t);
+
+launch_fn find_class(int la, int lb, int lc, int ld) {
+#define GS_FIND(A, B, C, D) \
+    if (la == A && lb == B && lc == C && ld == D) return gs_launch_##A##B##C##D;
+    GS_FOR_EACH_BUILT(GS_FIND)
+#undef GS_FIND
+    return nullptr;
+}
+
+inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
+
+int check_launch() { return cudaPeekAtLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA; }
+
+__global__ void k_pairs_build(gs::ShellView sv, int npairs, const int* __restrict__ pair_shells,
+                              const int* __restrict__ pair_prim_off, gs::PairRec* pairs,
+                              gs::PrimRec<double>* p64, gs::PrimRec<float>* p32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npairs) return;
+    gs::make_pair(sv, pair_shells[2 * i], pair_shells[2 * i + 1], pair_prim_off[i], pairs[i], p64, p32);
+}
+
+__global__ void k_set_qmax(gs::PairRec* pairs, const double* __restrict__ q, int npairs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < npairs) pairs[i].qmax = (float)q[i];
+}
+
+template <int M, typename T>
+__global__ void k_boys(int n, const double* __restrict__ t, double* __restrict__ F) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T f[M + 1];
+    gs::boys<M, T>((T)t[i], T(1), f);
+    for (int m = 0; m <= M; ++m) F[(size_t)i * (M + 1) + m] = (double)f[m];
+}
+
+// Peak-rate probe: each thread runs `iters` rounds of 8 independent FMA chains.
+template <typename T>
+__global__ void k_fma(int iters, T seed, T* __restrict__ sink) {
+    T a0 = seed + threadIdx.x, a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
+    T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
+    const T b = T(0.999999), c = T(1e-7);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+            a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+        }
+    }
+    const T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == T(-12345)) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the work live
+}
+
+}  // namespace
+
+extern "C" {
+
+int gs_version(void) { return 1; }
+
+const char* gs_status_string(int status) {
+    switch (status) {
+        case GS_OK: return "ok";
+        case GS_ERR_ARG: return "invalid argument";
+        case GS_ERR_CUDA: return "CUDA launch or runtime error";
+        case GS_ERR_CLASS: return "angular-momentum class not built into this library";
+        case GS_ERR_DEVICE: return "device-side status error";
+        case GS_ERR_NOMEM: return "workspace too small";
+        default: return "unknown status";
+    }
+}
+
+int gs_record_sizes(int* sizes) {
+    if (!sizes) return GS_ERR_ARG;
+    sizes[0] = (int)sizeof(gs::PairRec);
+    sizes[1] = (int)sizeof(gs::PrimRec<double>);
+    sizes[2] = (int)sizeof(gs::PrimRec<float>);
+    sizes[3] = (int)sizeof(gs::WriteTask);
+    return GS_OK;
+}
+
+int gs_class_available(int la, int lb, int lc, int ld) {
+    return find_class(la, lb, lc, ld) != nullptr;
+}
+
+int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
+                   const double* coef, int npairs, const int* pair_shells,
+                   const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
+                   void* stream) {
+    if (npairs < 0 || !centre || !l || !prim_off || !expo || !coef || !pair_rec || !prim64)
+        return GS_ERR_ARG;
+    if (npairs == 0) return GS_OK;
+    gs::ShellView sv{centre, l, prim_off, expo, coef};
+    k_pairs_build<<<(npairs + 127) / 128, 128, 0, S(stream)>>>(
+        sv, npairs, pair_shells, pair_prim_off, (gs::PairRec*)pair_rec,
+        (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32);
+    return check_launch();
+}
+
+int gs_schwarz(int la, int lb, void* pair_rec, const void* prim64, const double* comp_scale,
+               int npair, const int* pair_index, double* q, int npairs_total, void* stream) {
+    launch_fn f = find_class(la, lb, la, lb);
+    if (!f) return GS_ERR_CLASS;
+    if (npair < 0 || !pair_rec || !prim64 || !comp_scale || !q) return GS_ERR_ARG;
+    gs::SchwarzArgs a{(const gs::PairRec*)pair_rec, prim64, comp_scale, pair_index, npair, q};
+    int rc = f(GS_KIND_SCHWARZ, 64, &a, S(stream));
+    if (rc) return rc;
+    if (npairs_total > 0)
+        k_set_qmax<<<(npairs_total + 127) / 128, 128, 0, S(stream)>>>((gs::PairRec*)pair_rec, q,
+                                                                       npairs_total);
+    return check_launch();
+}
+
+int gs_eri_blocks(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
+                  const void* prim, const double* comp_scale, int ntask, const void* tasks,
+                  double* out, void* stream) {
+    launch_fn f = find_class(la, lb, lc, ld);
+    if (!f) return GS_ERR_CLASS;
+    if ((precision != 64 && precision != 32) || ntask < 0 || !pair_rec || !prim || !comp_scale ||
+        !out || (ntask > 0 && !tasks))
+        return GS_ERR_ARG;
+    gs::WriteArgs a{(const gs::PairRec*)pair_rec, prim, comp_scale, (const gs::WriteTask*)tasks,
+                    ntask, out};
+    return f(GS_KIND_WRITE, precision, &a, S(stream));
+}
+
+int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
+               const void* prim, const double* comp_scale, const int* func_off, int nshell,
+               int nbf, int ntask, const int* tasks, const double* pj, double* j, int nk,
+               const double* pk, double* k, const double* shell_dmax, double screen_thr,
+               double prec_lo, double prec_hi, void* stream) {
+    launch_fn f = find_class(la, lb, lc, ld);
+    if (!f) return GS_ERR_CLASS;
+    if ((precision != 64 && precision != 32) || ntask < 0 || nbf <= 0 || nk < 0 || !pair_rec ||
+        !prim || !comp_scale || !func_off || (ntask > 0 && !tasks) || (!!pj != !!j) ||
+        (nk > 0 && (!pk || !k)) || (screen_thr > 0 && !shell_dmax))
+        return GS_ERR_ARG;
+    gs::JKArgs a;
+    a.pairs = (const gs::PairRec*)pair_rec;
+    a.prims = prim;
+    a.comp_scale = comp_scale;
+    a.func_off = func_off;
+    a.tasks = (const int2*)tasks;
+    a.ntask = ntask;
+    a.nbf = nbf;
+    a.nshell = nshell;
+    a.nk = nk;
+    a.pj = pj;
+    a.pk = pk;
+    a.j = j;
+    a.k = k;
+    a.shell_dmax = shell_dmax;
+    a.screen_thr = screen_thr;
+    a.prec_lo = prec_lo;
+    a.prec_hi = prec_hi;
+    return f(GS_KIND_JK, precision, &a, S(stream));
+}
+
+int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream) {
+    if (n < 0 || !t || !F || (precision != 64 && precision != 32)) return GS_ERR_ARG;
+    if (n == 0) return GS_OK;
+    const int g = (n + 127) / 128;
+#define GS_BM(MM)                                                                   \
+    case MM:                                                                        \
+        if (precision == 64) k_boys<MM, double><<<g, 128, 0, S(stream)>>>(n, t, F); \
+        else k_boys<MM, float><<<g, 128, 0, S(stream)>>>(n, t, F);                  \
+        break;
+    switch (m) {
+        GS_BM(0) GS_BM(1) GS_BM(2) GS_BM(3) GS_BM(4) GS_BM(5) GS_BM(6) GS_BM(7) GS_BM(8)
+        GS_BM(9) GS_BM(10)
+        default: return GS_ERR_ARG;
+    }
+#undef GS_BM
+    return check_launch();
+}
+
+int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream) {
+    if (blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0 || !sink) return GS_ERR_ARG;
+    if (precision == 64) k_fma<double><<<blocks, threads, 0, S(stream)>>>(iters, 1.0, (double*)sink);
+    else if (precision == 32) k_fma<float><<<blocks, threads, 0, S(stream)>>>(iters, 1.0f, (float*)sink);
+    else return GS_ERR_ARG;
+    return check_launch();
+}
+
+}  // extern "C"

@@ -1,0 +1,286 @@
+// Shared device/host code of the ERI engine: record layouts, the Boys function, the
+// per-shell-quartet driver (primitive loops -> generated VRR -> contraction -> HRR) and
+// the class kernels.  Compiled by nvcc for sm_103a; the record layouts, Boys function and
+// quartet driver also compile as plain C++ (GS_HOST_ONLY) for CPU checks of the generated
+// recursions.
+#pragma once
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define GS_HD __host__ __device__
+#define GS_INLINE __forceinline__
+#define GS_UNROLL _Pragma("unroll")
+#else
+#define GS_HD
+#define GS_INLINE inline
+#define GS_UNROLL
+#endif
+
+#include "boys_table.h"
+
+namespace gs {
+
+// ------------------------------------------------------------------ records
+// One primitive pair of a shell pair (a,b), la >= lb:
+//   p = alpha+beta, i2p = 1/(2p), P = (alpha A + beta B)/p, PA = P - A,
+//   Kp = sqrt(2 pi^(5/2)) * c_a c_b exp(-alpha beta/p |AB|^2) / p
+// so that [00|00]^(m) = Kp_bra Kp_ket (p+q)^(-1/2) F_m(T).
+template <typename T> struct PrimRec;
+template <> struct alignas(16) PrimRec<double> {
+    double p, i2p, Px, Py, Pz, PAx, PAy, PAz, Kp, pad;
+};
+template <> struct alignas(16) PrimRec<float> {
+    float p, i2p, Px, Py, Pz, PAx, PAy, PAz, Kp, pad0, pad1, pad2;
+};
+
+// One shell pair: AB = A - B, its primitive pairs [prim_off, prim_off + nprim), and the
+// two shells (sa has the larger angular momentum).
+struct alignas(16) PairRec {
+    double ABx, ABy, ABz;
+    int prim_off, nprim, sa, sb;
+    float qmax;   // Schwarz bound sqrt(max |(ab|ab)|) of the pair (0 until computed)
+    int pad;
+};
+
+// Microbench / dense-block task: canonical bra and ket pair, 3-bit permutation code
+// (bit0: bra shells swapped, bit1: ket shells swapped, bit2: bra<->ket swapped) and the
+// offset of the block in the caller's original (a,b,c,d) order.
+struct alignas(8) WriteTask {
+    int bra, ket;
+    int code, pad;
+    long long off;
+};
+
+template <typename T> struct VrrCoef {
+    T PAx, PAy, PAz, WPx, WPy, WPz, QCx, QCy, QCz, WQx, WQy, WQz, i2p, rp2, i2q, rq2, i2pq;
+};
+
+template <int LA, int LB, int LC, int LD> struct ClassGen;
+
+// ------------------------------------------------------------------ math helpers
+GS_HD GS_INLINE double gs_rsqrt(double x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrt(x);
+#else
+    return 1.0 / std::sqrt(x);
+#endif
+}
+GS_HD GS_INLINE float gs_rsqrt(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / std::sqrt(x);
+#endif
+}
+GS_HD GS_INLINE double gs_exp(double x) { return exp(x); }
+GS_HD GS_INLINE float gs_exp(float x) {
+#if defined(__CUDA_ARCH__)
+    return expf(x);
+#else
+    return std::exp(x);
+#endif
+}
+
+// ------------------------------------------------------------------ Boys function
+#if defined(__CUDACC__)
+__device__ const double g_boys_d[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
+__device__ const float g_boys_f[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
+#endif
+static const double h_boys_d[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
+static const float h_boys_f[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
+
+template <typename T> GS_HD GS_INLINE const T* boys_table();
+template <> GS_HD GS_INLINE const double* boys_table<double>() {
+#if defined(__CUDA_ARCH__)
+    return g_boys_d;
+#else
+    return h_boys_d;
+#endif
+}
+template <> GS_HD GS_INLINE const float* boys_table<float>() {
+#if defined(__CUDA_ARCH__)
+    return g_boys_f;
+#else
+    return h_boys_f;
+#endif
+}
+
+template <typename T> GS_HD GS_INLINE T ldg(const T* p) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
+// F[m] = pref * F_m(t), m = 0..M.  Below BOYS_TMAX: Taylor expansion of F_M about the
+// nearest grid point (7 terms in double, 4 in float) and downward recursion.  Above it:
+// F_0 = sqrt(pi/t)/2 (erf(sqrt t) = 1 to 2e-17) and upward recursion, stable for t > M.
+template <int M, typename T>
+GS_HD GS_INLINE void boys(T t, T pref, T* __restrict__ F) {
+    constexpr bool dbl = sizeof(T) == 8;
+    if (t < T(BOYS_TMAX)) {
+        const int k = (int)(t * T(BOYS_INV_H) + T(0.5));
+        const T d = T(k) * T(1.0 / BOYS_INV_H) - t;
+        const T* row = boys_table<T>() + k * BOYS_NCOL;
+        T f, e;
+        if (dbl) {
+            const T d2 = d * T(1.0 / 2), d3 = d * T(1.0 / 3), d4 = d * T(1.0 / 4);
+            const T d5 = d * T(1.0 / 5), d6 = d * T(1.0 / 6);
+            f = ldg(row + M + 6);
+            f = f * d6 + ldg(row + M + 5);
+            f = f * d5 + ldg(row + M + 4);
+            f = f * d4 + ldg(row + M + 3);
+            f = f * d3 + ldg(row + M + 2);
+            f = f * d2 + ldg(row + M + 1);
+            f = f * d + ldg(row + M);
+            if (M > 0) {
+                e = d6 + T(1);
+                e = e * d5 + T(1);
+                e = e * d4 + T(1);
+                e = e * d3 + T(1);
+                e = e * d2 + T(1);
+                e = e * d + T(1);
+            }
+        } else {
+            const T d2 = d * T(1.0 / 2), d3 = d * T(1.0 / 3);
+            f = ldg(row + M + 3);
+            f = f * d3 + ldg(row + M + 2);
+            f = f * d2 + ldg(row + M + 1);
+            f = f * d + ldg(row + M);
+            if (M > 0) {
+                e = d3 + T(1);
+                e = e * d2 + T(1);
+                e = e * d + T(1);
+            }
+        }
+        F[M] = f * pref;
+        if (M > 0) {
+            const T et = e * ldg(row + BOYS_NCOL - 1) * pref;
+            const T t2 = t + t;
+            GS_UNROLL for (int m = M; m >= 1; --m) F[m - 1] = (t2 * F[m] + et) * T(1.0 / (2 * m - 1));
+        }
+    } else {
+        const T rs = gs_rsqrt(t);
+        F[0] = pref * T(0.88622692545275801365) * rs;   // sqrt(pi)/2
+        if (M > 0) {
+            const T hit = T(0.5) * rs * rs;
+            const T et = t < T(dbl ? 700 : 85) ? pref * gs_exp(-t) : T(0);
+            GS_UNROLL for (int m = 0; m < M; ++m) F[m + 1] = (T(2 * m + 1) * F[m] - et) * hit;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ one shell quartet
+// Contracted Cartesian block of the canonical quartet (bra | ket), in the component
+// order of ClassGen (blk[((ia*NB+ib)*NC+ic)*ND+id]), without per-component scaling.
+template <int LA, int LB, int LC, int LD, typename T>
+GS_HD GS_INLINE void eri_quartet(const PairRec& B, const PairRec& K,
+                                 const PrimRec<T>* __restrict__ prims, T* __restrict__ blk) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    T acc[G::NACC];
+    GS_UNROLL for (int i = 0; i < G::NACC; ++i) acc[i] = T(0);
+    for (int i = 0; i < B.nprim; ++i) {
+        const PrimRec<T> P = prims[B.prim_off + i];
+        for (int j = 0; j < K.nprim; ++j) {
+            const PrimRec<T> Q = prims[K.prim_off + j];
+            const T pq = P.p + Q.p;
+            const T rs = gs_rsqrt(pq);
+            const T ipq = rs * rs;
+            const T PQx = Q.Px - P.Px, PQy = Q.Py - P.Py, PQz = Q.Pz - P.Pz;
+            const T wq = Q.p * ipq, wp = P.p * ipq;
+            const T t = P.p * wq * (PQx * PQx + PQy * PQy + PQz * PQz);
+            T F[G::L + 1];
+            boys<G::L, T>(t, P.Kp * Q.Kp * rs, F);
+            VrrCoef<T> c;
+            c.PAx = P.PAx; c.PAy = P.PAy; c.PAz = P.PAz;
+            c.WPx = wq * PQx; c.WPy = wq * PQy; c.WPz = wq * PQz;
+            c.QCx = Q.PAx; c.QCy = Q.PAy; c.QCz = Q.PAz;
+            c.WQx = -wp * PQx; c.WQy = -wp * PQy; c.WQz = -wp * PQz;
+            c.i2p = P.i2p; c.i2q = Q.i2p;
+            c.rp2 = wq * P.i2p; c.rq2 = wp * Q.i2p;
+            c.i2pq = T(0.5) * ipq;
+            G::vrr(F, c, acc);
+        }
+    }
+    G::hrr(acc, T(B.ABx), T(B.ABy), T(B.ABz), T(K.ABx), T(K.ABy), T(K.ABz), blk);
+}
+
+// ------------------------------------------------------------------ shell-pair records
+// Shells as the engine stores them: centre (bohr), angular momentum l, primitives
+// [prim_off[s], prim_off[s+1]) with exponent and effective coefficient (contraction times
+// primitive and contracted normalisation of the shell's first Cartesian component), and
+// comp_scale[s*6 + i], the ratio of component i's normalisation to the first one's.
+struct ShellView {
+    const double* centre;
+    const int* l;
+    const int* prim_off;
+    const double* expo;
+    const double* coef;
+};
+
+constexpr double kSqrt2Pi52 = 5.914967172795613;  // sqrt(2 pi^(5/2))
+
+// Fill the PairRec and the primitive-pair records of shell pair (sa, sb); la >= lb.
+GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off, PairRec& pr,
+                               PrimRec<double>* pd, PrimRec<float>* pf) {
+    const double* A = S.centre + 3 * sa;
+    const double* B = S.centre + 3 * sb;
+    const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
+    const double ab2 = ABx * ABx + ABy * ABy + ABz * ABz;
+    const int a0 = S.prim_off[sa], a1 = S.prim_off[sa + 1];
+    const int b0 = S.prim_off[sb], b1 = S.prim_off[sb + 1];
+    pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
+    pr.prim_off = prim_off;
+    pr.nprim = (a1 - a0) * (b1 - b0);
+    pr.sa = sa; pr.sb = sb;
+    pr.qmax = 0.0f; pr.pad = 0;
+    int n = prim_off;
+    for (int i = a0; i < a1; ++i) {
+        for (int j = b0; j < b1; ++j, ++n) {
+            const double a = S.expo[i], b = S.expo[j];
+            const double p = a + b, ip = 1.0 / p;
+            PrimRec<double> r;
+            r.p = p;
+            r.i2p = 0.5 * ip;
+            r.Px = (a * A[0] + b * B[0]) * ip;
+            r.Py = (a * A[1] + b * B[1]) * ip;
+            r.Pz = (a * A[2] + b * B[2]) * ip;
+            r.PAx = r.Px - A[0]; r.PAy = r.Py - A[1]; r.PAz = r.Pz - A[2];
+            r.Kp = kSqrt2Pi52 * S.coef[i] * S.coef[j] * exp(-a * b * ip * ab2) * ip;
+            r.pad = 0.0;
+            pd[n] = r;
+            if (pf) {
+                PrimRec<float> f;
+                f.p = (float)r.p; f.i2p = (float)r.i2p;
+                f.Px = (float)r.Px; f.Py = (float)r.Py; f.Pz = (float)r.Pz;
+                f.PAx = (float)r.PAx; f.PAy = (float)r.PAy; f.PAz = (float)r.PAz;
+                f.Kp = (float)r.Kp; f.pad0 = f.pad1 = f.pad2 = 0.0f;
+                pf[n] = f;
+            }
+        }
+    }
+}
+
+// Original-order strides of a canonical block (see WriteTask::code).
+GS_HD GS_INLINE void block_strides(int code, int nA, int nB, int nC, int nD, long long s[4]) {
+    const bool b0 = code & 1, b1 = code & 2, b2 = code & 4;
+    int n[4];
+    int posA, posB, posC, posD;
+    if (!b2) {
+        n[0] = b0 ? nB : nA; n[1] = b0 ? nA : nB;
+        n[2] = b1 ? nD : nC; n[3] = b1 ? nC : nD;
+        posA = b0 ? 1 : 0; posB = 1 - posA;
+        posC = b1 ? 3 : 2; posD = 5 - posC;
+    } else {
+        n[2] = b0 ? nB : nA; n[3] = b0 ? nA : nB;
+        n[0] = b1 ? nD : nC; n[1] = b1 ? nC : nD;
+        posA = b0 ? 3 : 2; posB = 5 - posA;
+        posC = b1 ? 1 : 0; posD = 1 - posC;
+    }
+    long long st[4] = {(long long)n[1] * n[2] * n[3], (long long)n[2] * n[3], n[3], 1};
+    s[0] = st[posA]; s[1] = st[posB]; s[2] = st[posC]; s[3] = st[posD];
+}
+
+}  // namespace gs

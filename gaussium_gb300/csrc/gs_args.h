@@ -1,0 +1,56 @@
+// Argument blocks passed by value to the class kernels (device pointers only).
+#pragma once
+#include <cuda_runtime.h>
+
+#define GS_KIND_WRITE 0
+#define GS_KIND_JK 1
+#define GS_KIND_SCHWARZ 2
+
+#define GS_OK 0
+#define GS_ERR_ARG 1
+#define GS_ERR_CUDA 2
+#define GS_ERR_CLASS 3
+#define GS_ERR_DEVICE 4
+#define GS_ERR_NOMEM 5
+
+namespace gs {
+struct PairRec;
+struct WriteTask;
+
+struct WriteArgs {
+    const PairRec* pairs;
+    const void* prims;          // PrimRec<double> or PrimRec<float>
+    const double* comp_scale;   // [nshell][6]
+    const WriteTask* tasks;
+    int ntask;
+    double* out;
+};
+
+struct JKArgs {
+    const PairRec* pairs;
+    const void* prims;
+    const double* comp_scale;
+    const int* func_off;        // [nshell]
+    const int2* tasks;          // (bra pair, ket pair), canonical
+    int ntask;
+    int nbf;
+    int nshell;
+    int nk;                     // number of exchange densities
+    const double* pj;           // density for J (nbf x nbf) or null
+    const double* pk;           // nk densities for K
+    double* j;                  // J' accumulator (nbf x nbf) or null
+    double* k;                  // nk K' accumulators
+    const double* shell_dmax;   // [nshell][nshell] max |P| per shell block (screening)
+    double screen_thr;          // 0 disables screening and precision selection
+    double prec_lo, prec_hi;    // evaluate only quartets with prec_lo <= bound < prec_hi
+};
+
+struct SchwarzArgs {
+    const PairRec* pairs;
+    const void* prims;          // PrimRec<double>
+    const double* comp_scale;
+    const int* pair_index;      // pairs of this class
+    int npair;
+    double* q;                  // [npairs total] output
+};
+}  // namespace gs

@@ -1,0 +1,331 @@
+"""Device-side ERI engine: shells and shell pairs in HBM, class-sorted quartet task lists,
+and the launches of the sm_103a class kernels through the C ABI.
+
+Layout in HBM (all owned by torch tensors):
+  DeviceShells  per shell: centre[3] f64, l i32, prim_off i32, func_off i32, comp_scale[6] f64;
+                per primitive: exponent f64, effective coefficient f64.
+  PairSet       per shell pair a 48-byte PairRec (AB, primitive-pair range, shells, Schwarz
+                bound); per primitive pair an 80-byte f64 record and a 48-byte f32 record
+                (p, 1/2p, P, PA, Kp) -- see csrc/eri_common.cuh.
+  tasks         write tasks (24 B: bra, ket, permutation code, output offset) or Fock
+                tasks (8 B: bra, ket), grouped by angular-momentum class and sorted by
+                primitive counts so a warp's threads run the same loop trip counts.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from .basis import COMPONENTS, ShellBasis
+
+PAIR_ORDER = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
+PAIR_CLASS = {p: i for i, p in enumerate(PAIR_ORDER)}
+NCART = np.array([1, 3, 6, 10])
+PAIR_REC, PRIM64, PRIM32, WRITE_TASK = 48, 80, 48, 24
+WRITE_TASK_DTYPE = np.dtype([("bra", "<i4"), ("ket", "<i4"), ("code", "<i4"), ("pad", "<i4"),
+                             ("off", "<i8")])
+
+_pc_lut = np.full((3, 3), -1, dtype=np.int64)
+for _i, (_a, _b) in enumerate(PAIR_ORDER):
+    _pc_lut[_a, _b] = _i
+
+
+def _check_sizes():
+    sizes = np.zeros(4, dtype=np.int32)
+    _lib.check(_lib.lib().gs_record_sizes(sizes.ctypes.data), "gs_record_sizes")
+    if tuple(sizes) != (PAIR_REC, PRIM64, PRIM32, WRITE_TASK):
+        raise _lib.GsError(f"record sizes mismatch: library {tuple(sizes)}")
+
+
+class DeviceShells:
+    """A ShellBasis copied to the device."""
+
+    def __init__(self, sb: ShellBasis, device="cuda"):
+        self.host = sb
+        self.device = torch.device(device)
+
+        def t(a, dt):
+            return torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.device)
+
+        self.centre = t(sb.centre, torch.float64)
+        self.l = t(sb.l, torch.int32)
+        self.prim_off = t(sb.prim_off, torch.int32)
+        self.expo = t(sb.expo, torch.float64)
+        self.coef = t(sb.coef, torch.float64)
+        self.comp_scale = t(sb.comp_scale, torch.float64)
+        self.func_off = t(sb.func_off, torch.int32)
+        self.nshell = sb.nshell
+        self.nbf = sb.nbf
+
+
+class PairSet:
+    """Shell pairs (la >= lb inside each pair) with their primitive-pair records."""
+
+    def __init__(self, ds: DeviceShells, pair_shells, want32=True, stream=None):
+        ps = np.ascontiguousarray(pair_shells, dtype=np.int32).reshape(-1, 2)
+        sb = ds.host
+        if len(ps) and np.any(sb.l[ps[:, 0]] < sb.l[ps[:, 1]]):
+            raise ValueError("pair shells must have l[first] >= l[second]")
+        npp = sb.nprim[ps[:, 0]].astype(np.int64) * sb.nprim[ps[:, 1]]
+        off = np.zeros(len(ps) + 1, dtype=np.int64)
+        off[1:] = np.cumsum(npp)
+        if off[-1] >= 2 ** 31:
+            raise ValueError("too many primitive pairs for one PairSet")
+        self.ds = ds
+        self.n = len(ps)
+        self.host_shells = ps
+        self.nprim = npp
+        self.la = sb.l[ps[:, 0]] if len(ps) else np.zeros(0, np.int32)
+        self.lb = sb.l[ps[:, 1]] if len(ps) else np.zeros(0, np.int32)
+        dev = ds.device
+        self.shells = torch.as_tensor(ps).to(dev)
+        self.prim_start = torch.as_tensor(off[:-1].astype(np.int32)).to(dev)
+        self.rec = torch.empty(max(1, self.n) * PAIR_REC, dtype=torch.uint8, device=dev)
+        total = max(1, int(off[-1]))
+        self.p64 = torch.empty(total * PRIM64, dtype=torch.uint8, device=dev)
+        self.p32 = torch.empty(total * PRIM32, dtype=torch.uint8, device=dev) if want32 else None
+        self.nprim_pairs = int(off[-1])
+        self.build(stream)
+
+    def build(self, stream=None):
+        """(Re)compute the pair records (kernel K0) from the device shells."""
+        ds = self.ds
+        L = _lib.lib()
+        _lib.check(L.gs_pairs_build(_lib.ptr(ds.centre), _lib.ptr(ds.l), _lib.ptr(ds.prim_off),
+                                    _lib.ptr(ds.expo), _lib.ptr(ds.coef), self.n,
+                                    _lib.ptr(self.shells), _lib.ptr(self.prim_start),
+                                    _lib.ptr(self.rec), _lib.ptr(self.p64), _lib.ptr(self.p32),
+                                    _lib.stream(stream)), "gs_pairs_build")
+
+    def prims(self, precision):
+        return self.p64 if precision == 64 else self.p32
+
+
+# ---------------------------------------------------------------------- shell-quartet blocks
+def canonicalize(l4):
+    """Per quartet of angular momenta (n,4): canonical order (bra pair class >= ket pair
+    class, la >= lb, lc >= ld), the 3-bit permutation code, and index maps."""
+    la, lb, lc, ld = l4[:, 0], l4[:, 1], l4[:, 2], l4[:, 3]
+    s_ab = la < lb
+    s_cd = lc < ld
+    A = np.where(s_ab, 1, 0); B = 1 - A
+    C = np.where(s_cd, 3, 2); Dd = 5 - C
+    pc1 = _pc_lut[np.maximum(la, lb), np.minimum(la, lb)]
+    pc2 = _pc_lut[np.maximum(lc, ld), np.minimum(lc, ld)]
+    s_bk = pc2 > pc1
+    code = np.where(s_bk, s_cd.astype(np.int32) | (s_ab.astype(np.int32) << 1) | 4,
+                    s_ab.astype(np.int32) | (s_cd.astype(np.int32) << 1))
+    pos = np.stack([np.where(s_bk, C, A), np.where(s_bk, Dd, B),
+                    np.where(s_bk, A, C), np.where(s_bk, B, Dd)], axis=1)
+    return pos, code.astype(np.int32), np.where(s_bk, pc2, pc1), np.where(s_bk, pc1, pc2)
+
+
+class QuartetBatch:
+    """A batch of shell quartets (n,4 shell indices, any order) evaluated into one flat f64
+    buffer: quartet q's block occupies out[off[q] : off[q] + na*nb*nc*nd] in the caller's
+    (a,b,c,d) order, row-major.  Host preparation sorts the quartets by class and
+    primitive counts; ``run`` launches one kernel per class."""
+
+    def __init__(self, ds: DeviceShells, quartets, want32=True):
+        q = np.ascontiguousarray(quartets, dtype=np.int64).reshape(-1, 4)
+        sb = ds.host
+        n = len(q)
+        l4 = sb.l[q]
+        pos, code, pcb, pck = canonicalize(l4)
+        qc = np.take_along_axis(q, pos, axis=1)          # canonical shells
+        size = np.prod(NCART[l4], axis=1)
+        off = np.zeros(n + 1, dtype=np.int64)
+        off[1:] = np.cumsum(size)
+        self.n = n
+        self.offsets = off
+        self.total = int(off[-1])
+        pairs = np.concatenate([qc[:, 0:2], qc[:, 2:4]], axis=0)
+        self.pairs = PairSet(ds, pairs, want32=want32)
+        nb = self.pairs.nprim[:n]
+        nk = self.pairs.nprim[n:]
+        cls = pcb * 6 + pck
+        order = np.lexsort((nk, nb, cls))
+        tasks = np.zeros(n, dtype=WRITE_TASK_DTYPE)
+        tasks["bra"] = order
+        tasks["ket"] = order + n
+        tasks["code"] = code[order]
+        tasks["off"] = off[:-1][order]
+        self.prim_quartets = int(np.sum(nb * nk))
+        scls = cls[order]
+        self.segments = []
+        starts = np.flatnonzero(np.diff(np.concatenate([[-1], scls]))) if n else []
+        bounds = list(starts) + [n]
+        for s, e in zip(bounds[:-1], bounds[1:]):
+            c = int(scls[s])
+            (la, lb), (lc, ld) = PAIR_ORDER[c // 6], PAIR_ORDER[c % 6]
+            self.segments.append(((la, lb, lc, ld), int(s), int(e)))
+        self.tasks_host = tasks
+        self.tasks = torch.as_tensor(tasks.view(np.uint8)).to(ds.device)
+        self.ds = ds
+        self.sorted_bra_nprim = nb[order]
+        self.sorted_ket_nprim = nk[order]
+
+    def class_counts(self):
+        return {cls: e - s for cls, s, e in self.segments}
+
+    def run(self, out, precision=64, stream=None, classes=None):
+        L = _lib.lib()
+        st = _lib.stream(stream)
+        base = self.tasks.data_ptr()
+        prims = self.pairs.prims(precision)
+        for cls, s, e in self.segments:
+            if classes is not None and cls not in classes:
+                continue
+            rc = L.gs_eri_blocks(*cls, precision, _lib.ptr(self.pairs.rec), _lib.ptr(prims),
+                                 _lib.ptr(self.ds.comp_scale), e - s,
+                                 base + s * WRITE_TASK, _lib.ptr(out), st)
+            _lib.check(rc, f"gs_eri_blocks{cls}")
+        return out
+
+
+def eri_blocks(sb: ShellBasis, quartets, precision=64, device="cuda"):
+    """Convenience: blocks of the given shell quartets, returned as a host f64 array."""
+    ds = DeviceShells(sb, device)
+    batch = QuartetBatch(ds, quartets, want32=precision == 32)
+    out = torch.zeros(max(1, batch.total), dtype=torch.float64, device=ds.device)
+    batch.run(out, precision)
+    return out[:batch.total].cpu().numpy(), batch.offsets
+
+
+# ---------------------------------------------------------------------- Fock (J/K) engine
+class JKEngine:
+    """Integral-direct Coulomb/exchange builder over all unique shell quartets of one
+    basis, with Schwarz screening (task list built once per geometry) and optional
+    density-weighted screening / precision selection per call."""
+
+    def __init__(self, sb: ShellBasis, device="cuda", schwarz_thr=1e-12, want32=True):
+        self.sb = sb
+        self.ds = ds = DeviceShells(sb, device)
+        self.dev = ds.device
+        ns = sb.nshell
+        i, j = np.tril_indices(ns)                      # shell i >= shell j
+        swap = sb.l[i] < sb.l[j]
+        sa = np.where(swap, j, i)
+        sbb = np.where(swap, i, j)
+        self.pairs = PairSet(ds, np.stack([sa, sbb], axis=1), want32=want32)
+        self.pair_class = _pc_lut[sb.l[sa], sb.l[sbb]]
+        self.npairs = len(sa)
+        self.schwarz_thr = schwarz_thr
+        self.q = torch.zeros(self.npairs, dtype=torch.float64, device=self.dev)
+        L = _lib.lib()
+        for c, (la, lb) in enumerate(PAIR_ORDER):
+            idx = np.flatnonzero(self.pair_class == c).astype(np.int32)
+            if len(idx) == 0:
+                continue
+            it = torch.as_tensor(idx).to(self.dev)
+            _lib.check(L.gs_schwarz(la, lb, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
+                                    _lib.ptr(ds.comp_scale), len(idx), _lib.ptr(it),
+                                    _lib.ptr(self.q), self.npairs, _lib.stream()), "gs_schwarz")
+        self._build_tasks()
+        # function -> shell map for per-shell-block density maxima
+        self.func_shell = torch.as_tensor(np.repeat(np.arange(ns), sb.nfunc)).to(self.dev)
+
+    def _build_tasks(self):
+        dev = self.dev
+        q = self.q
+        nprim = torch.as_tensor(self.pairs.nprim).to(dev)
+        self.segments = []
+        chunks = []
+        ntot = 0
+        thr = self.schwarz_thr
+        pc = torch.as_tensor(self.pair_class).to(dev)
+        for cb in range(len(PAIR_ORDER)):
+            bra_ids = torch.nonzero(pc == cb).flatten()
+            if bra_ids.numel() == 0:
+                continue
+            qb, ob = torch.sort(q[bra_ids], descending=True)
+            bra_sorted = bra_ids[ob]
+            for ck in range(cb + 1):
+                ket_ids = torch.nonzero(pc == ck).flatten()
+                if ket_ids.numel() == 0:
+                    continue
+                qk, ok = torch.sort(q[ket_ids], descending=True)
+                ket_sorted = ket_ids[ok]
+                # number of kets with qb*qk >= thr: prefix of the descending list
+                need = torch.where(qb > 0, thr / qb, torch.full_like(qb, float("inf")))
+                cnt = torch.searchsorted(-qk.contiguous(), -need.contiguous(), right=True)
+                if cb == ck:
+                    start = torch.arange(len(qb), device=dev)
+                    cnt = torch.clamp(cnt - start, min=0)
+                else:
+                    start = torch.zeros(len(qb), dtype=torch.int64, device=dev)
+                total = int(cnt.sum())
+                if total == 0:
+                    continue
+                bra_pos = torch.repeat_interleave(torch.arange(len(qb), device=dev), cnt)
+                first = torch.cumsum(cnt, 0) - cnt
+                within = torch.arange(total, device=dev) - first[bra_pos]
+                ket_pos = start[bra_pos] + within
+                bra = bra_sorted[bra_pos]
+                ket = ket_sorted[ket_pos]
+                key = nprim[bra] * 64 + nprim[ket]
+                key, o = torch.sort(key, stable=True)
+                t = torch.stack([bra[o], ket[o]], dim=1).to(torch.int32)
+                (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
+                self.segments.append(((la, lb, lc, ld), ntot, ntot + total))
+                chunks.append(t)
+                ntot += total
+        self.tasks = torch.cat(chunks, 0).contiguous() if chunks else \
+            torch.zeros((1, 2), dtype=torch.int32, device=dev)
+        self.ntasks = ntot
+
+    def shell_dmax(self, mats):
+        """max |P_ij| over each (shell, shell) block, over all given matrices."""
+        ns = self.sb.nshell
+        m = torch.stack([x.abs() for x in mats]).amax(0)
+        fs = self.func_shell
+        rows = torch.full((ns, m.shape[1]), 0.0, dtype=torch.float64, device=self.dev)
+        rows.index_reduce_(0, fs, m, "amax", include_self=True)
+        out = torch.full((ns, ns), 0.0, dtype=torch.float64, device=self.dev)
+        out.index_reduce_(1, fs, rows, "amax", include_self=True)
+        return out.contiguous()
+
+    def jk(self, pj=None, pk=(), precision=64, screen_thr=0.0, mixed_cut=None, stream=None,
+           classes=None):
+        """J[pj] and K[pk_s] (symmetric densities, nbf x nbf f64 device tensors).
+
+        precision 64 or 32 evaluates every task in that precision.  With ``mixed_cut``
+        the quartets whose density-weighted bound is below it run in f32 and the rest in
+        f64 (accumulation is always f64).  ``screen_thr`` > 0 additionally skips quartets
+        whose density-weighted bound is below it."""
+        n = self.sb.nbf
+        dev = self.dev
+        pk = list(pk)
+        nk = len(pk)
+        jbuf = torch.zeros((n, n), dtype=torch.float64, device=dev) if pj is not None else None
+        kbuf = torch.zeros((max(nk, 1), n, n), dtype=torch.float64, device=dev) if nk else None
+        pj_c = pj.contiguous() if pj is not None else None
+        pk_c = torch.stack(pk).contiguous() if nk else None
+        dmax = None
+        runs = [(precision, 0.0, float("inf"))]
+        if mixed_cut is not None or screen_thr > 0:
+            mats = ([pj] if pj is not None else []) + pk
+            dmax = self.shell_dmax(mats)
+            thr = screen_thr if screen_thr > 0 else 1e-300
+            if mixed_cut is not None:
+                runs = [(64, mixed_cut, float("inf")), (32, 0.0, mixed_cut)]
+            else:
+                runs = [(precision, 0.0, float("inf"))]
+        else:
+            thr = 0.0
+        L = _lib.lib()
+        st = _lib.stream(stream)
+        base = self.tasks.data_ptr()
+        for prec, lo, hi in runs:
+            prims = self.pairs.prims(prec)
+            for cls, s, e in self.segments:
+                if classes is not None and cls not in classes:
+                    continue
+                rc = L.gs_fock_jk(*cls, prec, _lib.ptr(self.pairs.rec), _lib.ptr(prims),
+                                  _lib.ptr(self.ds.comp_scale), _lib.ptr(self.ds.func_off),
+                                  self.sb.nshell, n, e - s, base + s * 8, _lib.ptr(pj_c),
+                                  _lib.ptr(jbuf), nk, _lib.ptr(pk_c), _lib.ptr(kbuf),
+                                  _lib.ptr(dmax), thr, lo, hi, st)
+                _lib.check(rc, f"gs_fock_jk{cls}")
+        J = (jbuf + jbuf.T) if jbuf is not None else None
+        K = [kbuf[s] + kbuf[s].T for s in range(nk)]
+        return J, K

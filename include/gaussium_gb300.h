@@ -1,0 +1,117 @@
+/*
+ * gaussium_gb300 -- C ABI of the GB300 (sm_103a) two-electron-integral and Fock-build
+ * engine.  The reference Gaussium is pure Python and has no FFI; these entry points are
+ * what its ERI path binds through ctypes.  Each one cites the
+ * reference function it replaces (file:line within the reference project).
+ *
+ * Conventions
+ *   - All array arguments are DEVICE pointers owned by the caller (torch tensors in the
+ *     Python host code); `stream` is a cudaStream_t passed as void*.  No entry point
+ *     allocates device memory.
+ *   - Every entry point returns a status code: 0 = GS_OK, otherwise one of GS_ERR_*;
+ *     gs_status_string() gives its text.  Nothing throws or aborts across the ABI.
+ *   - Launches are asynchronous on `stream`; errors of the kernels themselves surface at
+ *     the caller's next synchronisation.
+ *   - Records (sizes from gs_record_sizes):
+ *       PairRec  48 B  {double AB[3]; int prim_off, nprim, sa, sb; float qmax; int pad;}
+ *       Prim64   80 B  {double p, 1/(2p), P[3], PA[3], Kp, pad;}
+ *       Prim32   48 B  {float  p, 1/(2p), P[3], PA[3], Kp, pad[3];}
+ *       WriteTask 24 B {int bra, ket, code, pad; long long off;}
+ *   - Shells: l <= 2, Cartesian components in the reference order
+ *     (s; x,y,z; xx,yy,zz,xy,xz,yz -- factory/primitive_basis_factory.py:5-86), effective
+ *     contraction coefficients and per-component scale factors as built by
+ *     gaussium_gb300/basis.py from the reference's normalisations
+ *     (objects/basis_function.py:22-53, objects/primitive_basis_function.py:26-42).
+ */
+#ifndef GAUSSIUM_GB300_H
+#define GAUSSIUM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS_OK 0
+#define GS_ERR_ARG 1
+#define GS_ERR_CUDA 2
+#define GS_ERR_CLASS 3
+#define GS_ERR_DEVICE 4
+#define GS_ERR_NOMEM 5
+
+/* Library version (1). */
+int gs_version(void);
+
+/* Text of a status code (static storage). */
+const char* gs_status_string(int status);
+
+/* sizes[0..3] = sizeof PairRec, Prim64, Prim32, WriteTask (host pointer). */
+int gs_record_sizes(int* sizes);
+
+/* 1 if the (la lb | lc ld) class kernel is built into this library, else 0. */
+int gs_class_available(int la, int lb, int lc, int ld);
+
+/* K0 shell-pair builder.  Replaces the per-primitive-quartet prologue of
+ * ObaraSaika.integrate (integrals/twoelectronrepulsion/obara_saika_scheme.py:52-70:
+ * Gaussian product centre, exponent sums, exp(-ab/p |AB|^2) and the contraction/
+ * normalisation product), hoisted to once per primitive *pair*.
+ * Shells: centre[nshell*3] (bohr), l[nshell], prim_off[nshell+1], expo[nprim],
+ * coef[nprim].  Pairs: pair_shells[npairs*2] (l[first] >= l[second]),
+ * pair_prim_off[npairs] (first primitive-pair record of each pair).  Outputs:
+ * pair_rec[npairs], prim64[sum Ka*Kb], prim32 (may be NULL). */
+int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
+                   const double* coef, int npairs, const int* pair_shells,
+                   const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
+                   void* stream);
+
+/* K1 Schwarz bounds q[p] = sqrt(max |(ab|ab)|) for the npair pairs pair_index[] of class
+ * (la lb), in FP64; then copies all npairs_total bounds into pair_rec[].qmax.  No
+ * reference counterpart (the reference does not screen); it feeds the screened quartet
+ * lists that stand in for the key loop of create_repulsion_matrix
+ * (matrixelements/electron_repulsion_matrix.py:30-33). */
+int gs_schwarz(int la, int lb, void* pair_rec, const void* prim64, const double* comp_scale,
+               int npair, const int* pair_index, double* q, int npairs_total, void* stream);
+
+/* K3 ERI class kernel, block output.  Replaces ObaraSaika.integrate /
+ * HeadGordonPople.integrate / ElectronRepulsion.integrate
+ * (obara_saika_scheme.py:17-82, head_gordon_pople.py:18-91, cook_integral.py:15-99) for
+ * every function quartet of ntask shell quartets of class (la lb | lc ld) at once
+ * (la >= lb, lc >= ld, bra pair class >= ket pair class).  tasks[] are WriteTasks; block
+ * q is written to out + off in the caller's original (a,b,c,d) order, row-major.
+ * precision 64: FP64 throughout; 32: FP32 evaluation, FP64 output. */
+int gs_eri_blocks(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
+                  const void* prim, const double* comp_scale, int ntask, const void* tasks,
+                  double* out, void* stream);
+
+/* K3+K4 integral-direct Coulomb/exchange digestion.  Replaces the Python element loops
+ * of FockMatrixRestricted.create (hartreefock/fock_matrix.py:12-22),
+ * FockMatrixUnrestricted.create (fock_matrix.py:32-53),
+ * BlockedFockMatrixUnrestricted.create (fock_matrix.py:63-81) and the Coulomb part of
+ * RestrictedKohnShamHamiltonian.create (kohnsham/kohn_sham_hamiltonian.py:15-19),
+ * which read a stored N^4 tensor.  For the ntask unique shell quartets tasks[2*t] =
+ * (bra pair, ket pair) of class (la lb | lc ld) it accumulates (FP64 atomics)
+ *   J'_ab += 2 v P_cd, J'_cd += 2 v P_ab                  (if pj and j are given)
+ *   K'_ac += v P_bd, K'_ad += v P_bc, K'_bc += v P_ad, K'_bd += v P_ac   (nk densities)
+ * with v the quartet's integral over its permutation multiplicity; the caller forms
+ * J = J' + J'^T and K = K' + K'^T.  Matrices are nbf x nbf row-major.  With
+ * screen_thr > 0 a quartet is evaluated only if qmax_bra*qmax_ket*max|P| over its six
+ * shell blocks (shell_dmax[nshell*nshell]) is >= screen_thr and lies in
+ * [prec_lo, prec_hi) -- the mixed-precision split.  precision 64 or 32 (FP32 integrals
+ * and digestion, FP64 accumulation). */
+int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
+               const void* prim, const double* comp_scale, const int* func_off, int nshell,
+               int nbf, int ntask, const int* tasks, const double* pj, double* j, int nk,
+               const double* pk, double* k, const double* shell_dmax, double screen_thr,
+               double prec_lo, double prec_hi, void* stream);
+
+/* K2 Boys function F_0..F_m(t) (m <= 10) of n arguments t[] into F[n*(m+1)], in FP64 or
+ * FP32 (results widened to FP64).  Replaces boys_function / boys_function_recursion
+ * (integrals/boys_function.py:4-76). */
+int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream);
+
+/* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
+ * blocks*threads elements of the chosen type.  No reference counterpart. */
+int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAUSSIUM_GB300_H */

@@ -20,9 +20,9 @@ Each file records what produced it:
                      shell quartets, sampled function quartets through ObaraSaika, and a
                      subset through HeadGordonPople and Cook; also the reference's contracted
                      and primitive normalisations of every shell.
-* ``energies.npz``   reference total energies of test_start.py systems that run without
-                     point-group symmetry (HeH+ STO-3G, O2 UHF/GUHF STO-3G) and the
-                     test_hatree_fock.py electronic energy.
+* ``energies.npz``   reference total energies of test_start.py systems run without
+                     point-group symmetry (HeH+ STO-3G RHF, O2 UHF/GUHF STO-3G).
+* ``heh_sto3g.npz``, ``o2_sto3g.npz``  their basis functions and S, T, V matrices.
 """
 import argparse
 import contextlib
@@ -355,12 +355,20 @@ def make_energies(procs):
     out = {}
     d = f"{REF}/tests/testslow/start"
     nuclei, electrons, mult, basis = load_molecule(f"{d}/HeH+.mol", f"{d}/STO-3G.gbs")
-    out["heh_sto3g_rhf"], _ = run_rhf(nuclei, electrons, basis, procs)
+    out["heh_sto3g_rhf"], out["heh_sto3g_rhf_iterations"] = run_rhf(nuclei, electrons, basis, procs)
+    np.savez_compressed(os.path.join(HERE, "heh_sto3g.npz"), electrons=electrons, multiplicity=mult,
+                        coords=np.array([x.coordinates for x in nuclei]),
+                        charges=np.array([x.charge for x in nuclei]),
+                        **one_electron(nuclei, basis), **basis_arrays(basis))
     for method in ("UHF", "GUHF"):
         nuclei, electrons, mult, basis = load_molecule(f"{d}/O2.mol", f"{d}/STO-3G.gbs")
         energy = Energy(electrons, mult, procs, method)
         energy.symmetry_object = ref_harness.c1_symmetry(basis)
         out[f"o2_sto3g_{method.lower()}"] = float(quiet(energy.calculate_energy, nuclei, basis))
+    np.savez_compressed(os.path.join(HERE, "o2_sto3g.npz"), electrons=electrons, multiplicity=mult,
+                        coords=np.array([x.coordinates for x in nuclei]),
+                        charges=np.array([x.charge for x in nuclei]),
+                        **one_electron(nuclei, basis), **basis_arrays(basis))
     np.savez_compressed(os.path.join(HERE, "energies.npz"), **out)
 
 

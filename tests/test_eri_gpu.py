@@ -1,0 +1,135 @@
+"""ERI class kernels on the GPU (through the C ABI) against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import golden, synthetic_shells
+from molecules import load
+import hostcheck
+
+pytestmark = pytest.mark.gpu
+
+
+def test_boys_device_matches_exact(gpu_lib):
+    from gaussium_gb300 import _lib
+    g = golden("boys")
+    xs = torch.tensor(g["x"], dtype=torch.float64, device="cuda")
+    for M in (0, 4, 8, 10):
+        ex = np.array([[oracle.boys_exact(m, x) for m in range(M + 1)] for x in g["x"]])
+        for prec, rtol, atol in ((64, 5e-15, 0.0), (32, 2e-6, 1e-30)):
+            F = torch.zeros(len(xs) * (M + 1), dtype=torch.float64, device="cuda")
+            _lib.check(gpu_lib.gs_boys_eval(M, prec, len(xs), _lib.ptr(xs), _lib.ptr(F),
+                                            _lib.stream()), "boys")
+            F = F.view(-1, M + 1).cpu().numpy()
+            assert np.all(np.abs(F - ex) <= atol + rtol * np.abs(ex)), (M, prec)
+
+
+@pytest.mark.parametrize("precision,rtol,atol", [(64, 1e-11, 1e-13), (32, 1e-4, 1e-8)])
+def test_synthetic_every_class(gpu_lib, precision, rtol, atol):
+    from gaussium_gb300 import engine
+    from gaussium_gb300.basis import ShellBasis
+    shells = synthetic_shells()
+    sb = ShellBasis.from_shell_dicts(shells)
+    table = oracle.FunctionTable.from_shells(shells)
+    g = golden("synthetic")
+    quartets = np.array([q for q in g["quartets"]
+                         if gpu_lib.gs_class_available(*sorted(sb.l[q][:2], reverse=True),
+                                                       *sorted(sb.l[q][2:], reverse=True))
+                         or gpu_lib.gs_class_available(*sorted(sb.l[q][2:], reverse=True),
+                                                       *sorted(sb.l[q][:2], reverse=True))])
+    out, off = engine.eri_blocks(sb, quartets, precision=precision)
+    for i, q in enumerate(quartets):
+        ref = oracle.eri_functions(table, hostcheck.function_quartets(sb, q), boys_mode=1)
+        got = out[off[i]:off[i + 1]]
+        assert np.max(np.abs(got - ref)) <= atol + rtol * np.max(np.abs(ref)), q
+
+
+def test_h2o_631gs_all_quartets_match_reference(gpu_lib):
+    """Every canonical function quartet of water/6-31G* against the as-is reference
+    (its Boys error bounds the difference) and the exact-Boys oracle (1e-13)."""
+    from gaussium_gb300.dropin import TwoElectronRepulsionMatrixGPU
+    g, funcs, table = load("h2o_631gs")
+    dense = TwoElectronRepulsionMatrixGPU(funcs, None, 1).create_repulsion_matrix()
+    keys = g["keys"].astype(np.int64)
+    got = dense[keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3]]
+    assert np.max(np.abs(got - g["eri"])) < 1e-10
+    exact = oracle.eri_functions(table, keys, boys_mode=1)
+    assert np.max(np.abs(got - exact)) < 1e-13
+    # 8-fold symmetry of the dense tensor
+    assert np.array_equal(dense, dense.transpose(1, 0, 2, 3))
+    assert np.array_equal(dense, dense.transpose(2, 3, 0, 1))
+
+
+def test_dense_tensor_h2o_sto3g(gpu_lib):
+    from gaussium_gb300.dropin import TwoElectronRepulsionMatrixOSGPU
+    g, funcs, _ = load("h2o_sto3g")
+    dense = TwoElectronRepulsionMatrixOSGPU(funcs, None, 4).create_repulsion_matrix()
+    assert np.max(np.abs(dense - g["dense"])) < 1e-10
+
+
+def test_integral_objects_reference_unit_quartets(gpu_lib):
+    """The reference's own ERI unit test (test_electron_repulsion_matrix.py) through the
+    drop-in integral objects, for all three scheme names."""
+    from types import SimpleNamespace as NS
+    from gaussium_gb300.dropin import GpuObaraSaika, GpuHeadGordonPople, GpuElectronRepulsion
+    g = golden("eri_heh")
+    he_r, h_r = (0, 0, 0.7316), (0, 0, -0.7316)
+
+    def fn(r, prims):
+        return NS(primitive_gaussian_array=[NS(contraction=c, exponent=a, coordinates=r,
+                                                integral_exponents=(0, 0, 0), normalisation=n)
+                                             for c, a, n in prims],
+                  coordinates=r, integral_exponents=(0, 0, 0), normalisation=1)
+    he = fn(he_r, [(0.15432897, 9.75393461, 3.9336432656254527),
+                   (0.53532814, 1.77669115, 1.0967787981767012),
+                   (0.44463454, 0.48084429, 0.41154131374122654)])
+    h = fn(h_r, [(0.15432897, 3.42525091, 1.794441832218435),
+                 (0.53532814, 0.62391373, 0.5003264923314032),
+                 (0.44463454, 0.16885540, 0.18773545851092535)])
+    basis = [he, h]
+    for cls, ref in ((GpuObaraSaika, g["os"]), (GpuHeadGordonPople, g["hgp"]),
+                     (GpuElectronRepulsion, g["cook"])):
+        obj = cls()
+        got = np.array([obj.integrate(*[basis[i] for i in k]) for k in g["keys"]])
+        assert np.max(np.abs(got - ref)) < 1e-10
+        for v, want in zip(got, g["test_values"]):
+            np.testing.assert_approx_equal(v, want, 4)
+
+
+def test_integral_object_p_and_d_functions(gpu_lib):
+    """Single-function calls with p and d components and arbitrary given normalisations."""
+    from gaussium_gb300.dropin import GpuObaraSaika
+    g, funcs, table = load("h2o_631gs")
+    rng = np.random.default_rng(3)
+    keys = rng.integers(0, len(funcs), size=(40, 4))
+    obj = GpuObaraSaika()
+    got = np.array([obj.integrate(*[funcs[i] for i in k]) for k in keys])
+    ref = oracle.eri_functions(table, keys, boys_mode=1)
+    assert np.max(np.abs(got - ref)) < 1e-13
+
+
+def test_empty_batch(gpu_lib):
+    from gaussium_gb300 import engine
+    from gaussium_gb300.basis import ShellBasis
+    sb = ShellBasis.from_shell_dicts(synthetic_shells()[:4])
+    out, off = engine.eri_blocks(sb, np.zeros((0, 4), dtype=np.int64))
+    assert len(off) == 1 and off[0] == 0
+
+
+def test_permuted_quartets_agree(gpu_lib):
+    from gaussium_gb300 import engine
+    from gaussium_gb300.basis import ShellBasis
+    shells = synthetic_shells()
+    sb = ShellBasis.from_shell_dicts(shells)
+    g = golden("synthetic")
+    q = [x for x in g["quartets"] if sum(sb.l[x]) <= 5][:12]
+    perms = [(0, 1, 2, 3), (1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1), (3, 2, 1, 0)]
+    allq = np.array([[x[p] for p in perm] for x in q for perm in perms])
+    out, off = engine.eri_blocks(sb, allq)
+    n = [[len(engine.COMPONENTS[int(sb.l[s])]) for s in x] for x in allq]
+    for i in range(len(q)):
+        base = out[off[5 * i]:off[5 * i + 1]].reshape(n[5 * i])
+        for j, perm in enumerate(perms):
+            blk = out[off[5 * i + j]:off[5 * i + j + 1]].reshape(n[5 * i + j])
+            np.testing.assert_allclose(blk, base.transpose(perm), rtol=0, atol=1e-15)

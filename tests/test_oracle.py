@@ -1,0 +1,89 @@
+"""The oracle (C restatement of the reference ERI path) against the golden vectors that
+tests/golden/make_golden.py produced by running the reference itself."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden, synthetic_shells
+
+
+def test_boys_reference_port_matches_reference():
+    g = golden("boys")
+    got = np.array([[oracle.boys_reference(v, x) for x in g["x"]] for v in g["v"]])
+    ref = g["reference"]
+    assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)) < 1e-13
+
+
+def test_boys_exact_matches_mpmath():
+    g = golden("boys")
+    got = np.array([[oracle.boys_exact(v, x) for x in g["x"]] for v in g["v"]])
+    assert np.max(np.abs(got - g["exact"]) / np.abs(g["exact"])) < 1e-14
+
+
+def test_reference_boys_error_is_the_known_one():
+    # the reference's series stops at a term < 1e-10 (boys_function.py:34,48)
+    g = golden("boys")
+    err = np.max(np.abs(g["reference"] - g["exact"]))
+    assert 1e-12 < err < 1e-10
+
+
+@pytest.mark.parametrize("memo", [True, False])
+def test_heh_unit_test_quartets(memo):
+    g = golden("eri_heh")
+    he_r, h_r = (0, 0, 0.7316), (0, 0, -0.7316)
+    he = [(0.15432897, 9.75393461, 3.9336432656254527), (0.53532814, 1.77669115, 1.0967787981767012),
+          (0.44463454, 0.48084429, 0.41154131374122654)]
+    h = [(0.15432897, 3.42525091, 1.794441832218435), (0.53532814, 0.62391373, 0.5003264923314032),
+         (0.44463454, 0.16885540, 0.18773545851092535)]
+    t = oracle.FunctionTable(np.array([he_r, h_r]), np.zeros((2, 3)), np.ones(2), [he, h])
+    got = oracle.eri_functions(t, g["keys"], boys_mode=0, memo=memo)
+    np.testing.assert_allclose(got, g["os"], rtol=0, atol=1e-15)
+    # the reference test file's own values, to its 4 significant figures
+    for v, want in zip(got, g["test_values"]):
+        np.testing.assert_approx_equal(v, want, 4)
+
+
+@pytest.mark.parametrize("name", ["h2o_sto3g", "h2o_631gs"])
+def test_molecule_eris_match_reference(name):
+    g = golden(name)
+    t = oracle.FunctionTable.from_arrays(g)
+    got = oracle.eri_functions(t, g["keys"], boys_mode=0)
+    assert np.max(np.abs(got - g["eri"])) < 1e-14
+    exact = oracle.eri_functions(t, g["keys"], boys_mode=1)
+    # exact-Boys oracle differs from the as-is reference by the reference's Boys error only
+    assert np.max(np.abs(exact - g["eri"])) < 1e-10
+
+
+def test_dense_tensor_and_fock_restatements():
+    g = golden("h2o_sto3g")
+    t = oracle.FunctionTable.from_arrays(g)
+    dense = oracle.dense_tensor(t, boys_mode=0)
+    assert np.max(np.abs(dense - g["dense"])) < 1e-14
+    eri = g["dense"]
+    pa, pb = g["density_a"], g["density_b"]
+    h = np.zeros_like(pa)
+    np.testing.assert_allclose(oracle.fock_restricted(h, eri, pa), g["fock_rhf"], atol=1e-13)
+    fa, fb = oracle.fock_unrestricted(h, eri, pa, pb)
+    np.testing.assert_allclose(fa, g["fock_uhf_a"], atol=1e-13)
+    np.testing.assert_allclose(fb, g["fock_uhf_b"], atol=1e-13)
+    np.testing.assert_allclose(oracle.coulomb(eri, pa), g["coulomb_ks"], atol=1e-13)
+
+
+def test_synthetic_quartets_and_normalisation():
+    g = golden("synthetic")
+    shells = synthetic_shells()
+    t = oracle.FunctionTable.from_shells(shells)
+    ncomp = [len(oracle.COMPONENTS[s["l"]]) for s in shells]
+    off = np.concatenate([[0], np.cumsum(ncomp)])
+    cn = np.concatenate([g["contracted_norm"][i, :ncomp[i]] for i in range(len(shells))])
+    np.testing.assert_allclose(t.cnorm, cn, rtol=1e-14)
+    q = g["quartets"][g["sample_quartet"]]
+    fq = np.array([[off[q[i, k]] + g["sample_comp"][i, k] for k in range(4)] for i in range(len(q))])
+    got = oracle.eri_functions(t, fq, boys_mode=0)
+    assert np.max(np.abs(got - g["os"])) < 1e-15
+    # HGP agrees with OS in the reference itself; Cook calls the (inexact) reference Boys
+    # series once per order instead of recursing down, so it differs by that error
+    m = ~np.isnan(g["hgp"])
+    assert np.max(np.abs(g["hgp"][m] - g["os"][m])) < 1e-15
+    m = ~np.isnan(g["cook"])
+    assert np.max(np.abs(g["cook"][m] - g["os"][m])) < 5e-9
