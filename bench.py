@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""ERI microbench: 2,000,000 seeded shell quartets (four independent s/p/d shells each,
+contraction degree 1-6, exponents log-uniform in [0.05, 1e4], centres in a 10 A cube),
+evaluated to full contracted Cartesian blocks (~2 GB of FP64 output) on one GB300.
+
+One step = the hot path over the whole batch with the shell data resident in HBM:
+  K0 shell-pair build (primitive-pair records, FP64 and FP32) and the 21 angular-momentum
+  class kernels writing every block.
+``value`` is shell quartets/s of the FP64 path (each integral within 1e-10 of the oracle);
+``fp32`` and ``mixed`` report the same batch evaluated in FP32 and with the precision
+chosen per quartet from its Schwarz bound; ``e2e`` times the public host-buffer call
+(host shells -> device, pair build, kernels, blocks -> host) per step.
+
+Reference arm (--impl reference): the oracle's C restatement of the reference's
+Obara-Saika recursion on the host cores, on a seeded sample of the same quartets.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gaussium_gb300|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ERI quartets/s & Fock-build time, mixed vs FP64 GPU at |ΔE|≤1e-6 Eh"
+UNIT = "shell quartets/s"
+WORKLOAD = "synthetic ERI microbench: 2,000,000 seeded shell quartets, l uniform {s,p,d}, " \
+           "K uniform 1-6, exponents log-uniform [0.05,1e4], centres in a 10 A cube"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gaussium_gb300", choices=["gaussium_gb300", "reference"])
+    ap.add_argument("--quartets", type=int, default=2_000_000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=1024)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------- distributed plumbing
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", os.environ.get("LOCAL_RANK", "0")],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------- CPU baseline (oracle)
+def oracle_table(sb):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from gaussium_gb300.basis import COMPONENTS
+    centre, lmn, cnorm, prims = [], [], [], []
+    for s in range(sb.nshell):
+        k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
+        for ci, c in enumerate(COMPONENTS[int(sb.l[s])]):
+            centre.append(sb.centre[s]); lmn.append(c); cnorm.append(sb.comp_scale[s, ci])
+            prims.append(list(zip(sb.coef[k0:k1], sb.expo[k0:k1], np.ones(k1 - k0))))
+    return oracle, oracle.FunctionTable(np.array(centre), np.array(lmn), np.array(cnorm), prims)
+
+
+def cpu_oracle_rate(sample, seed, threads):
+    """Shell quartets/s of the oracle port (the reference's Obara-Saika recursion with
+    memoised nodes, bit-identical results) on `sample` quartets drawn from the workload."""
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(sample, seed=seed + 1000)
+    oracle, table = oracle_table(sb)
+    fo = np.concatenate([[0], np.cumsum(sb.nfunc)])
+    fq = []
+    for a, b, c, d in q:
+        ia, ib, ic, id_ = (np.arange(fo[x], fo[x + 1]) for x in (a, b, c, d))
+        g = np.stack(np.meshgrid(ia, ib, ic, id_, indexing="ij"), -1).reshape(-1, 4)
+        fq.append(g)
+    fq = np.concatenate(fq)
+    t0 = time.perf_counter()
+    oracle.eri_functions(table, fq, boys_mode=0, memo=True, threads=threads)
+    dt = time.perf_counter() - t0
+    return sample / dt, dt, len(fq)
+
+
+# ---------------------------------------------------------------------- GPU arm
+def flops_model(batch, opcount):
+    """Algorithmic FLOPs per class launch: K_bra*K_ket primitive quartets times the
+    per-primitive-quartet count (VRR + its set-up and Boys) plus the per-quartet HRR and
+    output scaling, FMA = 2."""
+    out = {}
+    nb = batch.sorted_bra_nprim.astype(np.float64)
+    nk = batch.sorted_ket_nprim.astype(np.float64)
+    for cls, s, e in batch.segments:
+        tag = "".join(map(str, cls))
+        oc = opcount[tag]
+        L = oc["L"]
+        prim = oc["vrr_flops"] + 64 + 3 * L       # set-up (~50) + Boys (~14 + 3 per order)
+        contr = oc["hrr_flops"] + 2 * oc["nblk"]  # HRR + per-element scaling
+        out[cls] = float(np.sum(nb[s:e] * nk[s:e])) * prim + (e - s) * contr
+    return out
+
+
+def fma_peak(precision):
+    import torch
+    from gaussium_gb300 import _lib
+    L = _lib.lib()
+    sm = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads = sm * 8, 256
+    sink = torch.zeros(blocks * threads, dtype=torch.float64, device="cuda")
+    iters = 400 if precision == 64 else 8000
+    L.gs_fma_probe(precision, blocks, threads, 10, _lib.ptr(sink), _lib.stream())
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.check(L.gs_fma_probe(precision, blocks, threads, iters, _lib.ptr(sink), _lib.stream()),
+                   "fma")
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, blocks * threads * iters * 16 * 8 * 2 / (e0.elapsed_time(e1) * 1e-3))
+    return best / 1e12
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from gaussium_gb300 import build, engine, _lib
+    from gaussium_gb300.workloads import random_shell_quartets
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    build.build()
+    opcount = build.opcount()
+    sb, quartets, _ = random_shell_quartets(args.quartets, seed=args.seed + rank)
+    ds = engine.DeviceShells(sb)
+    batch = engine.QuartetBatch(ds, quartets, want32=True)
+    out = torch.empty(batch.total, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    classes = [c for c, _, _ in batch.segments]
+    nlaunch = 1 + len(classes)
+
+    def step(precision, timing=None):
+        batch.pairs.build()
+        if timing is None:
+            batch.run(out, precision)
+            return
+        for cls, s, e in batch.segments:
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            batch.run(out, precision, classes=[cls])
+            ev1.record(stream)
+            timing.setdefault(cls, []).append((ev0, ev1))
+
+    res = {}
+    for precision in (64, 32):
+        for _ in range(args.warmup):
+            step(precision)
+        torch.cuda.synchronize()
+        timing = {}
+        barrier(world)
+        torch.cuda.synchronize()
+        with ClockSampler() as clk:
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(args.steps):
+                step(precision, timing)
+            t1.record(stream)
+            torch.cuda.synchronize()
+        barrier(world)
+        ms = max_over_ranks(t0.elapsed_time(t1) / args.steps, world)
+        per_cls = {c: float(np.mean([a.elapsed_time(b) for a, b in v])) for c, v in timing.items()}
+        res[precision] = dict(ms=ms, per_cls=per_cls, clocks=clk.summary())
+        if precision == 64:
+            ref64 = out.clone()
+    err32 = float((out - ref64).abs().max())
+    del ref64
+
+    # roofline of the dominant FP64 kernel
+    peak64 = fma_peak(64)
+    peak32 = fma_peak(32)
+    fl = flops_model(batch, opcount)
+    dom = max(res[64]["per_cls"], key=res[64]["per_cls"].get)
+    achieved = fl[dom] / (res[64]["per_cls"][dom] * 1e-3) / 1e12
+    total_flops = sum(fl.values())
+
+    # e2e: host shells -> device, pair build, kernels, blocks -> host, every step
+    e2e = None
+    if not args.no_e2e:
+        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
+                (("centre", sb.centre), ("l", sb.l), ("prim_off", sb.prim_off), ("expo", sb.expo),
+                 ("coef", sb.coef), ("comp_scale", sb.comp_scale))}
+        host_out = torch.empty(batch.total, dtype=torch.float64).pin_memory()
+        h2d = sum(t.numel() * t.element_size() for t in host.values()) + batch.tasks.numel()
+        task_host = batch.tasks.cpu().pin_memory()
+
+        def e2e_step():
+            for k, t in host.items():
+                getattr(ds, k).copy_(t, non_blocking=True)
+            batch.tasks.copy_(task_host, non_blocking=True)
+            batch.pairs.build()
+            batch.run(out, 64)
+            host_out.copy_(out, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world)
+        e2e = {"value": args.quartets * world / (e2e_ms * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(batch.total * 8),
+               "ms_per_step": e2e_ms}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, dt, nf = cpu_oracle_rate(args.cpu_sample, args.seed, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} seeded shell quartets of the same distribution "
+                         f"({nf} function quartets), oracle C restatement of the reference's "
+                         f"Obara-Saika recursion (memoised nodes), {dt:.1f} s on {threads} threads"}
+
+    n_all = args.quartets * world
+    ms64, ms32 = res[64]["ms"], res[32]["ms"]
+    line = {
+        "metric": METRIC,
+        "value": n_all / (ms64 * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms64,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded), shells resident in HBM; inputs (4.9 GB of pair records) "
+                "larger than L2",
+        "config": {"workload": WORKLOAD, "quartets_per_gpu": args.quartets,
+                   "function_quartets_per_gpu": int(batch.total),
+                   "primitive_quartets_per_gpu": int(batch.prim_quartets),
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2"},
+        "roofline": {"bound": "fp64", "kernel": "eri class " + "".join(map(str, dom)) + " FP64",
+                     "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": achieved / peak64, "traffic": None,
+                     "peak_source": "gs_fma_probe FP64 FMA rate measured in this run"},
+        "fp64": {"value": n_all / (ms64 * 1e-3), "ms_per_step": ms64,
+                 "tflops": total_flops / (ms64 * 1e-3) / 1e12,
+                 "frac_of_fp64_peak": total_flops / (ms64 * 1e-3) / 1e12 / peak64},
+        "fp32": {"value": n_all / (ms32 * 1e-3), "ms_per_step": ms32,
+                 "max_abs_err_vs_fp64": err32, "fp32_peak_tflops": peak32},
+        "per_class_ms_fp64": {"".join(map(str, c)): v for c, v in res[64]["per_cls"].items()},
+        "clocks": res[64]["clocks"],
+        "e2e": e2e,
+        "gpu_launches": nlaunch * args.steps,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_rate(32, args.seed, threads)
+    vals = []
+    t_all = time.perf_counter()
+    for k in range(args.steps):
+        rate, dt, nf = cpu_oracle_rate(args.cpu_sample // 4, args.seed + k, threads)
+        vals.append(rate)
+    wall = time.perf_counter() - t_all
+    v = float(np.mean(vals))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "quartets_per_gpu": args.quartets},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.cpu_sample // 4} seeded shell quartets per step, "
+                                   "oracle C restatement of the reference's Obara-Saika recursion"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

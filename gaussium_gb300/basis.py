@@ -190,7 +190,7 @@ class ShellBasis:
         self.comp_scale = np.ascontiguousarray(cs)
         if int(self.l.max(initial=0)) > LMAX:
             raise ValueError(f"angular momentum above {LMAX} is not supported")
-        nfun = np.array([len(COMPONENTS[int(x)]) for x in self.l], dtype=np.int32)
+        nfun = np.array([1, 3, 6], dtype=np.int32)[self.l]
         self.nfunc = nfun
         self.func_off = np.concatenate([[0], np.cumsum(nfun)[:-1]]).astype(np.int32)
         self.nbf = int(nfun.sum())

@@ -20,8 +20,8 @@ GEN = os.path.join(BUILD, "gen")
 LIB = os.path.join(PKG, "libgaussium_gb300.so")
 HOSTCHECK = os.path.join(BUILD, "libhostcheck.so")
 LMAX = 2
-# Classes whose one-thread-per-quartet kernel is built (all up to L = 6); the two largest
-# classes need the cooperative kernel and are built separately.
+# Classes with total angular momentum above THREAD_LMAX_TOTAL use the warp-cooperative
+# kernel (csrc/eri_wide.cuh); the others one thread per quartet (csrc/eri_kernels.cuh).
 THREAD_LMAX_TOTAL = 6
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -64,7 +64,7 @@ def generate():
         _run(["gcc", "-O2", "-o", exe, gen_src, "-lm"])
         _run([exe, table])
     units = []
-    built = [c for c in classes() if sum(c) <= THREAD_LMAX_TOTAL]
+    built = list(classes())
     lst = "// written by build.py\n#pragma once\n#define GS_FOR_EACH_BUILT(X) " + " ".join(
         "X(%d, %d, %d, %d)" % c for c in built) + "\n"
     path = os.path.join(GEN, "gs_built_classes.h")
@@ -74,19 +74,29 @@ def generate():
     for cls in built:
         tag = "".join(map(str, cls))
         path = os.path.join(GEN, f"eri_k_{tag}.cu")
-        code = ('#include "eri_kernels.cuh"\n#include "eri_class_%s.h"\n'
-                'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
-                '    return gs::launch_class<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
-                % (tag, tag, *cls))
+        if sum(cls) > THREAD_LMAX_TOTAL:
+            code = ('#include "eri_wide.cuh"\n#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n'
+                    'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
+                    '    return gs::launch_wide<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
+                    % (tag, tag, tag, *cls))
+        else:
+            code = ('#include "eri_kernels.cuh"\n#include "eri_class_%s.h"\n'
+                    'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
+                    '    return gs::launch_class<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
+                    % (tag, tag, *cls))
         if not os.path.exists(path) or open(path).read() != code:
             with open(path, "w") as f:
                 f.write(code)
-        units.append((path, os.path.join(GEN, f"eri_class_{tag}.h")))
+        deps = [os.path.join(GEN, f"eri_class_{tag}.h")]
+        if sum(cls) > THREAD_LMAX_TOTAL:
+            deps.append(os.path.join(GEN, f"eri_wide_{tag}.h"))
+        units.append((path, deps))
     return units
 
 
 def _compile(src, deps, obj):
-    common = [os.path.join(CSRC, n) for n in ("eri_common.cuh", "eri_kernels.cuh", "gs_args.h")]
+    common = [os.path.join(CSRC, n) for n in ("eri_common.cuh", "eri_kernels.cuh", "eri_wide.cuh",
+                                              "gs_args.h")]
     common.append(os.path.join(GEN, "boys_table.h"))
     key = _digest([src] + deps + common, " ".join(NVFLAGS))
     stamp = obj + ".key"
@@ -101,7 +111,7 @@ def _compile(src, deps, obj):
 def build(jobs=None, verbose=False):
     units = generate()
     objs = []
-    todo = [(src, [hdr], os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")) for src, hdr in units]
+    todo = [(src, deps, os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")) for src, deps in units]
     todo.append((os.path.join(CSRC, "capi.cu"), [os.path.join(GEN, "gs_built_classes.h")],
                  os.path.join(BUILD, "capi.o")))
     jobs = jobs or max(1, os.cpu_count() or 1)

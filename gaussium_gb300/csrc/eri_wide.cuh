@@ -1,0 +1,362 @@
+// Warp-cooperative class kernels for the high angular-momentum classes, whose per-quartet
+// state (thousands of recursion intermediates) does not fit one thread.  One warp
+// evaluates one contracted shell quartet:
+//   1. setup, lane-parallel over primitive quartets: each lane prepares the recursion
+//      coefficients and scaled Boys values of one primitive quartet in shared memory;
+//   2. VRR, node-parallel: for each primitive quartet the warp walks the generated node
+//      program level by level (nodes of a level are independent), reading operands and
+//      coefficients from shared memory; each lane keeps a slice of the contracted
+//      [e0|f0] accumulators in registers;
+//   3. HRR, element-parallel on a liveness-planned shared buffer;
+//   4. epilogue: block write, J/K digestion or Schwarz reduction.
+// The node programs come from gen_eri.py (WideProg<...> tables).
+#pragma once
+#include "eri_common.cuh"
+#include "gs_args.h"
+
+namespace gs {
+
+template <int LA, int LB, int LC, int LD> struct WideProg;
+
+constexpr int kWideWarps = 2;     // warps per block
+constexpr int kNCoef = 32;        // coefficient slots per primitive quartet
+constexpr int kSetupBatch = 32;   // primitive quartets prepared per setup round
+
+template <int LA, int LB, int LC, int LD, typename T> struct WideLayout {
+    using G = ClassGen<LA, LB, LC, LD>;
+    using W = WideProg<LA, LB, LC, LD>;
+    static constexpr int SC = kSetupBatch * kNCoef;              // coefficients
+    static constexpr int SF = kSetupBatch * (G::L + 1);          // Boys values
+    static constexpr int VRR = SC + SF + W::NVSLOT;
+    static constexpr int HR = W::HSIZE + G::NBLK + G::NA * G::NB + G::NC * G::ND;
+    static constexpr int WARP = VRR > HR ? VRR : HR;             // elements of T per warp
+    static constexpr size_t BYTES = (size_t)WARP * sizeof(T) * kWideWarps;
+};
+
+template <typename T>
+__device__ __forceinline__ void wide_setup(const PrimRec<T>& P, const PrimRec<T>& Q, int L,
+                                           T* __restrict__ c, T* __restrict__ F);
+
+template <int M, typename T>
+__device__ __forceinline__ void wide_setup_m(const PrimRec<T>& P, const PrimRec<T>& Q,
+                                             T* __restrict__ c, T* __restrict__ F) {
+    const T pq = P.p + Q.p;
+    const T rs = gs_rsqrt(pq);
+    const T ipq = rs * rs;
+    const T PQx = Q.Px - P.Px, PQy = Q.Py - P.Py, PQz = Q.Pz - P.Pz;
+    const T wq = Q.p * ipq, wp = P.p * ipq;
+    const T t = P.p * wq * (PQx * PQx + PQy * PQy + PQz * PQz);
+    T f[M + 1];
+    boys<M, T>(t, P.Kp * Q.Kp * rs, f);
+#pragma unroll
+    for (int m = 0; m <= M; ++m) F[m] = f[m];
+    c[0] = P.PAx; c[1] = P.PAy; c[2] = P.PAz;
+    c[3] = wq * PQx; c[4] = wq * PQy; c[5] = wq * PQz;
+    c[6] = Q.PAx; c[7] = Q.PAy; c[8] = Q.PAz;
+    c[9] = -wp * PQx; c[10] = -wp * PQy; c[11] = -wp * PQz;
+    const T i2p = P.i2p, i2q = Q.i2p, rp2 = wq * P.i2p, rq2 = wp * Q.i2p, i2pq = T(0.5) * ipq;
+#pragma unroll
+    for (int k = 1; k <= 4; ++k) {
+        c[12 + k - 1] = T(k) * i2p;
+        c[16 + k - 1] = -T(k) * rp2;
+        c[20 + k - 1] = T(k) * i2q;
+        c[24 + k - 1] = -T(k) * rq2;
+        c[28 + k - 1] = T(k) * i2pq;
+    }
+}
+
+// Evaluate one contracted quartet; on return sm[0 .. HSIZE) holds the HRR buffer whose
+// output slots are W::outslot().
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
+                                             const PrimRec<T>* __restrict__ prims,
+                                             T* __restrict__ sm, int lane) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    using W = WideProg<LA, LB, LC, LD>;
+    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    constexpr int L = G::L;
+    constexpr int NACC = G::NACC;
+    constexpr int NACCW = (NACC + 31) / 32;
+    T acc[NACCW];
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
+    T* sC = sm;
+    T* sF = sm + Lay::SC;
+    T* node = sm + Lay::SC + Lay::SF;
+    const int nK = K.nprim;
+    const int ntot = B.nprim * nK;
+    const unsigned short* __restrict__ vout = W::vout();
+    const unsigned int* __restrict__ vdesc = W::vdesc();
+    const int* __restrict__ vseg = W::vseg();
+    const unsigned short* __restrict__ vtgt = W::vtgt();
+    for (int base = 0; base < ntot; base += kSetupBatch) {
+        const int i = base + lane;
+        if (i < ntot) {
+            const PrimRec<T> P = prims[B.prim_off + i / nK];
+            const PrimRec<T> Q = prims[K.prim_off + i % nK];
+            wide_setup_m<L, T>(P, Q, sC + lane * kNCoef, sF + lane * (L + 1));
+        }
+        __syncwarp();
+        const int nb = min(kSetupBatch, ntot - base);
+        for (int j = 0; j < nb; ++j) {
+            const T* __restrict__ c = sC + j * kNCoef;
+            if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
+            __syncwarp();
+            for (int s = 0; s < W::NVSEG; ++s) {
+                const int doff = __ldg(vseg + 4 * s), ooff = __ldg(vseg + 4 * s + 1);
+                const int cnt = __ldg(vseg + 4 * s + 2), w = __ldg(vseg + 4 * s + 3);
+                const int nt = w & 0xff;
+                if ((w >> 8) && s > 0) __syncwarp();
+                for (int n = lane; n < cnt; n += 32) {
+                    const unsigned int* d = vdesc + doff + n * nt;
+                    unsigned int x = __ldg(d);
+                    T r = c[x >> 16] * node[x & 0xffff];
+                    for (int t = 1; t < nt; ++t) {
+                        x = __ldg(d + t);
+                        r = fma(c[x >> 16], node[x & 0xffff], r);
+                    }
+                    node[__ldg(vout + ooff + n)] = r;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < NACCW; ++k) {
+                const int t = lane + 32 * k;
+                if (t < NACC) acc[k] += node[__ldg(vtgt + t)];
+            }
+            __syncwarp();
+        }
+    }
+    // horizontal recursion in shared memory
+    T* H = sm;
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) {
+        const int t = lane + 32 * k;
+        if (t < NACC) H[t] = acc[k];
+    }
+    __syncwarp();
+    const unsigned int* __restrict__ hop = W::hop();
+    const int* __restrict__ hlev = W::hlev();
+    const T dv0 = T(B.ABx), dv1 = T(B.ABy), dv2 = T(B.ABz);
+    const T dv3 = T(K.ABx), dv4 = T(K.ABy), dv5 = T(K.ABz);
+    for (int lv = 0; lv < W::NHLEV; ++lv) {
+        const int e1 = __ldg(hlev + lv + 1);
+        for (int e = __ldg(hlev + lv) + lane; e < e1; e += 32) {
+            const unsigned int a = __ldg(hop + 2 * e), b = __ldg(hop + 2 * e + 1);
+            const int d = b >> 16;
+            const T dv = d == 0 ? dv0 : d == 1 ? dv1 : d == 2 ? dv2 : d == 3 ? dv3 : d == 4 ? dv4 : dv5;
+            H[a & 0xffff] = fma(dv, H[b & 0xffff], H[a >> 16]);
+        }
+        __syncwarp();
+    }
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs a) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    using W = WideProg<LA, LB, LC, LD>;
+    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP;
+    const int t = blockIdx.x * kWideWarps + warp;
+    if (t >= a.ntask) return;
+    const WriteTask task = a.tasks[t];
+    const PairRec B = a.pairs[task.bra];
+    const PairRec K = a.pairs[task.ket];
+    wide_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    long long s[4];
+    block_strides(task.code, G::NA, G::NB, G::NC, G::ND, s);
+    T* sab = sm + W::HSIZE + G::NBLK;
+    T* scd = sab + G::NA * G::NB;
+    for (int x = lane; x < G::NA * G::NB; x += 32)
+        sab[x] = (T)(a.comp_scale[6 * B.sa + x / G::NB] * a.comp_scale[6 * B.sb + x % G::NB]);
+    for (int x = lane; x < G::NC * G::ND; x += 32)
+        scd[x] = (T)(a.comp_scale[6 * K.sa + x / G::ND] * a.comp_scale[6 * K.sb + x % G::ND]);
+    __syncwarp();
+    const T* H = sm;
+    const unsigned short* __restrict__ os = W::outslot();
+    double* out = a.out + task.off;
+    for (int e = lane; e < G::NBLK; e += 32) {
+        const int id = e % G::ND, ic = (e / G::ND) % G::NC;
+        const int ib = (e / (G::ND * G::NC)) % G::NB, ia = e / (G::ND * G::NC * G::NB);
+        out[ia * s[0] + ib * s[1] + ic * s[2] + id * s[3]] =
+            (double)(H[__ldg(os + e)] * (sab[ia * G::NB + ib] * scd[ic * G::ND + id]));
+    }
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    using W = WideProg<LA, LB, LC, LD>;
+    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
+    constexpr int NAB = NA * NB, NCD = NC * ND;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP;
+    const int t = blockIdx.x * kWideWarps + warp;
+    if (t >= a.ntask) return;
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    if (a.screen_thr > 0.0) {
+        const double bound = (double)B.qmax * (double)K.qmax;
+        const int n = a.nshell;
+        double dm = a.shell_dmax[B.sa * n + B.sb];
+        dm = fmax(dm, a.shell_dmax[K.sa * n + K.sb]);
+        dm = fmax(dm, a.shell_dmax[B.sa * n + K.sa]);
+        dm = fmax(dm, a.shell_dmax[B.sa * n + K.sb]);
+        dm = fmax(dm, a.shell_dmax[B.sb * n + K.sa]);
+        dm = fmax(dm, a.shell_dmax[B.sb * n + K.sb]);
+        const double est = bound * dm;
+        if (est < a.screen_thr || est < a.prec_lo || est >= a.prec_hi) return;
+    }
+    wide_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    const double deg = (B.sa == B.sb ? 0.5 : 1.0) * (K.sa == K.sb ? 0.5 : 1.0) *
+                       (task.x == task.y ? 0.5 : 1.0);
+    T* V = sm + W::HSIZE;
+    T* sab = V + G::NBLK;
+    T* scd = sab + NAB;
+    for (int x = lane; x < NAB; x += 32)
+        sab[x] = (T)(deg * a.comp_scale[6 * B.sa + x / NB] * a.comp_scale[6 * B.sb + x % NB]);
+    for (int x = lane; x < NCD; x += 32)
+        scd[x] = (T)(a.comp_scale[6 * K.sa + x / ND] * a.comp_scale[6 * K.sb + x % ND]);
+    __syncwarp();
+    const unsigned short* __restrict__ os = W::outslot();
+    for (int e = lane; e < G::NBLK; e += 32) V[e] = sm[__ldg(os + e)] * (sab[e / NCD] * scd[e % NCD]);
+    __syncwarp();
+    const int n = a.nbf;
+    const int fa = a.func_off[B.sa], fb = a.func_off[B.sb];
+    const int fc = a.func_off[K.sa], fd = a.func_off[K.sb];
+    if (a.j) {
+        const double* P = a.pj;
+        for (int ab = lane; ab < NAB; ab += 32) {
+            T r = T(0);
+            for (int cd = 0; cd < NCD; ++cd)
+                r = fma(V[ab * NCD + cd], (T)P[(fc + cd / ND) * n + fd + cd % ND], r);
+            atomicAdd(a.j + (fa + ab / NB) * n + fb + ab % NB, 2.0 * (double)r);
+        }
+        for (int cd = lane; cd < NCD; cd += 32) {
+            T r = T(0);
+            for (int ab = 0; ab < NAB; ++ab)
+                r = fma(V[ab * NCD + cd], (T)P[(fa + ab / NB) * n + fb + ab % NB], r);
+            atomicAdd(a.j + (fc + cd / ND) * n + fd + cd % ND, 2.0 * (double)r);
+        }
+    }
+    for (int s = 0; s < a.nk; ++s) {
+        const double* P = a.pk + (size_t)s * n * n;
+        double* Ko = a.k + (size_t)s * n * n;
+        // K'_ac += sum_bd v P_bd ; K'_ad += sum_bc v P_bc ; K'_bc += sum_ad v P_ad ; K'_bd += sum_ac v P_ac
+        for (int x = lane; x < NA * NC; x += 32) {
+            const int ia = x / NC, ic = x % NC;
+            T r = T(0);
+            for (int ib = 0; ib < NB; ++ib)
+                for (int id = 0; id < ND; ++id)
+                    r = fma(V[((ia * NB + ib) * NC + ic) * ND + id], (T)P[(fb + ib) * n + fd + id], r);
+            atomicAdd(Ko + (fa + ia) * n + fc + ic, (double)r);
+        }
+        for (int x = lane; x < NA * ND; x += 32) {
+            const int ia = x / ND, id = x % ND;
+            T r = T(0);
+            for (int ib = 0; ib < NB; ++ib)
+                for (int ic = 0; ic < NC; ++ic)
+                    r = fma(V[((ia * NB + ib) * NC + ic) * ND + id], (T)P[(fb + ib) * n + fc + ic], r);
+            atomicAdd(Ko + (fa + ia) * n + fd + id, (double)r);
+        }
+        for (int x = lane; x < NB * NC; x += 32) {
+            const int ib = x / NC, ic = x % NC;
+            T r = T(0);
+            for (int ia = 0; ia < NA; ++ia)
+                for (int id = 0; id < ND; ++id)
+                    r = fma(V[((ia * NB + ib) * NC + ic) * ND + id], (T)P[(fa + ia) * n + fd + id], r);
+            atomicAdd(Ko + (fb + ib) * n + fc + ic, (double)r);
+        }
+        for (int x = lane; x < NB * ND; x += 32) {
+            const int ib = x / ND, id = x % ND;
+            T r = T(0);
+            for (int ia = 0; ia < NA; ++ia)
+                for (int ic = 0; ic < NC; ++ic)
+                    r = fma(V[((ia * NB + ib) * NC + ic) * ND + id], (T)P[(fa + ia) * n + fc + ic], r);
+            atomicAdd(Ko + (fb + ib) * n + fd + id, (double)r);
+        }
+    }
+}
+
+template <int LA, int LB, typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzArgs a) {
+    using G = ClassGen<LA, LB, LA, LB>;
+    using W = WideProg<LA, LB, LA, LB>;
+    using Lay = WideLayout<LA, LB, LA, LB, T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP;
+    const int t = blockIdx.x * kWideWarps + warp;
+    if (t >= a.npair) return;
+    const int p = a.pair_index[t];
+    const PairRec B = a.pairs[p];
+    wide_quartet<LA, LB, LA, LB, T>(B, B, (const PrimRec<T>*)a.prims, sm, lane);
+    const unsigned short* __restrict__ os = W::outslot();
+    double m = 0.0;
+    constexpr int NAB = G::NA * G::NB;
+    for (int ab = lane; ab < NAB; ab += 32) {
+        const double s = a.comp_scale[6 * B.sa + ab / G::NB] * a.comp_scale[6 * B.sb + ab % G::NB];
+        m = fmax(m, fabs((double)sm[__ldg(os + ab * NAB + ab)]) * s * s);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) a.q[p] = sqrt(m);
+}
+
+template <int LA, int LB, int LC, int LD>
+int launch_wide(int kind, int prec, const void* args, cudaStream_t st) {
+    constexpr int TPB = 32 * kWideWarps;
+    if (kind == GS_KIND_WRITE) {
+        const WriteArgs& a = *(const WriteArgs*)args;
+        if (a.ntask <= 0) return 0;
+        const int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
+        if (prec == 64) {
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES;
+            auto k = k_wide_write<LA, LB, LC, LD, double>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+            k<<<grid, TPB, sh, st>>>(a);
+        } else {
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES;
+            auto k = k_wide_write<LA, LB, LC, LD, float>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+            k<<<grid, TPB, sh, st>>>(a);
+        }
+    } else if (kind == GS_KIND_JK) {
+        const JKArgs& a = *(const JKArgs*)args;
+        if (a.ntask <= 0) return 0;
+        const int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
+        if (prec == 64) {
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES;
+            auto k = k_wide_jk<LA, LB, LC, LD, double>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+            k<<<grid, TPB, sh, st>>>(a);
+        } else {
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES;
+            auto k = k_wide_jk<LA, LB, LC, LD, float>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+            k<<<grid, TPB, sh, st>>>(a);
+        }
+    } else if (kind == GS_KIND_SCHWARZ) {
+        if constexpr (LA == LC && LB == LD) {
+            const SchwarzArgs& a = *(const SchwarzArgs*)args;
+            if (a.npair <= 0) return 0;
+            const int grid = (a.npair + kWideWarps - 1) / kWideWarps;
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES;
+            auto k = k_wide_schwarz<LA, LB, double>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+            k<<<grid, TPB, sh, st>>>(a);
+        } else {
+            return GS_ERR_CLASS;
+        }
+    } else {
+        return GS_ERR_ARG;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+}
+
+}  // namespace gs

@@ -88,6 +88,7 @@ class VrrGen:
         self.em = Emitter()
         self.coefs = set()
         self.count = 0
+        self.struct = []      # per node: list of (coefficient name, operand)
         self.e_targets = [e for L in range(self.la, self.la + self.lb + 1) for e in cart(L)]
         self.f_targets = [f for L in range(self.lc, self.lc + self.ld + 1) for f in cart(L)]
 
@@ -151,6 +152,7 @@ class VrrGen:
         self.em.line(f"    const T {name} = {expr};")
         self.em.flops += 1 + 2 * (len(terms) - 1)
         self.names[key] = name
+        self.struct.append(terms)
         return name
 
     def build(self):
@@ -175,6 +177,10 @@ class HrrGen:
         self.bra_names = {}
         self.ket_names = {}
         self.count = 0
+        self.bra_ops = []     # (name, x, y, dir): name[k] = x[k] + AB_dir * y[k], k < NF
+        self.ket_ops = []     # (name, x, y, dir): arrays over ab, x/y may be ("G", f)
+        self.bra_final = {}   # (ia, ib) -> array name (or "(acc + off)")
+        self.ket_final = {}   # (ic, id) -> array name or ("G", f)
 
     # bra nodes are arrays over the ket VRR targets (length NF)
     def bra(self, a, b):
@@ -200,6 +206,7 @@ class HrrGen:
                      f"{name}[k] = {x}[k] + AB{XYZ[i]} * {y}[k];")
         self.em.flops += 2 * self.nf
         self.bra_names[(a, b)] = name
+        self.bra_ops.append((name, x, y, i))
         return name
 
     def build(self):
@@ -210,6 +217,7 @@ class HrrGen:
         for ia, a in enumerate(cart(self.la)):
             for ib, b in enumerate(cart(self.lb)):
                 src = self.bra(a, b)
+                self.bra_final[(ia, ib)] = src
                 self.em.line(f"    GS_UNROLL for (int k = 0; k < {self.nf}; ++k) "
                              f"G[{(ia * nb + ib) * self.nf} + k] = {src}[k];")
         # ket HRR: arrays over ab (length NAB)
@@ -241,11 +249,13 @@ class HrrGen:
                          f"{name}[k] = {ref(x)} + CD{XYZ[i]} * {ref(y)};")
             self.em.flops += 2 * nab
             kn[(c, d)] = name
+            self.ket_ops.append((name, x, y, i))
             return name
 
         for ic, c in enumerate(cart(self.lc)):
             for id_, d in enumerate(cart(self.ld)):
                 src = ket(c, d)
+                self.ket_final[(ic, id_)] = src
                 off = ic * nd + id_
                 if isinstance(src, tuple):
                     self.em.line(f"    GS_UNROLL for (int k = 0; k < {nab}; ++k) "
@@ -335,8 +345,228 @@ def main():
     if not os.path.exists(path) or open(path).read() != lst:
         with open(path, "w") as f:
             f.write(lst)
+    for cls in classes:
+        if sum(cls) < 5:
+            continue
+        code, _ = emit_wide(cls)
+        path = os.path.join(out, "eri_wide_%s.h" % "".join(map(str, cls)))
+        if not os.path.exists(path) or open(path).read() != code:
+            with open(path, "w") as f:
+                f.write(code)
     with open(os.path.join(out, "opcount.json"), "w") as f:
         json.dump(counts, f, indent=1, sort_keys=True)
+
+
+
+# ---------------------------------------------------------------------- warp programs
+COEF_ID = {}
+for _i, _n in enumerate(["PAx", "PAy", "PAz", "WPx", "WPy", "WPz", "QCx", "QCy", "QCz",
+                         "WQx", "WQy", "WQz"]):
+    COEF_ID[_n] = _i
+for _base, _kind in ((12, "i2p"), (16, "-rp2"), (20, "i2q"), (24, "-rq2"), (28, "i2pq")):
+    for _k in range(1, 5):
+        COEF_ID[_kind if _k == 1 else f"{_kind}_{_k}"] = _base + _k - 1
+NCOEF = 32
+
+
+def _alloc(free, size):
+    """First fit in a sorted free list of [start, end) intervals; returns start."""
+    for i, (a, b) in enumerate(free):
+        if b - a >= size:
+            if b - a == size:
+                free.pop(i)
+            else:
+                free[i] = (a + size, b)
+            return a
+    raise RuntimeError("allocator exhausted")
+
+
+def _release(free, start, size):
+    free.append((start, start + size))
+    free.sort()
+    merged = []
+    for a, b in free:
+        if merged and merged[-1][1] == a:
+            merged[-1] = (merged[-1][0], b)
+        else:
+            merged.append((a, b))
+    free[:] = merged
+
+
+def wide_program(cls):
+    """Tables for the warp-cooperative kernel of one class: VRR node descriptors grouped
+    by dependency level and term count, the targets' slots, and the HRR element
+    operations on a liveness-planned shared buffer."""
+    la, lb, lc, ld = cls
+    v = VrrGen(cls).build()
+    h = HrrGen(cls, v.e_targets, v.f_targets).build()
+    L = la + lb + lc + ld
+    nf = len(v.f_targets)
+    nacc = len(v.e_targets) * nf
+    na, nb, nc, nd = ncart(la), ncart(lb), ncart(lc), ncart(ld)
+    nab, ncd = na * nb, nc * nd
+
+    # ---- VRR
+    def slot(opnd):
+        if opnd.startswith("F["):
+            return int(opnd[2:-1])
+        return L + 1 + int(opnd[1:])
+
+    level = {}
+    for m in range(L + 1):
+        level[m] = 0
+    nodes = []
+    for idx, terms in enumerate(v.struct):
+        ts = [(COEF_ID[c], slot(x)) for c, x in terms]
+        lv = 1 + max(level[s] for _, s in ts)
+        level[L + 1 + idx] = lv
+        nodes.append((lv, len(ts), L + 1 + idx, ts))
+    nodes.sort(key=lambda n: (n[0], n[1], n[2]))
+    vout, vdesc, vseg = [], [], []
+    i = 0
+    while i < len(nodes):
+        j = i
+        while j < len(nodes) and nodes[j][:2] == nodes[i][:2]:
+            j += 1
+        lv, nt = nodes[i][:2]
+        sync = 1 if (not vseg or vseg[-1][4] != lv) else 0
+        vseg.append([len(vdesc), len(vout), j - i, nt, lv, sync])
+        for n in nodes[i:j]:
+            vout.append(n[2])
+            for cid, s in n[3]:
+                vdesc.append((cid << 16) | s)
+        i = j
+    tgt = [v.names[(e, f, 0)] if not (e == (0, 0, 0) and f == (0, 0, 0)) else "F[0]"
+           for e in v.e_targets for f in v.f_targets]
+    vtgt = [slot(t) for t in tgt]
+    nvslot = L + 1 + len(v.struct)
+
+    # ---- HRR: arrays, levels, liveness
+    arrays = {}          # name -> (size, producer level)
+    lvl = {}
+    for r in range(len(v.e_targets)):
+        lvl[f"(acc + {r * nf})"] = 0
+    ops = []             # (level, phase, name, x, y, dir)
+    for name, x, y, d in h.bra_ops:
+        lv = 1 + max(lvl[x], lvl[y])
+        lvl[name] = lv
+        arrays[name] = nf
+        ops.append((lv, 0, name, x, y, d))
+    nbra = max([o[0] for o in ops], default=0)
+
+    def kl(n):
+        return nbra if isinstance(n, tuple) else lvl[n]
+    for name, x, y, d in h.ket_ops:
+        lv = 1 + max(kl(x), kl(y))
+        lvl[name] = lv
+        arrays[name] = nab
+        ops.append((lv, 1, name, x, y, d))
+    nlev = max([o[0] for o in ops], default=0)
+    # last level each array is read at (finals live to the end)
+    last = {}
+
+    def touch(n, lv):
+        if isinstance(n, tuple):
+            for ab in range(nab):
+                rn = h.bra_final[(ab // nb, ab % nb)]
+                last[rn] = max(last.get(rn, 0), lv)
+        else:
+            last[n] = max(last.get(n, 0), lv)
+    for lv, ph, name, x, y, d in ops:
+        touch(x, lv)
+        touch(y, lv)
+    for n in h.bra_final.values():
+        last[n] = max(last.get(n, 0), nbra + 1 if h.ket_ops else nlev + 1)
+    for n in h.ket_final.values():
+        if isinstance(n, tuple):
+            touch(n, nlev + 1)
+        else:
+            last[n] = nlev + 1
+    if not h.ket_ops:
+        for n in h.bra_final.values():
+            last[n] = nlev + 1
+    base = {}
+    big = 1 << 20
+    free = [(nacc, big)]
+    for r in range(len(v.e_targets)):
+        base[f"(acc + {r * nf})"] = r * nf
+    # acc rows are freed after their last read
+    acc_rows = [f"(acc + {r * nf})" for r in range(len(v.e_targets))]
+    peak = nacc
+    for lv in range(1, nlev + 2):
+        for o in ops:
+            if o[0] == lv:
+                base[o[2]] = _alloc(free, arrays[o[2]])
+                peak = max(peak, base[o[2]] + arrays[o[2]])
+        for n in list(base):
+            if last.get(n, 0) == lv and n not in ("",):
+                size = nf if n in acc_rows else arrays[n]
+                _release(free, base[n], size)
+    hsize = peak
+
+    def eslot(n, k):
+        """slot of element k of array n (k over f for bra arrays, over ab for ket arrays)."""
+        if isinstance(n, tuple):
+            rn = h.bra_final[(k // nb, k % nb)]
+            return base[rn] + n[1]
+        return base[n] + k
+    hops, hlev = [], []
+    for lv in range(1, nlev + 1):
+        hlev.append(len(hops))
+        for o in ops:
+            if o[0] != lv:
+                continue
+            _, ph, name, x, y, d = o
+            n = nf if ph == 0 else nab
+            for k in range(n):
+                hops.append((base[name] + k, eslot(x, k), eslot(y, k), d + 3 * ph))
+    hlev.append(len(hops))
+    outslot = []
+    for ab in range(nab):
+        for cd in range(ncd):
+            src = h.ket_final[(cd // nd, cd % nd)]
+            if isinstance(src, tuple):
+                rn = h.bra_final[(ab // nb, ab % nb)]
+                outslot.append(base[rn] + src[1])
+            else:
+                outslot.append(base[src] + ab)
+    assert max(outslot) < hsize and hsize < 65536 and nvslot < 65536
+    return dict(L=L, nacc=nacc, nvslot=nvslot, vout=vout, vdesc=vdesc, vseg=vseg, vtgt=vtgt,
+                hsize=hsize, hops=hops, hlev=hlev, outslot=outslot,
+                vrr_flops=v.em.flops, hrr_flops=h.em.flops)
+
+
+def emit_wide(cls):
+    p = wide_program(cls)
+    tag = "".join(map(str, cls))
+    la, lb, lc, ld = cls
+
+    def arr(ctype, name, vals):
+        body = ",".join(str(x) for x in vals) if vals else "0"
+        return f"__device__ const {ctype} {name}[{max(1, len(vals))}] = {{{body}}};"
+    segs = [x for s in p["vseg"] for x in (s[0], s[1], s[2], s[3] | (s[5] << 8))]
+    hop = [x for o in p["hops"] for x in (o[0] | (o[1] << 16), o[2] | (o[3] << 16))]
+    out = [f"// generated by gen_eri.py -- warp program of class ({la}{lb}|{lc}{ld})",
+           "#pragma once", "namespace gs {",
+           arr("unsigned short", f"w{tag}_vout", p["vout"]),
+           arr("unsigned int", f"w{tag}_vdesc", p["vdesc"]),
+           arr("int", f"w{tag}_vseg", segs),
+           arr("unsigned short", f"w{tag}_vtgt", p["vtgt"]),
+           arr("unsigned int", f"w{tag}_hop", hop),
+           arr("int", f"w{tag}_hlev", p["hlev"]),
+           arr("unsigned short", f"w{tag}_out", p["outslot"]),
+           f"template <> struct WideProg<{la}, {lb}, {lc}, {ld}> {{",
+           f"  static constexpr int NVSLOT = {p['nvslot']}, NVSEG = {len(p['vseg'])};",
+           f"  static constexpr int HSIZE = {p['hsize']}, NHLEV = {len(p['hlev']) - 1};",
+           f"  static __device__ const unsigned short* vout() {{ return w{tag}_vout; }}",
+           f"  static __device__ const unsigned int* vdesc() {{ return w{tag}_vdesc; }}",
+           f"  static __device__ const int* vseg() {{ return w{tag}_vseg; }}",
+           f"  static __device__ const unsigned short* vtgt() {{ return w{tag}_vtgt; }}",
+           f"  static __device__ const unsigned int* hop() {{ return w{tag}_hop; }}",
+           f"  static __device__ const int* hlev() {{ return w{tag}_hlev; }}",
+           f"  static __device__ const unsigned short* outslot() {{ return w{tag}_out; }}",
+           "};", "}  // namespace gs", ""]
+    return "\n".join(out), p
 
 
 if __name__ == "__main__":

@@ -313,6 +313,7 @@ typedef struct {
     long begin, end;
     int boys_mode, memo;
     double *out;
+    long *next;     /* shared work counter: quartets are handed out 8 at a time */
 } job_t;
 
 #define MEMO_CAP (1 << 20)
@@ -326,8 +327,13 @@ static void *worker(void *arg)
         val = (double *)malloc(sizeof(double) * MEMO_CAP);
         have = (unsigned char *)malloc(MEMO_CAP);
     }
-    for (long i = j->begin; i < j->end; ++i)
-        j->out[i] = integrate(j->t, j->quartets + 4 * i, j->boys_mode, j->memo, val, have);
+    for (;;) {
+        long i0 = __sync_fetch_and_add(j->next, 8);
+        if (i0 >= j->end) break;
+        long i1 = i0 + 8 < j->end ? i0 + 8 : j->end;
+        for (long i = i0; i < i1; ++i)
+            j->out[i] = integrate(j->t, j->quartets + 4 * i, j->boys_mode, j->memo, val, have);
+    }
     free(val);
     free(have);
     return NULL;
@@ -358,15 +364,16 @@ int oracle_eri_functions(int nfunc, const double *centre, const int *lmn, const 
     if (nq < nthreads) nthreads = nq > 0 ? (int)nq : 1;
     pthread_t th[256];
     job_t jobs[256];
-    long chunk = (nq + nthreads - 1) / nthreads;
+    long next = 0;
     for (int k = 0; k < nthreads; ++k) {
         jobs[k].t = &t;
         jobs[k].quartets = quartets;
-        jobs[k].begin = k * chunk < nq ? k * chunk : nq;
-        jobs[k].end = (k + 1) * chunk < nq ? (k + 1) * chunk : nq;
+        jobs[k].begin = 0;
+        jobs[k].end = nq;
         jobs[k].boys_mode = boys_mode;
         jobs[k].memo = memo;
         jobs[k].out = out;
+        jobs[k].next = &next;
     }
     if (nthreads == 1) {
         worker(&jobs[0]);

@@ -48,9 +48,9 @@ def test_synthetic_every_class(gpu_lib, precision, rtol, atol):
 def test_h2o_631gs_all_quartets_match_reference(gpu_lib):
     """Every canonical function quartet of water/6-31G* against the as-is reference
     (its Boys error bounds the difference) and the exact-Boys oracle (1e-13)."""
-    from gaussium_gb300.dropin import TwoElectronRepulsionMatrixGPU
+    from gaussium_gb300.dropin import TwoElectronRepulsionGPU
     g, funcs, table = load("h2o_631gs")
-    dense = TwoElectronRepulsionMatrixGPU(funcs, None, 1).create_repulsion_matrix()
+    dense = TwoElectronRepulsionGPU(funcs, None, None, 1).create_repulsion_matrix()
     keys = g["keys"].astype(np.int64)
     got = dense[keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3]]
     assert np.max(np.abs(got - g["eri"])) < 1e-10

@@ -1,0 +1,85 @@
+"""The warp-cooperative kernels' generated programs (VRR node levels, HRR element
+operations on the planned shared buffer, output slots) emulated on the CPU and compared
+with the straight-line generated code, for every class that uses them."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import synthetic_shells, golden, ROOT
+from gaussium_gb300.basis import ShellBasis
+import hostcheck
+
+sys.path.insert(0, os.path.join(ROOT, "gaussium_gb300", "csrc"))
+import gen_eri  # noqa: E402
+
+
+def emulate(cls, pr, pd, bra, ket):
+    """Run the warp program of `cls` for quartet (bra|ket) with numpy, sequentially."""
+    p = gen_eri.wide_program(cls)
+    L = p["L"]
+    B, K = pr[bra], pr[ket]
+    acc = np.zeros(p["nacc"])
+    for i in range(B["nprim"]):
+        P = pd[B["prim_off"] + i]
+        for j in range(K["nprim"]):
+            Q = pd[K["prim_off"] + j]
+            pq = P[0] + Q[0]
+            PQ = Q[2:5] - P[2:5]
+            wq, wp = Q[0] / pq, P[0] / pq
+            t = P[0] * wq * PQ @ PQ
+            pref = P[8] * Q[8] / np.sqrt(pq)
+            F = np.array([oracle.boys_exact(m, t) for m in range(L + 1)]) * pref
+            c = np.zeros(32)
+            c[0:3] = P[5:8]; c[3:6] = wq * PQ; c[6:9] = Q[5:8]; c[9:12] = -wp * PQ
+            i2p, i2q = P[1], Q[1]
+            for k in range(1, 5):
+                c[11 + k] = k * i2p; c[15 + k] = -k * wq * i2p; c[19 + k] = k * i2q
+                c[23 + k] = -k * wp * i2q; c[27 + k] = k * 0.5 / pq
+            node = np.zeros(p["nvslot"])
+            node[:L + 1] = F
+            for doff, ooff, cnt, nt, lv, sync in p["vseg"]:
+                for n in range(cnt):
+                    r = 0.0
+                    for tt in range(nt):
+                        x = p["vdesc"][doff + n * nt + tt]
+                        r += c[x >> 16] * node[x & 0xffff]
+                    node[p["vout"][ooff + n]] = r
+            acc += node[np.array(p["vtgt"])]
+    H = np.zeros(p["hsize"])
+    H[:p["nacc"]] = acc
+    dv = [B["AB"][0], B["AB"][1], B["AB"][2], K["AB"][0], K["AB"][1], K["AB"][2]]
+    for lv in range(len(p["hlev"]) - 1):
+        new = {}
+        for e in range(p["hlev"][lv], p["hlev"][lv + 1]):
+            out, x, y, d = p["hops"][e]
+            new[out] = H[x] + dv[d] * H[y]
+        for k, v in new.items():
+            H[k] = v
+    return H[np.array(p["outslot"])]
+
+
+@pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(2) if sum(c) >= 5])
+def test_wide_program_matches_generated_code(cls):
+    shells = synthetic_shells()
+    sb = ShellBasis.from_shell_dicts(shells)
+    g = golden("synthetic")
+    done = 0
+    for q in g["quartets"]:
+        a, b, c, d = (int(x) for x in q)
+        ls = tuple(int(sb.l[x]) for x in (a, b, c, d))
+        if ls != cls:
+            continue
+        pr, pd, _ = hostcheck.make_pairs(sb, [(a, b), (c, d)])
+        got = emulate(cls, pr, pd, 0, 1)
+        blk, _ = hostcheck.canonical_block(sb, q, 64)
+        s = [sb.comp_scale[x][:n] for x, n in zip((a, b, c, d), blk.shape)]
+        blk = blk / (s[0][:, None, None, None] * s[1][None, :, None, None] *
+                     s[2][None, None, :, None] * s[3][None, None, None, :])
+        assert np.max(np.abs(got - blk.ravel())) <= 1e-13 + 1e-11 * np.max(np.abs(blk))
+        done += 1
+        if done == 2:
+            break
+    assert done > 0
