@@ -333,7 +333,9 @@ def run_gpu(args, rank, world):
                  "frac_of_fp64_peak": total_flops / (ms64 * 1e-3) / 1e12 / peak64},
         "fp32": {"value": n_all / (ms32 * 1e-3), "ms_per_step": ms32,
                  "max_abs_err_vs_fp64": err32, "fp32_peak_tflops": peak32},
-        "per_class_ms_fp64": {"".join(map(str, c)): v for c, v in res[64]["per_cls"].items()},
+        "per_class_ms_fp64": {"".join(map(str, c)): round(v, 3) for c, v in res[64]["per_cls"].items()},
+        "per_class_ms_fp32": {"".join(map(str, c)): round(v, 3) for c, v in res[32]["per_cls"].items()},
+        "per_class_gflop": {"".join(map(str, c)): round(v / 1e9, 3) for c, v in fl.items()},
         "clocks": res[64]["clocks"],
         "e2e": e2e,
         "gpu_launches": nlaunch * args.steps,

@@ -25,6 +25,7 @@ _SIGS = {
     "gs_fock_jk": (I, [I, I, I, I, I, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, D, P]),
     "gs_boys_eval": (I, [I, I, I, P, P, P]),
     "gs_fma_probe": (I, [I, I, I, I, P, P]),
+    "gs_one_electron": (I, [P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),
 }
 
 

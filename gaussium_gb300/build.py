@@ -114,6 +114,7 @@ def build(jobs=None, verbose=False):
     todo = [(src, deps, os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")) for src, deps in units]
     todo.append((os.path.join(CSRC, "capi.cu"), [os.path.join(GEN, "gs_built_classes.h")],
                  os.path.join(BUILD, "capi.o")))
+    todo.append((os.path.join(CSRC, "one_electron.cu"), [], os.path.join(BUILD, "one_electron.o")))
     jobs = jobs or max(1, os.cpu_count() or 1)
     changed = False
     with cf.ThreadPoolExecutor(jobs) as ex:

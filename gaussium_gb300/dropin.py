@@ -92,8 +92,12 @@ def dense_eri(sb: ShellBasis, device="cuda", precision=64):
         idx[:, k] = rem % nq[:, k] + fo[qt[owner, k]]
         rem = rem // nq[:, k]
     v = vals[:batch.total]
-    t = torch.zeros((n, n, n, n), dtype=torch.float64, device=dev)
     a, b, c, d = idx.unbind(1)
+    # one writer per 8-fold orbit: keep i >= j, k >= l, (i,j) >= (k,l); blocks of shell
+    # quartets with repeated shells hold each orbit more than once
+    keep = (a >= b) & (c >= d) & ((a > c) | ((a == c) & (b >= d)))
+    a, b, c, d, v = a[keep], b[keep], c[keep], d[keep], v[keep]
+    t = torch.zeros((n, n, n, n), dtype=torch.float64, device=dev)
     for (w, x, y, z) in ((a, b, c, d), (b, a, c, d), (a, b, d, c), (b, a, d, c),
                          (c, d, a, b), (d, c, a, b), (c, d, b, a), (d, c, b, a)):
         t[w, x, y, z] = v

@@ -107,6 +107,20 @@ int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_r
  * (integrals/boys_function.py:4-76). */
 int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream);
 
+/* K7 one-electron integrals over npairs shell pairs pair_shells[2*p] (any order of l):
+ * overlap S, kinetic T (-1/2 nabla^2 on the ket) and nuclear attraction V of natom point
+ * charges atom_z[] at atom_xyz[3*natom], written to both (a,b) and (b,a) blocks of the
+ * nbf x nbf matrices.  Replaces OrbitalOverlapMatrix / KineticEnergyMatrix /
+ * NuclearAttractionMatrix .create (matrixelements/orbital_overlap_matrix.py:15-27,
+ * kinetic_energy_matrix.py:16-33, nuclear_attraction_matrix.py:16-29) and the integrals
+ * they call (integrals/orbital_overlap_integral.py:16-36,
+ * integrals/nuclear_attraction_integral.py:19-57). */
+int gs_one_electron(const double* centre, const int* l, const int* prim_off, const double* expo,
+                    const double* coef, const double* comp_scale, const int* func_off,
+                    int npairs, const int* pair_shells, int nbf, int natom,
+                    const double* atom_xyz, const double* atom_z, double* S, double* T,
+                    double* V, void* stream);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);
