@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--prim-screen", type=float, default=55.262,
+                    help="drop primitive pairs with alpha*beta/p |AB|^2 above this (0: keep all)")
     return ap.parse_args()
 
 
@@ -211,7 +213,7 @@ def run_gpu(args, rank, world):
     opcount = build.opcount()
     sb, quartets, _ = random_shell_quartets(args.quartets, seed=args.seed + rank)
     ds = engine.DeviceShells(sb)
-    batch = engine.QuartetBatch(ds, quartets, want32=True)
+    batch = engine.QuartetBatch(ds, quartets, want32=True, max_exp=args.prim_screen)
     out = torch.empty(batch.total, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     classes = [c for c, _, _ in batch.segments]
@@ -322,7 +324,11 @@ def run_gpu(args, rank, world):
                 "larger than L2",
         "config": {"workload": WORKLOAD, "quartets_per_gpu": args.quartets,
                    "function_quartets_per_gpu": int(batch.total),
-                   "primitive_quartets_per_gpu": int(batch.prim_quartets),
+                   "primitive_quartets_per_gpu": int(batch.full_prim_quartets),
+                   "primitive_quartets_evaluated_per_gpu": int(batch.prim_quartets),
+                   "primitive_pair_screen": (f"alpha*beta/p|AB|^2 > {args.prim_screen} dropped "
+                                             "(Gaussian-product factor < 1e-24)")
+                   if args.prim_screen > 0 else "none",
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2"},
         "roofline": {"bound": "fp64", "kernel": "eri class " + "".join(map(str, dom)) + " FP64",
                      "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",

@@ -15,19 +15,21 @@ import sys
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
-BUILD = os.path.join(PKG, "_build")
+# GS_BUILD_DIR / GS_LIB_PATH / GS_NVCC_EXTRA let a tuning sweep build variants side by side
+BUILD = os.environ.get("GS_BUILD_DIR", os.path.join(PKG, "_build"))
 GEN = os.path.join(BUILD, "gen")
-LIB = os.path.join(PKG, "libgaussium_gb300.so")
+LIB = os.environ.get("GS_LIB_PATH", os.path.join(PKG, "libgaussium_gb300.so"))
 HOSTCHECK = os.path.join(BUILD, "libhostcheck.so")
 LMAX = 2
 # Classes with total angular momentum above THREAD_LMAX_TOTAL use the warp-cooperative
 # kernel (csrc/eri_wide.cuh); the others one thread per quartet (csrc/eri_kernels.cuh).
-THREAD_LMAX_TOTAL = 6
+THREAD_LMAX_TOTAL = int(os.environ.get("GS_THREAD_LMAX", "6"))
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                  "--expt-relaxed-constexpr", "-I", CSRC, "-I", GEN]
+                  "--expt-relaxed-constexpr", "-I", CSRC, "-I", GEN] + \
+    os.environ.get("GS_NVCC_EXTRA", "").split()
 
 
 def _run(cmd, **kw):

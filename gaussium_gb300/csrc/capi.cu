@@ -29,10 +29,13 @@ int check_launch() { return cudaPeekAtLastError() == cudaSuccess ? GS_OK : GS_ER
 
 __global__ void k_pairs_build(gs::ShellView sv, int npairs, const int* __restrict__ pair_shells,
                               const int* __restrict__ pair_prim_off, gs::PairRec* pairs,
-                              gs::PrimRec<double>* p64, gs::PrimRec<float>* p32) {
+                              gs::PrimRec<double>* p64, gs::PrimRec<float>* p32, double max_exp,
+                              int* __restrict__ kept) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npairs) return;
-    gs::make_pair(sv, pair_shells[2 * i], pair_shells[2 * i + 1], pair_prim_off[i], pairs[i], p64, p32);
+    gs::make_pair(sv, pair_shells[2 * i], pair_shells[2 * i + 1], pair_prim_off[i], pairs[i], p64,
+                  p32, max_exp);
+    if (kept) kept[i] = pairs[i].nprim;
 }
 
 __global__ void k_set_qmax(gs::PairRec* pairs, const double* __restrict__ q, int npairs) {
@@ -100,14 +103,14 @@ int gs_class_available(int la, int lb, int lc, int ld) {
 int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
                    const double* coef, int npairs, const int* pair_shells,
                    const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
-                   void* stream) {
+                   double max_exp, int* kept, void* stream) {
     if (npairs < 0 || !centre || !l || !prim_off || !expo || !coef || !pair_rec || !prim64)
         return GS_ERR_ARG;
     if (npairs == 0) return GS_OK;
     gs::ShellView sv{centre, l, prim_off, expo, coef};
     k_pairs_build<<<(npairs + 127) / 128, 128, 0, S(stream)>>>(
         sv, npairs, pair_shells, pair_prim_off, (gs::PairRec*)pair_rec,
-        (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32);
+        (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32, max_exp, kept);
     return check_launch();
 }
 

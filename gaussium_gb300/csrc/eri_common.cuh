@@ -223,8 +223,11 @@ struct ShellView {
 constexpr double kSqrt2Pi52 = 5.914967172795613;  // sqrt(2 pi^(5/2))
 
 // Fill the PairRec and the primitive-pair records of shell pair (sa, sb); la >= lb.
+// Primitive pairs whose Gaussian-product factor exp(-ab/p |AB|^2) is below exp(-max_exp)
+// are dropped when max_exp > 0 (their contributions are below that factor times the
+// normalised block's scale); pr.nprim is the number kept.
 GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off, PairRec& pr,
-                               PrimRec<double>* pd, PrimRec<float>* pf) {
+                               PrimRec<double>* pd, PrimRec<float>* pf, double max_exp = 0.0) {
     const double* A = S.centre + 3 * sa;
     const double* B = S.centre + 3 * sb;
     const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
@@ -238,9 +241,10 @@ GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off,
     pr.qmax = 0.0f; pr.pad = 0;
     int n = prim_off;
     for (int i = a0; i < a1; ++i) {
-        for (int j = b0; j < b1; ++j, ++n) {
+        for (int j = b0; j < b1; ++j) {
             const double a = S.expo[i], b = S.expo[j];
             const double p = a + b, ip = 1.0 / p;
+            if (max_exp > 0.0 && a * b * ip * ab2 > max_exp) continue;
             PrimRec<double> r;
             r.p = p;
             r.i2p = 0.5 * ip;
@@ -259,8 +263,10 @@ GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off,
                 f.Kp = (float)r.Kp; f.pad0 = f.pad1 = f.pad2 = 0.0f;
                 pf[n] = f;
             }
+            ++n;
         }
     }
+    pr.nprim = n - prim_off;
 }
 
 // Original-order strides of a canonical block (see WriteTask::code).

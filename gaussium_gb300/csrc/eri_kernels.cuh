@@ -11,9 +11,12 @@
 namespace gs {
 
 constexpr int kBlock = 128;
+#ifndef GS_THREAD_MINB
+#define GS_THREAD_MINB 1
+#endif
 
 template <int LA, int LB, int LC, int LD, typename T>
-__global__ void __launch_bounds__(kBlock) k_eri_write(const WriteArgs a) {
+__global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_write(const WriteArgs a) {
     using G = ClassGen<LA, LB, LC, LD>;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.ntask) return;
@@ -48,7 +51,7 @@ __global__ void __launch_bounds__(kBlock) k_eri_write(const WriteArgs a) {
 // with v = (ab|cd) / ((1+d_ab)(1+d_cd)(1+d_ab,cd)), so that J = J' + J'^T and
 // K = K' + K'^T sum every permutation of every quartet once.
 template <int LA, int LB, int LC, int LD, typename T>
-__global__ void __launch_bounds__(kBlock) k_eri_jk(const JKArgs a) {
+__global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs a) {
     using G = ClassGen<LA, LB, LC, LD>;
     constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;

@@ -28,9 +28,14 @@ template <int LA, int LB, int LC, int LD, typename T> struct WideLayout {
     static constexpr int SC = kSetupBatch * kNCoef;              // coefficients
     static constexpr int SF = kSetupBatch * (G::L + 1);          // Boys values
     static constexpr int VRR = SC + SF + W::NVSLOT;
-    static constexpr int HR = W::HSIZE + G::NBLK + G::NA * G::NB + G::NC * G::ND;
-    static constexpr int WARP = VRR > HR ? VRR : HR;             // elements of T per warp
-    static constexpr size_t BYTES = (size_t)WARP * sizeof(T) * kWideWarps;
+    // write/Schwarz epilogues need the HRR buffer and the scale vectors; the J/K epilogue
+    // also a scaled copy of the block
+    static constexpr int HR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
+    static constexpr int HR_JK = W::HSIZE + G::NBLK + G::NA * G::NB + G::NC * G::ND;
+    static constexpr int WARP_W = VRR > HR_W ? VRR : HR_W;       // elements of T per warp
+    static constexpr int WARP_JK = VRR > HR_JK ? VRR : HR_JK;
+    static constexpr size_t BYTES_W = (size_t)WARP_W * sizeof(T) * kWideWarps;
+    static constexpr size_t BYTES_JK = (size_t)WARP_JK * sizeof(T) * kWideWarps;
 };
 
 template <typename T>
@@ -85,8 +90,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     T* node = sm + Lay::SC + Lay::SF;
     const int nK = K.nprim;
     const int ntot = B.nprim * nK;
-    const unsigned short* __restrict__ vout = W::vout();
-    const unsigned int* __restrict__ vdesc = W::vdesc();
+    const uint4* __restrict__ vrec = W::vrec();
     const int* __restrict__ vseg = W::vseg();
     const unsigned short* __restrict__ vtgt = W::vtgt();
     for (int base = 0; base < ntot; base += kSetupBatch) {
@@ -103,19 +107,27 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
             if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
             __syncwarp();
             for (int s = 0; s < W::NVSEG; ++s) {
-                const int doff = __ldg(vseg + 4 * s), ooff = __ldg(vseg + 4 * s + 1);
-                const int cnt = __ldg(vseg + 4 * s + 2), w = __ldg(vseg + 4 * s + 3);
-                const int nt = w & 0xff;
-                if ((w >> 8) && s > 0) __syncwarp();
-                for (int n = lane; n < cnt; n += 32) {
-                    const unsigned int* d = vdesc + doff + n * nt;
-                    unsigned int x = __ldg(d);
-                    T r = c[x >> 16] * node[x & 0xffff];
-                    for (int t = 1; t < nt; ++t) {
-                        x = __ldg(d + t);
-                        r = fma(c[x >> 16], node[x & 0xffff], r);
+                const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
+                const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
+                if (sync && s > 0) __syncwarp();
+                int n = lane;
+                uint4 ra = make_uint4(0, 0, 0, 0), rb = ra;
+                if (n < cnt) {
+                    ra = __ldg(vrec + 2 * (noff + n));
+                    rb = __ldg(vrec + 2 * (noff + n) + 1);
+                }
+                for (; n < cnt; n += 32) {
+                    const uint4 a = ra, b = rb;
+                    if (n + 32 < cnt) {                       // prefetch the next node
+                        ra = __ldg(vrec + 2 * (noff + n + 32));
+                        rb = __ldg(vrec + 2 * (noff + n + 32) + 1);
                     }
-                    node[__ldg(vout + ooff + n)] = r;
+                    T r = c[a.y >> 16] * node[a.y & 0xffff];
+                    r = fma(c[a.z >> 16], node[a.z & 0xffff], r);
+                    if (nt > 2) r = fma(c[a.w >> 16], node[a.w & 0xffff], r);
+                    if (nt > 3) r = fma(c[b.x >> 16], node[b.x & 0xffff], r);
+                    if (nt > 4) r = fma(c[b.y >> 16], node[b.y & 0xffff], r);
+                    node[a.x & 0xffff] = r;
                 }
             }
             __syncwarp();
@@ -158,7 +170,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs 
     using Lay = WideLayout<LA, LB, LC, LD, T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_W;
     const int t = blockIdx.x * kWideWarps + warp;
     if (t >= a.ntask) return;
     const WriteTask task = a.tasks[t];
@@ -167,7 +179,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs 
     wide_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     long long s[4];
     block_strides(task.code, G::NA, G::NB, G::NC, G::ND, s);
-    T* sab = sm + W::HSIZE + G::NBLK;
+    T* sab = sm + W::HSIZE;
     T* scd = sab + G::NA * G::NB;
     for (int x = lane; x < G::NA * G::NB; x += 32)
         sab[x] = (T)(a.comp_scale[6 * B.sa + x / G::NB] * a.comp_scale[6 * B.sb + x % G::NB]);
@@ -194,7 +206,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
     constexpr int NAB = NA * NB, NCD = NC * ND;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_JK;
     const int t = blockIdx.x * kWideWarps + warp;
     if (t >= a.ntask) return;
     const int2 task = a.tasks[t];
@@ -290,7 +302,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
     using Lay = WideLayout<LA, LB, LA, LB, T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_W;
     const int t = blockIdx.x * kWideWarps + warp;
     if (t >= a.npair) return;
     const int p = a.pair_index[t];
@@ -316,12 +328,12 @@ int launch_wide(int kind, int prec, const void* args, cudaStream_t st) {
         if (a.ntask <= 0) return 0;
         const int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
         if (prec == 64) {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES;
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES_W;
             auto k = k_wide_write<LA, LB, LC, LD, double>;
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
             k<<<grid, TPB, sh, st>>>(a);
         } else {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES;
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES_W;
             auto k = k_wide_write<LA, LB, LC, LD, float>;
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
             k<<<grid, TPB, sh, st>>>(a);
@@ -331,12 +343,12 @@ int launch_wide(int kind, int prec, const void* args, cudaStream_t st) {
         if (a.ntask <= 0) return 0;
         const int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
         if (prec == 64) {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES;
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES_JK;
             auto k = k_wide_jk<LA, LB, LC, LD, double>;
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
             k<<<grid, TPB, sh, st>>>(a);
         } else {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES;
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES_JK;
             auto k = k_wide_jk<LA, LB, LC, LD, float>;
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
             k<<<grid, TPB, sh, st>>>(a);
@@ -346,7 +358,7 @@ int launch_wide(int kind, int prec, const void* args, cudaStream_t st) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;
             if (a.npair <= 0) return 0;
             const int grid = (a.npair + kWideWarps - 1) / kWideWarps;
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES;
+            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES_W;
             auto k = k_wide_schwarz<LA, LB, double>;
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
             k<<<grid, TPB, sh, st>>>(a);

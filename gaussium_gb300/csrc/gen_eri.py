@@ -422,7 +422,36 @@ def wide_program(cls):
         level[L + 1 + idx] = lv
         nodes.append((lv, len(ts), L + 1 + idx, ts))
     nodes.sort(key=lambda n: (n[0], n[1], n[2]))
-    vout, vdesc, vseg = [], [], []
+    tgt = [v.names[(e, f, 0)] if not (e == (0, 0, 0) and f == (0, 0, 0)) else "F[0]"
+           for e in v.e_targets for f in v.f_targets]
+    tslots = set(slot(t) for t in tgt)
+    # liveness: a node's slot is free after the last level that reads it; targets and
+    # the Boys values live to the end of the primitive quartet
+    maxlv = max((n[0] for n in nodes), default=0)
+    last = {}
+    for lv, nt, out, ts in nodes:
+        for _, sl in ts:
+            last[sl] = max(last.get(sl, 0), lv)
+    for sl in tslots:
+        last[sl] = maxlv + 1
+    phys = {m: m for m in range(L + 1)}
+    free = []
+    top = L + 1
+    by_level = {}
+    for n in nodes:
+        by_level.setdefault(n[0], []).append(n)
+    for lv in sorted(by_level):
+        for n in by_level[lv]:
+            if free:
+                phys[n[2]] = free.pop()
+            else:
+                phys[n[2]] = top
+                top += 1
+        for sl, lu in last.items():
+            if lu == lv and sl > L:
+                free.append(phys[sl])
+        free.sort(reverse=True)
+    vrec, vseg = [], []
     i = 0
     while i < len(nodes):
         j = i
@@ -430,17 +459,15 @@ def wide_program(cls):
             j += 1
         lv, nt = nodes[i][:2]
         sync = 1 if (not vseg or vseg[-1][4] != lv) else 0
-        vseg.append([len(vdesc), len(vout), j - i, nt, lv, sync])
+        vseg.append([len(vrec) // 8, 0, j - i, nt, lv, sync])
         for n in nodes[i:j]:
-            vout.append(n[2])
-            for cid, s in n[3]:
-                vdesc.append((cid << 16) | s)
+            words = [phys[n[2]] | (nt << 16)] + [(cid << 16) | phys[sl] for cid, sl in n[3]]
+            words += [0] * (8 - len(words))
+            vrec.extend(words)
         i = j
-    tgt = [v.names[(e, f, 0)] if not (e == (0, 0, 0) and f == (0, 0, 0)) else "F[0]"
-           for e in v.e_targets for f in v.f_targets]
-    vtgt = [slot(t) for t in tgt]
-    nvslot = L + 1 + len(v.struct)
-
+    vtgt = [phys[slot(t)] for t in tgt]
+    nvslot = top
+    vout, vdesc = [], []
     # ---- HRR: arrays, levels, liveness
     arrays = {}          # name -> (size, producer level)
     lvl = {}
@@ -531,7 +558,7 @@ def wide_program(cls):
             else:
                 outslot.append(base[src] + ab)
     assert max(outslot) < hsize and hsize < 65536 and nvslot < 65536
-    return dict(L=L, nacc=nacc, nvslot=nvslot, vout=vout, vdesc=vdesc, vseg=vseg, vtgt=vtgt,
+    return dict(L=L, nacc=nacc, nvslot=nvslot, vrec=vrec, vseg=vseg, vtgt=vtgt,
                 hsize=hsize, hops=hops, hlev=hlev, outslot=outslot,
                 vrr_flops=v.em.flops, hrr_flops=h.em.flops)
 
@@ -544,12 +571,11 @@ def emit_wide(cls):
     def arr(ctype, name, vals):
         body = ",".join(str(x) for x in vals) if vals else "0"
         return f"__device__ const {ctype} {name}[{max(1, len(vals))}] = {{{body}}};"
-    segs = [x for s in p["vseg"] for x in (s[0], s[1], s[2], s[3] | (s[5] << 8))]
+    segs = [x for s in p["vseg"] for x in (s[0], s[2], s[3], s[5])]
     hop = [x for o in p["hops"] for x in (o[0] | (o[1] << 16), o[2] | (o[3] << 16))]
     out = [f"// generated by gen_eri.py -- warp program of class ({la}{lb}|{lc}{ld})",
            "#pragma once", "namespace gs {",
-           arr("unsigned short", f"w{tag}_vout", p["vout"]),
-           arr("unsigned int", f"w{tag}_vdesc", p["vdesc"]),
+           arr("unsigned int __align__(16)", f"w{tag}_vrec", p["vrec"]),
            arr("int", f"w{tag}_vseg", segs),
            arr("unsigned short", f"w{tag}_vtgt", p["vtgt"]),
            arr("unsigned int", f"w{tag}_hop", hop),
@@ -558,8 +584,7 @@ def emit_wide(cls):
            f"template <> struct WideProg<{la}, {lb}, {lc}, {ld}> {{",
            f"  static constexpr int NVSLOT = {p['nvslot']}, NVSEG = {len(p['vseg'])};",
            f"  static constexpr int HSIZE = {p['hsize']}, NHLEV = {len(p['hlev']) - 1};",
-           f"  static __device__ const unsigned short* vout() {{ return w{tag}_vout; }}",
-           f"  static __device__ const unsigned int* vdesc() {{ return w{tag}_vdesc; }}",
+           f"  static __device__ const uint4* vrec() {{ return reinterpret_cast<const uint4*>(w{tag}_vrec); }}",
            f"  static __device__ const int* vseg() {{ return w{tag}_vseg; }}",
            f"  static __device__ const unsigned short* vtgt() {{ return w{tag}_vtgt; }}",
            f"  static __device__ const unsigned int* hop() {{ return w{tag}_hop; }}",

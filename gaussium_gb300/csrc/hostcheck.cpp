@@ -13,7 +13,7 @@ extern "C" int hc_make_pairs(int npairs, const int* pair_shells, const int* pair
                              PrimRec<double>* pd, PrimRec<float>* pf) {
     ShellView S{centre, l, prim_off, expo, coef};
     for (int i = 0; i < npairs; ++i)
-        make_pair(S, pair_shells[2 * i], pair_shells[2 * i + 1], pair_prim_off[i], pairs[i], pd, pf);
+        make_pair(S, pair_shells[2 * i], pair_shells[2 * i + 1], pair_prim_off[i], pairs[i], pd, pf, 0.0);
     return 0;
 }
 

@@ -93,9 +93,14 @@ def dense_eri(sb: ShellBasis, device="cuda", precision=64):
         rem = rem // nq[:, k]
     v = vals[:batch.total]
     a, b, c, d = idx.unbind(1)
-    # one writer per 8-fold orbit: keep i >= j, k >= l, (i,j) >= (k,l); blocks of shell
-    # quartets with repeated shells hold each orbit more than once
-    keep = (a >= b) & (c >= d) & ((a > c) | ((a == c) & (b >= d)))
+    # one writer per 8-fold orbit: a unique shell quartet holds an orbit more than once only
+    # where shells repeat (A = B, C = D, or bra pair = ket pair); keep one element there
+    sq = qt[owner]
+    same_ab = sq[:, 0] == sq[:, 1]
+    same_cd = sq[:, 2] == sq[:, 3]
+    same_pair = (sq[:, 0] == sq[:, 2]) & (sq[:, 1] == sq[:, 3])
+    keep = (~same_ab | (a >= b)) & (~same_cd | (c >= d)) & \
+        (~same_pair | (a > c) | ((a == c) & (b >= d)))
     a, b, c, d, v = a[keep], b[keep], c[keep], d[keep], v[keep]
     t = torch.zeros((n, n, n, n), dtype=torch.float64, device=dev)
     for (w, x, y, z) in ((a, b, c, d), (b, a, c, d), (a, b, d, c), (b, a, d, c),

@@ -21,6 +21,9 @@ PAIR_ORDER = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
 PAIR_CLASS = {p: i for i, p in enumerate(PAIR_ORDER)}
 NCART = np.array([1, 3, 6, 10])
 PAIR_REC, PRIM64, PRIM32, WRITE_TASK = 48, 80, 48, 24
+# Primitive pairs with alpha*beta/p |AB|^2 above this (Gaussian-product factor < 1e-24)
+# are dropped by the pair builder when screening is on.
+PRIM_SCREEN = 55.262
 WRITE_TASK_DTYPE = np.dtype([("bra", "<i4"), ("ket", "<i4"), ("code", "<i4"), ("pad", "<i4"),
                              ("off", "<i8")])
 
@@ -60,7 +63,7 @@ class DeviceShells:
 class PairSet:
     """Shell pairs (la >= lb inside each pair) with their primitive-pair records."""
 
-    def __init__(self, ds: DeviceShells, pair_shells, want32=True, stream=None):
+    def __init__(self, ds: DeviceShells, pair_shells, want32=True, stream=None, max_exp=0.0):
         ps = np.ascontiguousarray(pair_shells, dtype=np.int32).reshape(-1, 2)
         sb = ds.host
         if len(ps) and np.any(sb.l[ps[:, 0]] < sb.l[ps[:, 1]]):
@@ -84,7 +87,11 @@ class PairSet:
         self.p64 = torch.empty(total * PRIM64, dtype=torch.uint8, device=dev)
         self.p32 = torch.empty(total * PRIM32, dtype=torch.uint8, device=dev) if want32 else None
         self.nprim_pairs = int(off[-1])
+        self.max_exp = max_exp
+        self.kept = torch.zeros(max(1, self.n), dtype=torch.int32, device=dev)
         self.build(stream)
+        # primitive pairs kept per shell pair (the work per pair after screening)
+        self.nprim = self.kept[:self.n].cpu().numpy().astype(np.int64)
 
     def build(self, stream=None):
         """(Re)compute the pair records (kernel K0) from the device shells."""
@@ -94,6 +101,7 @@ class PairSet:
                                     _lib.ptr(ds.expo), _lib.ptr(ds.coef), self.n,
                                     _lib.ptr(self.shells), _lib.ptr(self.prim_start),
                                     _lib.ptr(self.rec), _lib.ptr(self.p64), _lib.ptr(self.p32),
+                                    float(self.max_exp), _lib.ptr(self.kept),
                                     _lib.stream(stream)), "gs_pairs_build")
 
     def prims(self, precision):
@@ -125,7 +133,7 @@ class QuartetBatch:
     (a,b,c,d) order, row-major.  Host preparation sorts the quartets by class and
     primitive counts; ``run`` launches one kernel per class."""
 
-    def __init__(self, ds: DeviceShells, quartets, want32=True):
+    def __init__(self, ds: DeviceShells, quartets, want32=True, max_exp=0.0):
         q = np.ascontiguousarray(quartets, dtype=np.int64).reshape(-1, 4)
         sb = ds.host
         n = len(q)
@@ -139,7 +147,9 @@ class QuartetBatch:
         self.offsets = off
         self.total = int(off[-1])
         pairs = np.concatenate([qc[:, 0:2], qc[:, 2:4]], axis=0)
-        self.pairs = PairSet(ds, pairs, want32=want32)
+        self.pairs = PairSet(ds, pairs, want32=want32, max_exp=max_exp)
+        self.full_prim_quartets = int(np.sum(sb.nprim[qc[:, 0]].astype(np.int64) * sb.nprim[qc[:, 1]] *
+                                             sb.nprim[qc[:, 2]] * sb.nprim[qc[:, 3]]))
         nb = self.pairs.nprim[:n]
         nk = self.pairs.nprim[n:]
         cls = pcb * 6 + pck
@@ -197,7 +207,8 @@ class JKEngine:
     basis, with Schwarz screening (task list built once per geometry) and optional
     density-weighted screening / precision selection per call."""
 
-    def __init__(self, sb: ShellBasis, device="cuda", schwarz_thr=1e-12, want32=True):
+    def __init__(self, sb: ShellBasis, device="cuda", schwarz_thr=1e-12, want32=True,
+                 max_exp=PRIM_SCREEN):
         self.sb = sb
         self.ds = ds = DeviceShells(sb, device)
         self.dev = ds.device
@@ -206,7 +217,7 @@ class JKEngine:
         swap = sb.l[i] < sb.l[j]
         sa = np.where(swap, j, i)
         sbb = np.where(swap, i, j)
-        self.pairs = PairSet(ds, np.stack([sa, sbb], axis=1), want32=want32)
+        self.pairs = PairSet(ds, np.stack([sa, sbb], axis=1), want32=want32, max_exp=max_exp)
         self.pair_class = _pc_lut[sb.l[sa], sb.l[sbb]]
         self.npairs = len(sa)
         self.schwarz_thr = schwarz_thr

@@ -55,12 +55,14 @@ int gs_class_available(int la, int lb, int lc, int ld);
  * normalisation product), hoisted to once per primitive *pair*.
  * Shells: centre[nshell*3] (bohr), l[nshell], prim_off[nshell+1], expo[nprim],
  * coef[nprim].  Pairs: pair_shells[npairs*2] (l[first] >= l[second]),
- * pair_prim_off[npairs] (first primitive-pair record of each pair).  Outputs:
- * pair_rec[npairs], prim64[sum Ka*Kb], prim32 (may be NULL). */
+ * pair_prim_off[npairs] (first primitive-pair record of each pair, Ka*Kb reserved).
+ * Outputs: pair_rec[npairs], prim64, prim32 (may be NULL), kept[npairs] (may be NULL:
+ * primitive pairs kept).  max_exp > 0 drops primitive pairs with
+ * alpha*beta/(alpha+beta)*|AB|^2 > max_exp (0 keeps all, as the reference does). */
 int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
                    const double* coef, int npairs, const int* pair_shells,
                    const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
-                   void* stream);
+                   double max_exp, int* kept, void* stream);
 
 /* K1 Schwarz bounds q[p] = sqrt(max |(ab|ab)|) for the npair pairs pair_index[] of class
  * (la lb), in FP64; then copies all npairs_total bounds into pair_rec[].qmax.  No

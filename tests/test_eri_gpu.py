@@ -133,3 +133,22 @@ def test_permuted_quartets_agree(gpu_lib):
         for j, perm in enumerate(perms):
             blk = out[off[5 * i + j]:off[5 * i + j + 1]].reshape(n[5 * i + j])
             np.testing.assert_allclose(blk, base.transpose(perm), rtol=0, atol=1e-15)
+
+
+def test_primitive_screening_changes_nothing_measurable(gpu_lib):
+    """Dropping primitive pairs with a Gaussian-product factor below 1e-24 changes no
+    block element by more than 1e-13 on the microbench's distribution."""
+    import torch
+    from gaussium_gb300 import engine
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(20000, seed=5)
+    ds = engine.DeviceShells(sb)
+    outs = []
+    for max_exp in (0.0, engine.PRIM_SCREEN):
+        b = engine.QuartetBatch(ds, q, want32=False, max_exp=max_exp)
+        o = torch.zeros(b.total, dtype=torch.float64, device="cuda")
+        b.run(o, 64)
+        outs.append(o)
+        kept = b.prim_quartets / b.full_prim_quartets
+    assert float((outs[0] - outs[1]).abs().max()) < 1e-13
+    assert kept < 0.8      # the screen does drop work on this distribution

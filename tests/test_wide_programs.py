@@ -40,13 +40,20 @@ def emulate(cls, pr, pd, bra, ket):
                 c[23 + k] = -k * wp * i2q; c[27 + k] = k * 0.5 / pq
             node = np.zeros(p["nvslot"])
             node[:L + 1] = F
-            for doff, ooff, cnt, nt, lv, sync in p["vseg"]:
+            rec = p["vrec"]
+            for noff, _, cnt, nt, lv, sync in p["vseg"]:
+                new = {}
                 for n in range(cnt):
+                    w = rec[8 * (noff + n): 8 * (noff + n) + 8]
+                    assert w[0] >> 16 == nt
                     r = 0.0
                     for tt in range(nt):
-                        x = p["vdesc"][doff + n * nt + tt]
+                        x = w[1 + tt]
                         r += c[x >> 16] * node[x & 0xffff]
-                    node[p["vout"][ooff + n]] = r
+                    new[w[0] & 0xffff] = r
+                # all nodes of a segment read values from earlier levels only
+                for k, val in new.items():
+                    node[k] = val
             acc += node[np.array(p["vtgt"])]
     H = np.zeros(p["hsize"])
     H[:p["nacc"]] = acc
