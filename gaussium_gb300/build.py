@@ -21,9 +21,12 @@ GEN = os.path.join(BUILD, "gen")
 LIB = os.environ.get("GS_LIB_PATH", os.path.join(PKG, "libgaussium_gb300.so"))
 HOSTCHECK = os.path.join(BUILD, "libhostcheck.so")
 LMAX = 2
-# Classes with total angular momentum above THREAD_LMAX_TOTAL use the warp-cooperative
-# kernel (csrc/eri_wide.cuh); the others one thread per quartet (csrc/eri_kernels.cuh).
-THREAD_LMAX_TOTAL = int(os.environ.get("GS_THREAD_LMAX", "6"))
+# Classes with total angular momentum L >= WIDE64_MIN (FP64) or >= WIDE32_MIN (FP32) use the
+# warp-cooperative kernel (csrc/eri_wide.cuh); the others one thread per quartet
+# (csrc/eri_kernels.cuh); csrc/eri_launch.cuh dispatches.
+WIDE64_MIN = int(os.environ.get("GS_WIDE64_MIN", "5"))
+WIDE32_MIN = int(os.environ.get("GS_WIDE32_MIN", "7"))
+WIDE_PROG_MIN = 3          # classes that get generated warp programs
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -76,21 +79,29 @@ def generate():
     for cls in built:
         tag = "".join(map(str, cls))
         path = os.path.join(GEN, f"eri_k_{tag}.cu")
-        if sum(cls) > THREAD_LMAX_TOTAL:
-            code = ('#include "eri_wide.cuh"\n#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n'
-                    'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
-                    '    return gs::launch_wide<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
-                    % (tag, tag, tag, *cls))
+        L = sum(cls)
+        if L >= WIDE_PROG_MIN:
+            inc = '#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n' % (tag, tag)
         else:
-            code = ('#include "eri_kernels.cuh"\n#include "eri_class_%s.h"\n'
-                    'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
-                    '    return gs::launch_class<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
-                    % (tag, tag, *cls))
+            # no warp program: the warp kernels are never selected below WIDE_PROG_MIN
+            inc = ('#include "eri_class_%s.h"\nnamespace gs { template <> struct WideProg<%d, %d, %d, %d> '
+                   '{ static constexpr int NVSLOT = 1, NVSEG = 0, HSIZE = 1, NHLEV = 0; '
+                   'static __device__ const uint4* vrec() { return nullptr; } '
+                   'static __device__ const int* vseg() { return nullptr; } '
+                   'static __device__ const unsigned short* vtgt() { return nullptr; } '
+                   'static __device__ const unsigned int* hop() { return nullptr; } '
+                   'static __device__ const int* hlev() { return nullptr; } '
+                   'static __device__ const unsigned short* outslot() { return nullptr; } }; }\n'
+                   % (tag, *cls))
+        code = ('#define GS_WIDE64_MIN %d\n#define GS_WIDE32_MIN %d\n#include "eri_launch.cuh"\n%s'
+                'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
+                '    return gs::launch_any<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
+                % (max(WIDE64_MIN, WIDE_PROG_MIN), max(WIDE32_MIN, WIDE_PROG_MIN), inc, tag, *cls))
         if not os.path.exists(path) or open(path).read() != code:
             with open(path, "w") as f:
                 f.write(code)
         deps = [os.path.join(GEN, f"eri_class_{tag}.h")]
-        if sum(cls) > THREAD_LMAX_TOTAL:
+        if L >= WIDE_PROG_MIN:
             deps.append(os.path.join(GEN, f"eri_wide_{tag}.h"))
         units.append((path, deps))
     return units
@@ -98,7 +109,7 @@ def generate():
 
 def _compile(src, deps, obj):
     common = [os.path.join(CSRC, n) for n in ("eri_common.cuh", "eri_kernels.cuh", "eri_wide.cuh",
-                                              "gs_args.h")]
+                                              "eri_launch.cuh", "gs_args.h")]
     common.append(os.path.join(GEN, "boys_table.h"))
     key = _digest([src] + deps + common, " ".join(NVFLAGS))
     stamp = obj + ".key"
@@ -117,6 +128,7 @@ def build(jobs=None, verbose=False):
     todo.append((os.path.join(CSRC, "capi.cu"), [os.path.join(GEN, "gs_built_classes.h")],
                  os.path.join(BUILD, "capi.o")))
     todo.append((os.path.join(CSRC, "one_electron.cu"), [], os.path.join(BUILD, "one_electron.o")))
+    todo.append((os.path.join(CSRC, "grad.cu"), [], os.path.join(BUILD, "grad.o")))
     jobs = jobs or max(1, os.cpu_count() or 1)
     changed = False
     with cf.ThreadPoolExecutor(jobs) as ex:

@@ -5,6 +5,7 @@
 // gs_launch_<class>.
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
 #include "eri_common.cuh"
 #include "gs_args.h"
 
@@ -180,26 +181,22 @@ __global__ void __launch_bounds__(kBlock) k_schwarz(const SchwarzArgs a) {
     a.q[p] = sqrt(m);
 }
 
-template <int LA, int LB, int LC, int LD>
-int launch_class(int kind, int prec, const void* args, cudaStream_t st) {
+template <int LA, int LB, int LC, int LD, int PREC>
+int launch_class(int kind, const void* args, cudaStream_t st) {
+    using T = typename std::conditional<PREC == 64, double, float>::type;
     if (kind == GS_KIND_WRITE) {
         const WriteArgs& a = *(const WriteArgs*)args;
         if (a.ntask <= 0) return 0;
-        const int grid = (a.ntask + kBlock - 1) / kBlock;
-        if (prec == 64) k_eri_write<LA, LB, LC, LD, double><<<grid, kBlock, 0, st>>>(a);
-        else k_eri_write<LA, LB, LC, LD, float><<<grid, kBlock, 0, st>>>(a);
+        k_eri_write<LA, LB, LC, LD, T><<<(a.ntask + kBlock - 1) / kBlock, kBlock, 0, st>>>(a);
     } else if (kind == GS_KIND_JK) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
-        const int grid = (a.ntask + kBlock - 1) / kBlock;
-        if (prec == 64) k_eri_jk<LA, LB, LC, LD, double><<<grid, kBlock, 0, st>>>(a);
-        else k_eri_jk<LA, LB, LC, LD, float><<<grid, kBlock, 0, st>>>(a);
+        k_eri_jk<LA, LB, LC, LD, T><<<(a.ntask + kBlock - 1) / kBlock, kBlock, 0, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
-        if constexpr (LA == LC && LB == LD) {
+        if constexpr (LA == LC && LB == LD && PREC == 64) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;
             if (a.npair <= 0) return 0;
-            const int grid = (a.npair + kBlock - 1) / kBlock;
-            k_schwarz<LA, LB, double><<<grid, kBlock, 0, st>>>(a);
+            k_schwarz<LA, LB, double><<<(a.npair + kBlock - 1) / kBlock, kBlock, 0, st>>>(a);
         } else {
             return GS_ERR_CLASS;
         }

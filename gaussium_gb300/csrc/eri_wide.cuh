@@ -11,6 +11,7 @@
 //   4. epilogue: block write, J/K digestion or Schwarz reduction.
 // The node programs come from gen_eri.py (WideProg<...> tables).
 #pragma once
+#include <type_traits>
 #include "eri_common.cuh"
 #include "gs_args.h"
 
@@ -320,48 +321,36 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
     if (lane == 0) a.q[p] = sqrt(m);
 }
 
-template <int LA, int LB, int LC, int LD>
-int launch_wide(int kind, int prec, const void* args, cudaStream_t st) {
+template <typename K>
+int set_smem(K k, size_t sh) {
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)
+               ? GS_ERR_CUDA : 0;
+}
+
+template <int LA, int LB, int LC, int LD, int PREC>
+int launch_wide(int kind, const void* args, cudaStream_t st) {
+    using T = typename std::conditional<PREC == 64, double, float>::type;
+    using Lay = WideLayout<LA, LB, LC, LD, T>;
     constexpr int TPB = 32 * kWideWarps;
     if (kind == GS_KIND_WRITE) {
         const WriteArgs& a = *(const WriteArgs*)args;
         if (a.ntask <= 0) return 0;
-        const int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
-        if (prec == 64) {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES_W;
-            auto k = k_wide_write<LA, LB, LC, LD, double>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
-            k<<<grid, TPB, sh, st>>>(a);
-        } else {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES_W;
-            auto k = k_wide_write<LA, LB, LC, LD, float>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
-            k<<<grid, TPB, sh, st>>>(a);
-        }
+        auto k = k_wide_write<LA, LB, LC, LD, T>;
+        if (set_smem(k, Lay::BYTES_W)) return GS_ERR_CUDA;
+        k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_W, st>>>(a);
     } else if (kind == GS_KIND_JK) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
-        const int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
-        if (prec == 64) {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES_JK;
-            auto k = k_wide_jk<LA, LB, LC, LD, double>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
-            k<<<grid, TPB, sh, st>>>(a);
-        } else {
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, float>::BYTES_JK;
-            auto k = k_wide_jk<LA, LB, LC, LD, float>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
-            k<<<grid, TPB, sh, st>>>(a);
-        }
+        auto k = k_wide_jk<LA, LB, LC, LD, T>;
+        if (set_smem(k, Lay::BYTES_JK)) return GS_ERR_CUDA;
+        k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_JK, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
-        if constexpr (LA == LC && LB == LD) {
+        if constexpr (LA == LC && LB == LD && PREC == 64) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;
             if (a.npair <= 0) return 0;
-            const int grid = (a.npair + kWideWarps - 1) / kWideWarps;
-            constexpr size_t sh = WideLayout<LA, LB, LC, LD, double>::BYTES_W;
             auto k = k_wide_schwarz<LA, LB, double>;
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
-            k<<<grid, TPB, sh, st>>>(a);
+            if (set_smem(k, Lay::BYTES_W)) return GS_ERR_CUDA;
+            k<<<(a.npair + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_W, st>>>(a);
         } else {
             return GS_ERR_CLASS;
         }

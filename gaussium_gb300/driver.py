@@ -25,9 +25,12 @@ class TimedFock(FockMatrixRestrictedGPU):
 
 
 def rhf(mol, basis="6-31G*", schwarz_thr=1e-12, mixed_cut=None, screen_thr=0.0,
-        incremental=False, reset_every=8, threshold=1e-10, max_iter=100, engine=None):
+        incremental=False, reset_every=8, threshold=1e-10, max_iter=100, engine=None,
+        final_fp64=False):
     """RHF total energy of ``mol``.  Returns a dict with the energy, iteration count,
-    per-build Fock times and the engine (reusable across calls on the same geometry)."""
+    per-build Fock times and the engine (reusable across calls on the same geometry).
+    ``final_fp64`` re-evaluates the converged density's Fock matrix with a full FP64 build
+    for the reported energy (the mixed/incremental builds only steer the iterations)."""
     sb = engine.sb if engine is not None else shell_basis(mol, basis)
     t0 = time.perf_counter()
     S, T, V = one_electron(sb, mol.coords, mol.charges)
@@ -40,8 +43,14 @@ def rhf(mol, basis="6-31G*", schwarz_thr=1e-12, mixed_cut=None, screen_thr=0.0,
     fb = TimedFock(hcore, engine, screen_thr=screen_thr, mixed_cut=mixed_cut,
                    incremental=incremental, reset_every=reset_every)
     res = scf.restricted_scf(S, hcore, mol.electrons, fb, threshold=threshold, max_iter=max_iter)
+    e_el = res.energy
+    if final_fp64:
+        fin = TimedFock(hcore, engine)
+        f = fin.create(res.density)
+        e_el = scf.total_energy_restricted(hcore, res.density, f)
+        fb.builds.extend(fin.builds)
     e_nuc = mol.nuclear_repulsion()
-    return dict(energy=res.energy + e_nuc, electronic=res.energy, iterations=res.iterations,
+    return dict(energy=e_el + e_nuc, electronic=e_el, iterations=res.iterations,
                 converged=res.converged, fock_seconds=list(fb.builds), one_electron_s=t1 - t0,
                 setup_s=t2 - t1, nbf=sb.nbf, ntasks=engine.ntasks, engine=engine,
-                density=res.density)
+                density=res.density, scf_energy=res.energy + e_nuc)

@@ -1,0 +1,207 @@
+"""Analytic RHF nuclear gradients (new: the reference optimises geometries with
+Nelder-Mead on energies, geometryoptimization/nelder_mead.py:28-144).
+
+dE/dR = sum P dH/dR - sum W dS/dR + sum Gamma d(ab|cd)/dR + dE_nuc/dR, with
+W = 2 sum_occ e_k C_k C_k^T and Gamma_abcd = 1/2 P_ab P_cd - 1/8 (P_ac P_bd + P_ad P_bc).
+
+Derivative integrals come from "raised" shells (l+1, primitive coefficients times
+2 alpha, unit component scales) and "lowered" shells (l-1):
+    d phi_a / dA_x = 2 alpha phi_{a+1x} - a_x phi_{a-1x},
+evaluated by the same one-electron and ERI class kernels as the energy; the ERI part is
+contracted with Gamma by the adjoint kernel gs_eri_grad_contract.  The nuclear-attraction
+operator derivative uses translational invariance per nucleus.
+
+``EnergyGradient`` wraps energy and gradient as a torch.autograd.Function of the
+nuclear coordinates.
+"""
+import numpy as np
+import torch
+
+from . import _lib, scf
+from .basis import ShellBasis
+from .engine import DeviceShells, JKEngine, QuartetBatch
+from .fock import FockMatrixRestrictedGPU
+from .hamiltonian import one_electron
+from .molecules import Molecule, shell_basis
+
+_COMP = {0: [(0, 0, 0)], 1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)],
+         2: [(2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)]}
+
+
+def _idx(lmn):
+    return _COMP[sum(lmn)].index(tuple(lmn))
+
+
+def combined_basis(sb: ShellBasis):
+    """Original shells, then a raised copy of every shell, then a lowered copy of every
+    shell with l >= 1.  Returns the ShellBasis and the raised/lowered shell indices."""
+    if np.any(sb.l >= 2):
+        raise NotImplementedError("gradients need f-type raised shells for d functions; "
+                                  "supported for s/p basis sets")
+    ns = sb.nshell
+    l, cen, expo, coef, scale, off = [], [], [], [], [], [0]
+
+    def add(ll, s, cf, sc):
+        k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
+        l.append(ll)
+        cen.append(sb.centre[s])
+        expo.extend(sb.expo[k0:k1])
+        coef.extend(cf)
+        off.append(len(expo))
+        scale.append(sc)
+
+    for s in range(ns):
+        add(int(sb.l[s]), s, sb.coef[sb.prim_off[s]:sb.prim_off[s + 1]], sb.comp_scale[s])
+    raised = np.arange(ns, 2 * ns)
+    for s in range(ns):
+        k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
+        add(int(sb.l[s]) + 1, s, sb.coef[k0:k1] * 2.0 * sb.expo[k0:k1], np.ones(6))
+    lowered = np.full(ns, -1)
+    for s in range(ns):
+        if sb.l[s] >= 1:
+            lowered[s] = len(l)
+            add(int(sb.l[s]) - 1, s, sb.coef[sb.prim_off[s]:sb.prim_off[s + 1]], np.ones(6))
+    comb = ShellBasis(l, np.array(cen), off, np.array(expo), np.array(coef), np.array(scale))
+    return comb, raised, lowered
+
+
+def _derivative_rows(sb, comb, raised, lowered, M):
+    """For matrix M over (combined x original) functions, D[x][i, j] = d M_ij / d(centre of i)_x."""
+    n = sb.nbf
+    D = np.zeros((3, n, n))
+    for s in range(sb.nshell):
+        ls = int(sb.l[s])
+        for ci, lmn in enumerate(_COMP[ls]):
+            i = sb.func_off[s] + ci
+            for x in range(3):
+                up = list(lmn)
+                up[x] += 1
+                r = comb.func_off[raised[s]] + _idx(up)
+                v = M[r, :n].copy()
+                if lmn[x] > 0:
+                    dn = list(lmn)
+                    dn[x] -= 1
+                    v -= lmn[x] * M[comb.func_off[lowered[s]] + _idx(dn), :n]
+                D[x, i] = sb.comp_scale[s, ci] * v
+    return D
+
+
+def one_electron_gradient(sb, mol, shell_atom, P, W):
+    comb, raised, lowered = combined_basis(sb)
+    func_atom = np.repeat(shell_atom, sb.nfunc)
+    g = np.zeros((len(mol.symbols), 3))
+    S, T, _ = one_electron(comb, mol.coords[:1], np.zeros(1))
+    dS = _derivative_rows(sb, comb, raised, lowered, S)
+    dT = _derivative_rows(sb, comb, raised, lowered, T)
+    for x in range(3):
+        contrib = 2.0 * np.sum(P * dT[x] - W * dS[x], axis=1)
+        np.add.at(g[:, x], func_atom, contrib)
+    for c in range(len(mol.symbols)):
+        _, _, Vc = one_electron(comb, mol.coords[c:c + 1], mol.charges[c:c + 1])
+        dV = _derivative_rows(sb, comb, raised, lowered, Vc)
+        for x in range(3):
+            h = 2.0 * np.sum(P * dV[x], axis=1)
+            np.add.at(g[:, x], func_atom, h)
+            g[c, x] -= h.sum()
+    return g
+
+
+def nuclear_repulsion_gradient(mol):
+    R, Z = mol.coords, mol.charges
+    g = np.zeros_like(R)
+    for a in range(len(Z)):
+        d = R[a] - R
+        r = np.linalg.norm(d, axis=1)
+        r[a] = np.inf
+        g[a] = -np.sum((Z[a] * Z / r ** 3)[:, None] * d, axis=0)
+    return g
+
+
+def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom):
+    comb, raised, lowered = combined_basis(sb)
+    tasks = engine.tasks[:engine.ntasks].cpu().numpy()
+    ps = engine.pairs.host_shells
+    quart = np.concatenate([ps[tasks[:, 0]], ps[tasks[:, 1]]], axis=1).astype(np.int64)
+    nq = len(quart)
+    mods = []
+    owner = []
+    slot = []
+    for cen in range(3):
+        s = quart[:, cen]
+        up = quart.copy()
+        up[:, cen] = raised[s]
+        mods.append(up); owner.append(np.arange(nq)); slot.append(np.full(nq, 2 * cen))
+        has = lowered[s] >= 0
+        dn = quart[has].copy()
+        dn[:, cen] = lowered[s[has]]
+        mods.append(dn); owner.append(np.flatnonzero(has)); slot.append(np.full(has.sum(), 2 * cen + 1))
+    mods = np.concatenate(mods)
+    owner = np.concatenate(owner)
+    slot = np.concatenate(slot)
+    ds = DeviceShells(comb, engine.dev)
+    batch = QuartetBatch(ds, mods, want32=False)
+    blocks = torch.zeros(max(1, batch.total), dtype=torch.float64, device=engine.dev)
+    batch.run(blocks, 64)
+    boff = np.full((nq, 6), -1, dtype=np.int64)
+    boff[owner, slot] = batch.offsets[:-1]
+    dev = engine.dev
+    t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt)).to(dev)
+    grad = torch.zeros(natom * 3, dtype=torch.float64, device=dev)
+    pt = torch.as_tensor(np.ascontiguousarray(P)).to(dev)
+    qd, bd = t(quart, np.int32), t(boff, np.int64)
+    L = _lib.lib()
+    _lib.check(L.gs_eri_grad_contract(nq, _lib.ptr(qd), _lib.ptr(bd), _lib.ptr(blocks),
+                                      _lib.ptr(engine.ds.l), _lib.ptr(engine.ds.func_off),
+                                      _lib.ptr(engine.ds.comp_scale),
+                                      _lib.ptr(t(shell_atom, np.int32)), sb.nbf, _lib.ptr(pt),
+                                      _lib.ptr(grad), _lib.stream()), "gs_eri_grad_contract")
+    return grad.view(natom, 3).cpu().numpy()
+
+
+def shell_atoms(mol, sb):
+    """Atom index of every shell (shells are generated atom by atom)."""
+    out = np.empty(sb.nshell, dtype=np.int64)
+    for s in range(sb.nshell):
+        d = np.linalg.norm(mol.coords - sb.centre[s], axis=1)
+        out[s] = int(np.argmin(d))
+    return out
+
+
+def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14):
+    """Converged RHF energy and analytic gradient (Eh, Eh/bohr)."""
+    sb = shell_basis(mol, basis)
+    S, T, V = one_electron(sb, mol.coords, mol.charges)
+    hcore = T + V
+    eng = JKEngine(sb, schwarz_thr=schwarz_thr)
+    fb = FockMatrixRestrictedGPU(hcore, eng)
+    res = scf.restricted_scf(S, hcore, mol.electrons, fb, threshold=threshold, max_iter=200)
+    if not res.converged:
+        raise RuntimeError("SCF did not converge")
+    nocc = mol.electrons // 2
+    la = scf.LinearAlgebra(S)
+    eps, C = la.diagonalize(res.fock)
+    P = 2.0 * C[:, :nocc] @ C[:, :nocc].T
+    W = 2.0 * (C[:, :nocc] * eps[:nocc]) @ C[:, :nocc].T
+    sa = shell_atoms(mol, sb)
+    g = one_electron_gradient(sb, mol, sa, P, W)
+    g += eri_gradient(sb, eng, sa, P, len(mol.symbols))
+    g += nuclear_repulsion_gradient(mol)
+    energy = res.energy + mol.nuclear_repulsion()
+    return energy, g, res
+
+
+class EnergyGradient(torch.autograd.Function):
+    """E(R) for nuclear coordinates R (natom x 3, bohr) with the analytic gradient as its
+    backward pass."""
+
+    @staticmethod
+    def forward(ctx, coords, symbols, basis):
+        mol = Molecule(symbols, coords.detach().cpu().numpy())
+        e, g, _ = rhf_energy_gradient(mol, basis)
+        ctx.save_for_backward(torch.as_tensor(g, dtype=coords.dtype))
+        return torch.tensor(e, dtype=coords.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (g,) = ctx.saved_tensors
+        return grad_out * g, None, None

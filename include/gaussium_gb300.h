@@ -123,6 +123,21 @@ int gs_one_electron(const double* centre, const int* l, const int* prim_off, con
                     const double* atom_xyz, const double* atom_z, double* S, double* T,
                     double* V, void* stream);
 
+/* K6 ERI adjoint.  For nq unique shell quartets quartets[4*q] = (A,B,C,D) it contracts the
+ * derivative integrals with the RHF weights
+ *   Gamma_abcd = w (1/2 P_ab P_cd - 1/8 (P_ac P_bd + P_ad P_bc)),  w = orbit size,
+ * and adds dE/dR into grad[natom*3] (FP64 atomics) through shell_atom[] (D by
+ * translational invariance).  block_off[6*q + 2*c] / [6*q + 2*c + 1] give the offsets in
+ * blocks[] of the raised / lowered block of centre c (A, B, C) in (A,B,C,D) order (-1 if
+ * absent), as written by gs_eri_blocks for the raised shell (l+1, coefficients times
+ * 2 alpha, unit component scales) and the lowered shell (l-1).  No reference counterpart:
+ * the reference has no gradients and optimises with Nelder-Mead
+ * (geometryoptimization/nelder_mead.py:28-144). */
+int gs_eri_grad_contract(int nq, const int* quartets, const long long* block_off,
+                         const double* blocks, const int* l, const int* func_off,
+                         const double* comp_scale, const int* shell_atom, int nbf,
+                         const double* density, double* grad, void* stream);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);
