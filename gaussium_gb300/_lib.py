@@ -23,6 +23,11 @@ _SIGS = {
     "gs_schwarz": (I, [I, I, P, P, P, I, P, P, I, P]),
     "gs_eri_blocks": (I, [I, I, I, I, I, P, P, P, I, P, P, P]),
     "gs_fock_jk": (I, [I, I, I, I, I, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, D, P]),
+    "gs_fock_jk_batched": (I, [I, I, I, I, I, P, P, P, P, P, P, P, P, ctypes.c_longlong, I, P,
+                               P, P, I, P, P, D, D, D, P]),
+    "gs_fock_jk_mixed_workspace": (ctypes.c_longlong, [I]),
+    "gs_fock_jk_mixed": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, P,
+                             ctypes.c_longlong, P]),
     "gs_boys_eval": (I, [I, I, I, P, P, P]),
     "gs_fma_probe": (I, [I, I, I, I, P, P]),
     "gs_one_electron": (I, [P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),

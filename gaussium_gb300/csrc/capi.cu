@@ -52,6 +52,48 @@ __global__ void k_boys(int n, const double* __restrict__ t, double* __restrict__
     for (int m = 0; m <= M; ++m) F[(size_t)i * (M + 1) + m] = (double)f[m];
 }
 
+// Split a class's quartet tasks by their density-weighted Schwarz estimate
+//   est = qmax_bra * qmax_ket * max |P| over the quartet's six shell blocks
+// into an FP64 list (est >= cut), an FP32 list (thr <= est < cut) and dropped (est < thr).
+// Warp-aggregated atomics keep each warp's survivors contiguous, so the primitive-count
+// order of the input survives approximately.
+__global__ void k_partition(int ntask, const int2* __restrict__ tasks,
+                            const gs::PairRec* __restrict__ pairs,
+                            const double* __restrict__ dmax, int nshell, double thr, double cut,
+                            int2* __restrict__ out64, int2* __restrict__ out32,
+                            int* __restrict__ counts) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int kind = 0;
+    int2 task = make_int2(0, 0);
+    if (t < ntask) {
+        task = tasks[t];
+        const gs::PairRec B = pairs[task.x];
+        const gs::PairRec K = pairs[task.y];
+        const int n = nshell;
+        double dm = dmax[B.sa * n + B.sb];
+        dm = fmax(dm, dmax[K.sa * n + K.sb]);
+        dm = fmax(dm, dmax[B.sa * n + K.sa]);
+        dm = fmax(dm, dmax[B.sa * n + K.sb]);
+        dm = fmax(dm, dmax[B.sb * n + K.sa]);
+        dm = fmax(dm, dmax[B.sb * n + K.sb]);
+        const double est = (double)B.qmax * (double)K.qmax * dm;
+        kind = est < thr ? 0 : (est >= cut ? 1 : 2);
+    }
+    const unsigned lane = threadIdx.x & 31;
+    for (int which = 1; which <= 2; ++which) {
+        const unsigned m = __ballot_sync(0xffffffffu, kind == which);
+        if (!m) continue;
+        int base = 0;
+        const int leader = __ffs(m) - 1;
+        if ((int)lane == leader) base = atomicAdd(counts + which - 1, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (kind == which) {
+            const int pos = base + __popc(m & ((1u << lane) - 1));
+            (which == 1 ? out64 : out32)[pos] = task;
+        }
+    }
+}
+
 // Peak-rate probe: each thread runs `iters` rounds of 8 independent FMA chains.
 template <typename T>
 __global__ void k_fma(int iters, T seed, T* __restrict__ sink) {
@@ -170,7 +212,125 @@ int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_r
     a.screen_thr = screen_thr;
     a.prec_lo = prec_lo;
     a.prec_hi = prec_hi;
+    a.shell_mol = nullptr;
+    a.mol_base = nullptr;
+    a.mol_n = nullptr;
+    a.mol_dmax = nullptr;
+    a.mat_stride = (long long)nbf * nbf;
+    a.ntask_dev = nullptr;
     return f(GS_KIND_JK, precision, &a, S(stream));
+}
+
+int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
+                       const void* prim, const double* comp_scale, const int* func_off,
+                       const int* shell_mol, const long long* mol_base, const int* mol_n,
+                       const double* mol_dmax, long long mat_stride, int ntask, const int* tasks,
+                       const double* pj, double* j, int nk, const double* pk, double* k,
+                       double screen_thr, double prec_lo, double prec_hi, void* stream) {
+    launch_fn f = find_class(la, lb, lc, ld);
+    if (!f) return GS_ERR_CLASS;
+    if ((precision != 64 && precision != 32) || ntask < 0 || nk < 0 || nk > 1 || !pair_rec ||
+        !prim || !comp_scale || !func_off || !shell_mol || !mol_base || !mol_n ||
+        (ntask > 0 && !tasks) || (!!pj != !!j) || (nk > 0 && (!pk || !k)) ||
+        (screen_thr > 0 && !mol_dmax) || mat_stride <= 0)
+        return GS_ERR_ARG;
+    gs::JKArgs a;
+    a.pairs = (const gs::PairRec*)pair_rec;
+    a.prims = prim;
+    a.comp_scale = comp_scale;
+    a.func_off = func_off;
+    a.tasks = (const int2*)tasks;
+    a.ntask = ntask;
+    a.nbf = 0;
+    a.nshell = 0;
+    a.nk = nk;
+    a.pj = pj;
+    a.pk = pk;
+    a.j = j;
+    a.k = k;
+    a.shell_dmax = nullptr;
+    a.screen_thr = screen_thr;
+    a.prec_lo = prec_lo;
+    a.prec_hi = prec_hi;
+    a.shell_mol = shell_mol;
+    a.mol_base = mol_base;
+    a.mol_n = mol_n;
+    a.mol_dmax = mol_dmax;
+    a.mat_stride = mat_stride;
+    a.ntask_dev = nullptr;
+    return f(GS_KIND_JK, precision, &a, S(stream));
+}
+
+// Bytes of workspace gs_fock_jk_mixed needs for ntask tasks.
+long long gs_fock_jk_mixed_workspace(int ntask) {
+    return 256 + 2 * (long long)(ntask > 0 ? ntask : 0) * (long long)sizeof(int2);
+}
+
+namespace {
+int fock_jk_mixed_impl(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
+                       const void* prim32, const double* comp_scale, const int* func_off,
+                       int nshell, int nbf, int ntask, const int* tasks, const double* pj,
+                       double* j, int nk, const double* pk, double* k,
+                       const double* shell_dmax, double screen_thr, double mixed_cut,
+                       void* workspace, long long ws_bytes, void* stream) {
+    launch_fn f = find_class(la, lb, lc, ld);
+    if (!f) return GS_ERR_CLASS;
+    if (ntask < 0 || nbf <= 0 || nk < 0 || !pair_rec || !prim64 || !prim32 || !comp_scale ||
+        !func_off || (ntask > 0 && !tasks) || (!!pj != !!j) || (nk > 0 && (!pk || !k)) ||
+        !shell_dmax || !workspace)
+        return GS_ERR_ARG;
+    if (ws_bytes < gs_fock_jk_mixed_workspace(ntask)) return GS_ERR_NOMEM;
+    if (ntask == 0) return GS_OK;
+    int* counts = (int*)workspace;
+    int2* l64 = (int2*)((char*)workspace + 256);
+    int2* l32 = l64 + ntask;
+    if (cudaMemsetAsync(counts, 0, 2 * sizeof(int), S(stream)) != cudaSuccess) return GS_ERR_CUDA;
+    k_partition<<<(ntask + 255) / 256, 256, 0, S(stream)>>>(
+        ntask, (const int2*)tasks, (const gs::PairRec*)pair_rec, shell_dmax, nshell, screen_thr,
+        mixed_cut, l64, l32, counts);
+    if (check_launch()) return GS_ERR_CUDA;
+    gs::JKArgs a;
+    a.pairs = (const gs::PairRec*)pair_rec;
+    a.comp_scale = comp_scale;
+    a.func_off = func_off;
+    a.ntask = ntask;
+    a.nbf = nbf;
+    a.nshell = nshell;
+    a.nk = nk;
+    a.pj = pj;
+    a.pk = pk;
+    a.j = j;
+    a.k = k;
+    a.shell_dmax = nullptr;
+    a.screen_thr = 0.0;
+    a.prec_lo = 0.0;
+    a.prec_hi = 0.0;
+    a.shell_mol = nullptr;
+    a.mol_base = nullptr;
+    a.mol_n = nullptr;
+    a.mol_dmax = nullptr;
+    a.mat_stride = (long long)nbf * nbf;
+    a.prims = prim64;
+    a.tasks = l64;
+    a.ntask_dev = counts;
+    int rc = f(GS_KIND_JK, 64, &a, S(stream));
+    if (rc) return rc;
+    a.prims = prim32;
+    a.tasks = l32;
+    a.ntask_dev = counts + 1;
+    return f(GS_KIND_JK, 32, &a, S(stream));
+}
+}  // namespace
+
+int gs_fock_jk_mixed(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
+                     const void* prim32, const double* comp_scale, const int* func_off,
+                     int nshell, int nbf, int ntask, const int* tasks, const double* pj, double* j,
+                     int nk, const double* pk, double* k, const double* shell_dmax,
+                     double screen_thr, double mixed_cut, void* workspace, long long ws_bytes,
+                     void* stream) {
+    return fock_jk_mixed_impl(la, lb, lc, ld, pair_rec, prim64, prim32, comp_scale, func_off,
+                              nshell, nbf, ntask, tasks, pj, j, nk, pk, k, shell_dmax, screen_thr,
+                              mixed_cut, workspace, ws_bytes, stream);
 }
 
 int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream) {

@@ -56,20 +56,32 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs 
     using G = ClassGen<LA, LB, LC, LD>;
     constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.ntask) return;
+    if (t >= (a.ntask_dev ? *a.ntask_dev : a.ntask)) return;
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
+    int n = a.nbf;
+    long long mbase = 0;
+    if (a.shell_mol) {
+        const int m = a.shell_mol[B.sa];
+        n = a.mol_n[m];
+        mbase = a.mol_base[m];
+    }
     if (a.screen_thr > 0.0) {
         // density-weighted Schwarz screening and precision selection
         const double bound = (double)B.qmax * (double)K.qmax;
-        const int n = a.nshell;
-        double dm = a.shell_dmax[B.sa * n + B.sb];
-        dm = fmax(dm, a.shell_dmax[K.sa * n + K.sb]);
-        dm = fmax(dm, a.shell_dmax[B.sa * n + K.sa]);
-        dm = fmax(dm, a.shell_dmax[B.sa * n + K.sb]);
-        dm = fmax(dm, a.shell_dmax[B.sb * n + K.sa]);
-        dm = fmax(dm, a.shell_dmax[B.sb * n + K.sb]);
+        double dm;
+        if (a.shell_mol) {
+            dm = a.mol_dmax[a.shell_mol[B.sa]];
+        } else {
+            const int ns = a.nshell;
+            dm = a.shell_dmax[B.sa * ns + B.sb];
+            dm = fmax(dm, a.shell_dmax[K.sa * ns + K.sb]);
+            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sa]);
+            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sb]);
+            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sa]);
+            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sb]);
+        }
         const double est = bound * dm;
         if (est < a.screen_thr) return;
         if (est < a.prec_lo || est >= a.prec_hi) return;
@@ -92,11 +104,11 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs 
             GS_UNROLL for (int cd = 0; cd < NC * ND; ++cd)
                 sc[ab * NC * ND + cd] = blk[ab * NC * ND + cd] * (sab[ab] * scd[cd]);
     }
-    const int n = a.nbf;
     const int fa = a.func_off[B.sa], fb = a.func_off[B.sb];
     const int fc = a.func_off[K.sa], fd = a.func_off[K.sb];
     if (a.j) {
-        const double* P = a.pj;
+        const double* P = a.pj + mbase;
+        double* Jo = a.j + mbase;
         T pab[NA * NB], pcd[NC * ND];
         GS_UNROLL for (int i = 0; i < NA; ++i)
             GS_UNROLL for (int j = 0; j < NB; ++j) pab[i * NB + j] = (T)P[(fa + i) * n + fb + j];
@@ -113,14 +125,14 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs 
             }
         GS_UNROLL for (int i = 0; i < NA; ++i)
             GS_UNROLL for (int j = 0; j < NB; ++j)
-                atomicAdd(a.j + (fa + i) * n + fb + j, 2.0 * (double)jab[i * NB + j]);
+                atomicAdd(Jo + (fa + i) * n + fb + j, 2.0 * (double)jab[i * NB + j]);
         GS_UNROLL for (int i = 0; i < NC; ++i)
             GS_UNROLL for (int j = 0; j < ND; ++j)
-                atomicAdd(a.j + (fc + i) * n + fd + j, 2.0 * (double)jcd[i * ND + j]);
+                atomicAdd(Jo + (fc + i) * n + fd + j, 2.0 * (double)jcd[i * ND + j]);
     }
     for (int s = 0; s < a.nk; ++s) {
-        const double* P = a.pk + (size_t)s * n * n;
-        double* Kout = a.k + (size_t)s * n * n;
+        const double* P = a.pk + (size_t)s * a.mat_stride + mbase;
+        double* Kout = a.k + (size_t)s * a.mat_stride + mbase;
         T pbd[NB * ND], pbc[NB * NC], pad[NA * ND], pac[NA * NC];
         GS_UNROLL for (int i = 0; i < NB; ++i)
             GS_UNROLL for (int j = 0; j < ND; ++j) pbd[i * ND + j] = (T)P[(fb + i) * n + fd + j];

@@ -209,19 +209,31 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_JK;
     const int t = blockIdx.x * kWideWarps + warp;
-    if (t >= a.ntask) return;
+    if (t >= (a.ntask_dev ? *a.ntask_dev : a.ntask)) return;
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
+    int n = a.nbf;
+    long long mbase = 0;
+    if (a.shell_mol) {
+        const int m = a.shell_mol[B.sa];
+        n = a.mol_n[m];
+        mbase = a.mol_base[m];
+    }
     if (a.screen_thr > 0.0) {
         const double bound = (double)B.qmax * (double)K.qmax;
-        const int n = a.nshell;
-        double dm = a.shell_dmax[B.sa * n + B.sb];
-        dm = fmax(dm, a.shell_dmax[K.sa * n + K.sb]);
-        dm = fmax(dm, a.shell_dmax[B.sa * n + K.sa]);
-        dm = fmax(dm, a.shell_dmax[B.sa * n + K.sb]);
-        dm = fmax(dm, a.shell_dmax[B.sb * n + K.sa]);
-        dm = fmax(dm, a.shell_dmax[B.sb * n + K.sb]);
+        double dm;
+        if (a.shell_mol) {
+            dm = a.mol_dmax[a.shell_mol[B.sa]];
+        } else {
+            const int ns = a.nshell;
+            dm = a.shell_dmax[B.sa * ns + B.sb];
+            dm = fmax(dm, a.shell_dmax[K.sa * ns + K.sb]);
+            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sa]);
+            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sb]);
+            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sa]);
+            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sb]);
+        }
         const double est = bound * dm;
         if (est < a.screen_thr || est < a.prec_lo || est >= a.prec_hi) return;
     }
@@ -239,27 +251,27 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
     const unsigned short* __restrict__ os = W::outslot();
     for (int e = lane; e < G::NBLK; e += 32) V[e] = sm[__ldg(os + e)] * (sab[e / NCD] * scd[e % NCD]);
     __syncwarp();
-    const int n = a.nbf;
     const int fa = a.func_off[B.sa], fb = a.func_off[B.sb];
     const int fc = a.func_off[K.sa], fd = a.func_off[K.sb];
     if (a.j) {
-        const double* P = a.pj;
+        const double* P = a.pj + mbase;
+        double* Jo = a.j + mbase;
         for (int ab = lane; ab < NAB; ab += 32) {
             T r = T(0);
             for (int cd = 0; cd < NCD; ++cd)
                 r = fma(V[ab * NCD + cd], (T)P[(fc + cd / ND) * n + fd + cd % ND], r);
-            atomicAdd(a.j + (fa + ab / NB) * n + fb + ab % NB, 2.0 * (double)r);
+            atomicAdd(Jo + (fa + ab / NB) * n + fb + ab % NB, 2.0 * (double)r);
         }
         for (int cd = lane; cd < NCD; cd += 32) {
             T r = T(0);
             for (int ab = 0; ab < NAB; ++ab)
                 r = fma(V[ab * NCD + cd], (T)P[(fa + ab / NB) * n + fb + ab % NB], r);
-            atomicAdd(a.j + (fc + cd / ND) * n + fd + cd % ND, 2.0 * (double)r);
+            atomicAdd(Jo + (fc + cd / ND) * n + fd + cd % ND, 2.0 * (double)r);
         }
     }
     for (int s = 0; s < a.nk; ++s) {
-        const double* P = a.pk + (size_t)s * n * n;
-        double* Ko = a.k + (size_t)s * n * n;
+        const double* P = a.pk + (size_t)s * a.mat_stride + mbase;
+        double* Ko = a.k + (size_t)s * a.mat_stride + mbase;
         // K'_ac += sum_bd v P_bd ; K'_ad += sum_bc v P_bc ; K'_bc += sum_ad v P_ad ; K'_bd += sum_ac v P_ac
         for (int x = lane; x < NA * NC; x += 32) {
             const int ia = x / NC, ic = x % NC;

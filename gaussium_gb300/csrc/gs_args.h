@@ -43,6 +43,15 @@ struct JKArgs {
     const double* shell_dmax;   // [nshell][nshell] max |P| per shell block (screening)
     double screen_thr;          // 0 disables screening and precision selection
     double prec_lo, prec_hi;    // evaluate only quartets with prec_lo <= bound < prec_hi
+    // batched mode (several molecules in one launch): shell -> molecule, and per molecule
+    // the offset of its nbf_m x nbf_m matrices, nbf_m, and max |P| (screening); func_off
+    // is then local to the molecule.  Null shell_mol: one molecule of nbf functions.
+    const int* shell_mol;
+    const long long* mol_base;
+    const int* mol_n;
+    const double* mol_dmax;
+    long long mat_stride;       // elements between the nk exchange densities / outputs
+    const int* ntask_dev;       // if set, the task count is read here (ntask is the bound)
 };
 
 struct SchwarzArgs {

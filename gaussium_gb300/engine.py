@@ -326,6 +326,21 @@ class JKEngine:
         L = _lib.lib()
         st = _lib.stream(stream)
         base = self.tasks.data_ptr()
+        if mixed_cut is not None:
+            need = max(L.gs_fock_jk_mixed_workspace(e - s) for _, s, e in self.segments)
+            if getattr(self, "_ws", None) is None or self._ws.numel() < need:
+                self._ws = torch.empty(int(need), dtype=torch.uint8, device=dev)
+            for cls, s, e in self.segments:
+                if classes is not None and cls not in classes:
+                    continue
+                rc = L.gs_fock_jk_mixed(*cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
+                                        _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale),
+                                        _lib.ptr(self.ds.func_off), self.sb.nshell, n, e - s,
+                                        base + s * 8, _lib.ptr(pj_c), _lib.ptr(jbuf), nk,
+                                        _lib.ptr(pk_c), _lib.ptr(kbuf), _lib.ptr(dmax), thr,
+                                        mixed_cut, _lib.ptr(self._ws), self._ws.numel(), st)
+                _lib.check(rc, f"gs_fock_jk_mixed{cls}")
+            runs = []
         for prec, lo, hi in runs:
             prims = self.pairs.prims(prec)
             for cls, s, e in self.segments:

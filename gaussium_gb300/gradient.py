@@ -167,7 +167,8 @@ def shell_atoms(mol, sb):
     return out
 
 
-def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14):
+def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
+                        want_gradient=True):
     """Converged RHF energy and analytic gradient (Eh, Eh/bohr)."""
     sb = shell_basis(mol, basis)
     S, T, V = one_electron(sb, mol.coords, mol.charges)
@@ -177,6 +178,8 @@ def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14):
     res = scf.restricted_scf(S, hcore, mol.electrons, fb, threshold=threshold, max_iter=200)
     if not res.converged:
         raise RuntimeError("SCF did not converge")
+    if not want_gradient:
+        return res.energy + mol.nuclear_repulsion(), None, res
     nocc = mol.electrons // 2
     la = scf.LinearAlgebra(S)
     eps, C = la.diagonalize(res.fock)

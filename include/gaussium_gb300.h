@@ -104,6 +104,36 @@ int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_r
                const double* pk, double* k, const double* shell_dmax, double screen_thr,
                double prec_lo, double prec_hi, void* stream);
 
+/* Bytes of device workspace gs_fock_jk_mixed needs for ntask tasks. */
+long long gs_fock_jk_mixed_workspace(int ntask);
+
+/* Mixed-precision form of gs_fock_jk (same replaced reference functions).  A partition
+ * kernel splits the ntask tasks by est = qmax_bra qmax_ket max|P| (over the quartet's six
+ * shell blocks, shell_dmax[nshell*nshell]): est >= mixed_cut -> FP64 (prim64 records),
+ * screen_thr <= est < mixed_cut -> FP32 (prim32 records), est < screen_thr -> skipped; the
+ * two lists and their counts live in the caller's workspace (ws_bytes >=
+ * gs_fock_jk_mixed_workspace(ntask)), and the two class launches read their counts there,
+ * so the call needs no host synchronisation.  Accumulation is FP64 in both cases. */
+int gs_fock_jk_mixed(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
+                     const void* prim32, const double* comp_scale, const int* func_off,
+                     int nshell, int nbf, int ntask, const int* tasks, const double* pj, double* j,
+                     int nk, const double* pk, double* k, const double* shell_dmax,
+                     double screen_thr, double mixed_cut, void* workspace, long long ws_bytes,
+                     void* stream);
+
+/* Batched form of gs_fock_jk for many molecules in one launch (the reference builds one
+ * molecule at a time; same replaced functions as gs_fock_jk).  shell_mol[s] is the
+ * molecule of shell s; molecule m's nbf_m x nbf_m matrices start at mol_base[m] in pj, j, pk
+ * and k, with nbf_m = mol_n[m]; func_off is local to each molecule.  nk <= 1 exchange
+ * density; mat_stride is the element count of one full set of matrices.  With
+ * screen_thr > 0 the density factor of the screening bound is mol_dmax[m]. */
+int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
+                       const void* prim, const double* comp_scale, const int* func_off,
+                       const int* shell_mol, const long long* mol_base, const int* mol_n,
+                       const double* mol_dmax, long long mat_stride, int ntask, const int* tasks,
+                       const double* pj, double* j, int nk, const double* pk, double* k,
+                       double screen_thr, double prec_lo, double prec_hi, void* stream);
+
 /* K2 Boys function F_0..F_m(t) (m <= 10) of n arguments t[] into F[n*(m+1)], in FP64 or
  * FP32 (results widened to FP64).  Replaces boys_function / boys_function_recursion
  * (integrals/boys_function.py:4-76). */
