@@ -121,8 +121,10 @@ class BatchedRHF:
         idx = np.full((B, N, N), -1, dtype=np.int64)
         for m, n in enumerate(self.nbf):
             idx[m, :n, :n] = self.base[m] + np.arange(n * n).reshape(n, n)
-        self.pad_idx = torch.as_tensor(idx).to(dev)
-        self.valid = self.pad_idx >= 0
+        flat = idx.reshape(-1)
+        pos = np.flatnonzero(flat >= 0)
+        self.pos_padded = torch.as_tensor(pos).to(dev)          # into [B*N*N]
+        self.pos_packed = torch.as_tensor(flat[pos]).to(dev)    # into packed storage
         S = torch.zeros((B, N, N), dtype=torch.float64, device=dev)
         H = torch.zeros_like(S)
         for m, n in enumerate(self.nbf):
@@ -130,12 +132,12 @@ class BatchedRHF:
             H[m, :n, :n] = torch.as_tensor(self.H[m]).to(dev)
             S[m, n:, n:] = torch.eye(N - n, dtype=torch.float64, device=dev)
         self.Sb, self.Hb = S, H
-        s, u = torch.linalg.eigh(S)
-        X = u * s.rsqrt().unsqueeze(1)
-        # padded orbitals: zero columns so they never enter the density
+        # canonical orthogonaliser per molecule (eigenvalues ascending, as the reference
+        # sorts them); padded orbitals are zero columns at positions n..N-1
+        X = torch.zeros_like(S)
         for m, n in enumerate(self.nbf):
-            X[m, n:, :] = 0
-            X[m, :, :] = X[m][:, torch.argsort(s[m])]
+            s, u = torch.linalg.eigh(S[m, :n, :n])
+            X[m, :n, :n] = u * s.rsqrt().unsqueeze(0)
         self.X = X
         self.nocc = torch.as_tensor([mol.electrons // 2 for mol in self.mols], device=dev)
         self.occ_mask = (torch.arange(N, device=dev)[None, :] < self.nocc[:, None]).double()
@@ -145,13 +147,13 @@ class BatchedRHF:
 
     def to_packed(self, Pb):
         out = torch.zeros(self.mat_stride, dtype=torch.float64, device=self.dev)
-        out[self.pad_idx[self.valid]] = Pb[self.valid]
+        out.index_copy_(0, self.pos_packed, Pb.reshape(-1).index_select(0, self.pos_padded))
         return out
 
     def to_padded(self, v):
-        Pb = torch.zeros((len(self.sbs), self.nmax, self.nmax), dtype=torch.float64, device=self.dev)
-        Pb[self.valid] = v[self.pad_idx[self.valid]]
-        return Pb
+        Pb = torch.zeros(len(self.sbs) * self.nmax * self.nmax, dtype=torch.float64, device=self.dev)
+        Pb.index_copy_(0, self.pos_padded, v.index_select(0, self.pos_packed))
+        return Pb.view(len(self.sbs), self.nmax, self.nmax)
 
     def _jk_launch(self, P, J, K, precision=64, mixed_cut=None, dmax=None):
         L = _lib.lib()

@@ -333,10 +333,15 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
     if (lane == 0) a.q[p] = sqrt(m);
 }
 
+// Raise a kernel's dynamic shared-memory limit once (the first launch happens before any
+// stream capture, so later launches inside a captured graph make no attribute call).
 template <typename K>
 int set_smem(K k, size_t sh) {
-    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)
-               ? GS_ERR_CUDA : 0;
+    static bool done = false;
+    if (done) return 0;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+    done = true;
+    return 0;
 }
 
 template <int LA, int LB, int LC, int LD, int PREC>

@@ -346,7 +346,7 @@ def main():
         with open(path, "w") as f:
             f.write(lst)
     for cls in classes:
-        if sum(cls) < 3:
+        if sum(cls) < 2:
             continue
         code, _ = emit_wide(cls)
         path = os.path.join(out, "eri_wide_%s.h" % "".join(map(str, cls)))
