@@ -62,6 +62,7 @@ def classes():
 def generate():
     os.makedirs(GEN, exist_ok=True)
     _run([sys.executable, os.path.join(CSRC, "gen_eri.py"), GEN, str(LMAX)])
+    _run([sys.executable, os.path.join(CSRC, "gen_grad.py"), GEN, "1"])
     table = os.path.join(GEN, "boys_table.h")
     gen_src = os.path.join(CSRC, "boys_table_gen.c")
     exe = os.path.join(BUILD, "boys_table_gen")
@@ -129,6 +130,10 @@ def build(jobs=None, verbose=False):
                  os.path.join(BUILD, "capi.o")))
     todo.append((os.path.join(CSRC, "one_electron.cu"), [], os.path.join(BUILD, "one_electron.o")))
     todo.append((os.path.join(CSRC, "grad.cu"), [], os.path.join(BUILD, "grad.o")))
+    todo.append((os.path.join(CSRC, "eri_grad.cu"),
+                 [os.path.join(CSRC, "eri_grad.cuh")] +
+                 [os.path.join(GEN, f"eri_grad_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110", "1111")],
+                 os.path.join(BUILD, "eri_grad.o")))
     jobs = jobs or max(1, os.cpu_count() or 1)
     changed = False
     with cf.ThreadPoolExecutor(jobs) as ex:

@@ -253,7 +253,7 @@ GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off,
             r.Pz = (a * A[2] + b * B[2]) * ip;
             r.PAx = r.Px - A[0]; r.PAy = r.Py - A[1]; r.PAz = r.Pz - A[2];
             r.Kp = kSqrt2Pi52 * S.coef[i] * S.coef[j] * exp(-a * b * ip * ab2) * ip;
-            r.pad = 0.0;
+            r.pad = a;          // exponent of the first shell (derivative weights)
             pd[n] = r;
             if (pf) {
                 PrimRec<float> f;

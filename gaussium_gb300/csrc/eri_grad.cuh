@@ -1,0 +1,250 @@
+// K6 fused ERI adjoint: one warp per unique shell quartet evaluates the derivative
+// integrals of all three independent centres from one VRR pass per primitive quartet
+// (four weighted contraction sets: 1, 2 alpha, 2 beta, 2 gamma), forms the raised and
+// lowered blocks by HRR in shared memory, contracts them with the RHF density weights
+//   Gamma_abcd = w (1/2 P_ab P_cd - 1/8 (P_ac P_bd + P_ad P_bc))   (w = orbit size)
+// and adds dE/dR of the four centres to the per-atom gradient (D by translational
+// invariance).  Programs come from gen_grad.py (GradProg<...>).
+#pragma once
+#include "eri_wide.cuh"
+
+namespace gs {
+
+template <int LA, int LB, int LC, int LD> struct GradProg;
+
+struct GradArgs {
+    const PairRec* pairs;
+    const PrimRec<double>* prims;   // pad holds the first shell's exponent
+    const double* comp_scale;
+    const int* func_off;
+    const int* shell_atom;
+    const int2* tasks;
+    int ntask;
+    int nbf;
+    const double* P;
+    double* grad;
+};
+
+constexpr int kGradWarps = 2;
+constexpr int kNCoefG = 36;
+
+template <int LA, int LB, int LC, int LD> struct GradLayout {
+    using W = GradProg<LA, LB, LC, LD>;
+    static constexpr int SC = kSetupBatch * kNCoefG;
+    static constexpr int SF = kSetupBatch * (W::L + 1);
+    static constexpr int VRR = SC + SF + W::NVSLOT;
+    static constexpr int WARP = VRR > W::HSIZE ? VRR : W::HSIZE;
+    static constexpr size_t BYTES = (size_t)WARP * sizeof(double) * kGradWarps;
+};
+
+__device__ __forceinline__ int g_ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+__device__ __forceinline__ void g_comp(int l, int k, int& x, int& y, int& z) {
+    if (l == 0) { x = y = z = 0; return; }
+    if (l == 1) { x = k == 0; y = k == 1; z = k == 2; return; }
+    if (l == 2) {
+        const int t[6][3] = {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}};
+        x = t[k][0]; y = t[k][1]; z = t[k][2]; return;
+    }
+    int c = 0;
+    for (int lx = l; lx >= 0; --lx)
+        for (int ly = l - lx; ly >= 0; --ly) {
+            if (c == k) { x = lx; y = ly; z = l - lx - ly; return; }
+            ++c;
+        }
+}
+
+__device__ __forceinline__ int g_index(int x, int y, int z) {
+    const int l = x + y + z;
+    if (l == 0) return 0;
+    if (l == 1) return x ? 0 : (y ? 1 : 2);
+    if (l == 2) {
+        if (x == 2) return 0;
+        if (y == 2) return 1;
+        if (z == 2) return 2;
+        if (x && y) return 3;
+        if (x && z) return 4;
+        return 5;
+    }
+    int c = 0;
+    for (int lx = l; lx >= 0; --lx)
+        for (int ly = l - lx; ly >= 0; --ly) {
+            if (lx == x && ly == y) return c;
+            ++c;
+        }
+    return -1;
+}
+
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) {
+    using W = GradProg<LA, LB, LC, LD>;
+    using Lay = GradLayout<LA, LB, LC, LD>;
+    constexpr int L = W::L;
+    constexpr int NACCW = (W::NACC + 31) / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double* sm = reinterpret_cast<double*>(smem_raw) + (size_t)warp * Lay::WARP;
+    const int t = blockIdx.x * kGradWarps + warp;
+    if (t >= a.ntask) return;
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    double acc[NACCW];
+    int accs[NACCW], acck[NACCW];
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) {
+        acc[k] = 0.0;
+        const int q = lane + 32 * k;
+        const unsigned e = q < W::NACC ? __ldg(W::acc() + q) : 0u;
+        accs[k] = e & 0xffff;
+        acck[k] = q < W::NACC ? (int)(e >> 16) : -1;
+    }
+    double* sC = sm;
+    double* sF = sm + Lay::SC;
+    double* node = sm + Lay::SC + Lay::SF;
+    const int nK = K.nprim;
+    const int ntot = B.nprim * nK;
+    const uint4* __restrict__ vrec = W::vrec();
+    const int* __restrict__ vseg = W::vseg();
+    for (int base = 0; base < ntot; base += kSetupBatch) {
+        const int i = base + lane;
+        if (i < ntot) {
+            const PrimRec<double> P = a.prims[B.prim_off + i / nK];
+            const PrimRec<double> Q = a.prims[K.prim_off + i % nK];
+            double* c = sC + lane * kNCoefG;
+            wide_setup_m<L, double>(P, Q, c, sF + lane * (L + 1));
+            c[32] = 2.0 * P.pad;               // 2 alpha (first bra shell)
+            c[33] = 2.0 * (P.p - P.pad);       // 2 beta
+            c[34] = 2.0 * Q.pad;               // 2 gamma (first ket shell)
+            c[35] = 1.0;
+        }
+        __syncwarp();
+        const int nb = min(kSetupBatch, ntot - base);
+        for (int j = 0; j < nb; ++j) {
+            const double* __restrict__ c = sC + j * kNCoefG;
+            if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
+            __syncwarp();
+            for (int s = 0; s < W::NVSEG; ++s) {
+                const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
+                const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
+                if (sync && s > 0) __syncwarp();
+                int n = lane;
+                uint4 ra = make_uint4(0, 0, 0, 0), rb = ra;
+                if (n < cnt) {
+                    ra = __ldg(vrec + 2 * (noff + n));
+                    rb = __ldg(vrec + 2 * (noff + n) + 1);
+                }
+                for (; n < cnt; n += 32) {
+                    const uint4 x = ra, y = rb;
+                    if (n + 32 < cnt) {
+                        ra = __ldg(vrec + 2 * (noff + n + 32));
+                        rb = __ldg(vrec + 2 * (noff + n + 32) + 1);
+                    }
+                    double r = c[x.y >> 16] * node[x.y & 0xffff];
+                    r = fma(c[x.z >> 16], node[x.z & 0xffff], r);
+                    if (nt > 2) r = fma(c[x.w >> 16], node[x.w & 0xffff], r);
+                    if (nt > 3) r = fma(c[y.x >> 16], node[y.x & 0xffff], r);
+                    if (nt > 4) r = fma(c[y.y >> 16], node[y.y & 0xffff], r);
+                    node[x.x & 0xffff] = r;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < NACCW; ++k) {
+                if (acck[k] >= 0) {
+                    const double w = acck[k] == 0 ? 1.0 : c[31 + acck[k]];
+                    acc[k] = fma(w, node[accs[k]], acc[k]);
+                }
+            }
+            __syncwarp();
+        }
+    }
+    double* H = sm;
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) {
+        const int q = lane + 32 * k;
+        if (q < W::NACC) H[__ldg(W::accpos() + q)] = acc[k];
+    }
+    __syncwarp();
+    const unsigned int* __restrict__ hop = W::hop();
+    const int* __restrict__ hlev = W::hlev();
+    const double dv0 = B.ABx, dv1 = B.ABy, dv2 = B.ABz, dv3 = K.ABx, dv4 = K.ABy, dv5 = K.ABz;
+    for (int lv = 0; lv < W::NHLEV; ++lv) {
+        const int e1 = __ldg(hlev + lv + 1);
+        for (int e = __ldg(hlev + lv) + lane; e < e1; e += 32) {
+            const unsigned int u = __ldg(hop + 2 * e), v = __ldg(hop + 2 * e + 1);
+            const int d = v >> 16;
+            const double dv = d == 0 ? dv0 : d == 1 ? dv1 : d == 2 ? dv2 : d == 3 ? dv3 : d == 4 ? dv4 : dv5;
+            H[u & 0xffff] = fma(dv, H[v & 0xffff], H[u >> 16]);
+        }
+        __syncwarp();
+    }
+    // contraction with the density weights
+    const int sh[4] = {B.sa, B.sb, K.sa, K.sb};
+    const int ls[4] = {LA, LB, LC, LD};
+    const int n[4] = {g_ncart(LA), g_ncart(LB), g_ncart(LC), g_ncart(LD)};
+    const int fo[4] = {a.func_off[B.sa], a.func_off[B.sb], a.func_off[K.sa], a.func_off[K.sb]};
+    double w = 8.0;
+    if (B.sa == B.sb) w *= 0.5;
+    if (K.sa == K.sb) w *= 0.5;
+    if (task.x == task.y) w *= 0.5;
+    const int nbf = a.nbf;
+    const double* Pm = a.P;
+    const unsigned short* __restrict__ out = W::out();
+    double g[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) g[k] = 0.0;
+    const int nblk = n[0] * n[1] * n[2] * n[3];
+    for (int e = lane; e < nblk; e += 32) {
+        int idx[4] = {e / (n[1] * n[2] * n[3]), (e / (n[2] * n[3])) % n[1], (e / n[3]) % n[2], e % n[3]};
+        const int pa = fo[0] + idx[0], pb = fo[1] + idx[1], pc = fo[2] + idx[2], pd = fo[3] + idx[3];
+        const double gam = w * (0.5 * Pm[pa * nbf + pb] * Pm[pc * nbf + pd] -
+                                0.125 * (Pm[pa * nbf + pc] * Pm[pb * nbf + pd] +
+                                         Pm[pa * nbf + pd] * Pm[pb * nbf + pc]));
+        for (int cen = 0; cen < 3; ++cen) {
+            int ex[3];
+            g_comp(ls[cen], idx[cen], ex[0], ex[1], ex[2]);
+            const double s = gam * a.comp_scale[6 * sh[cen] + idx[cen]];
+            for (int x = 0; x < 3; ++x) {
+                int up[3] = {ex[0], ex[1], ex[2]};
+                up[x] += 1;
+                int ii[4] = {idx[0], idx[1], idx[2], idx[3]};
+                int nn[4] = {n[0], n[1], n[2], n[3]};
+                ii[cen] = g_index(up[0], up[1], up[2]);
+                nn[cen] = g_ncart(ls[cen] + 1);
+                double v = H[out[__ldg(W::out_off() + cen) + ((ii[0] * nn[1] + ii[1]) * nn[2] + ii[2]) * nn[3] + ii[3]]];
+                if (ex[x] > 0) {
+                    int dn[3] = {ex[0], ex[1], ex[2]};
+                    dn[x] -= 1;
+                    ii[cen] = g_index(dn[0], dn[1], dn[2]);
+                    nn[cen] = g_ncart(ls[cen] - 1);
+                    v -= ex[x] * H[out[__ldg(W::out_off() + 3 + cen) + ((ii[0] * nn[1] + ii[1]) * nn[2] + ii[2]) * nn[3] + ii[3]]];
+                }
+                g[3 * cen + x] = fma(s, v, g[3 * cen + x]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) g[k] += __shfl_xor_sync(0xffffffffu, g[k], o);
+    if (lane == 0) {
+        for (int cen = 0; cen < 3; ++cen)
+            for (int x = 0; x < 3; ++x) {
+                atomicAdd(a.grad + 3 * a.shell_atom[sh[cen]] + x, g[3 * cen + x]);
+                atomicAdd(a.grad + 3 * a.shell_atom[sh[3]] + x, -g[3 * cen + x]);
+            }
+    }
+}
+
+template <int LA, int LB, int LC, int LD>
+int launch_grad(const GradArgs& a, cudaStream_t st) {
+    if (a.ntask <= 0) return 0;
+    using Lay = GradLayout<LA, LB, LC, LD>;
+    auto k = k_eri_grad<LA, LB, LC, LD>;
+    if (set_smem(k, Lay::BYTES)) return GS_ERR_CUDA;
+    k<<<(a.ntask + kGradWarps - 1) / kGradWarps, 32 * kGradWarps, Lay::BYTES, st>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+}
+
+}  // namespace gs

@@ -65,40 +65,51 @@ def combined_basis(sb: ShellBasis):
     return comb, raised, lowered
 
 
-def _derivative_rows(sb, comb, raised, lowered, M):
-    """For matrix M over (combined x original) functions, D[x][i, j] = d M_ij / d(centre of i)_x."""
+def _derivative_maps(sb, comb, raised, lowered):
+    """Row indices into the combined matrices: d M_ij / d(centre of i)_x =
+    scale_i (M[up[x, i], j] - fac[x, i] M[dn[x, i], j])."""
     n = sb.nbf
-    D = np.zeros((3, n, n))
+    up = np.zeros((3, n), dtype=np.int64)
+    dn = np.zeros((3, n), dtype=np.int64)
+    fac = np.zeros((3, n))
+    scale = np.zeros(n)
     for s in range(sb.nshell):
-        ls = int(sb.l[s])
-        for ci, lmn in enumerate(_COMP[ls]):
+        for ci, lmn in enumerate(_COMP[int(sb.l[s])]):
             i = sb.func_off[s] + ci
+            scale[i] = sb.comp_scale[s, ci]
             for x in range(3):
-                up = list(lmn)
-                up[x] += 1
-                r = comb.func_off[raised[s]] + _idx(up)
-                v = M[r, :n].copy()
+                u = list(lmn)
+                u[x] += 1
+                up[x, i] = comb.func_off[raised[s]] + _idx(u)
                 if lmn[x] > 0:
-                    dn = list(lmn)
-                    dn[x] -= 1
-                    v -= lmn[x] * M[comb.func_off[lowered[s]] + _idx(dn), :n]
-                D[x, i] = sb.comp_scale[s, ci] * v
-    return D
+                    d = list(lmn)
+                    d[x] -= 1
+                    dn[x, i] = comb.func_off[lowered[s]] + _idx(d)
+                    fac[x, i] = lmn[x]
+    return up, dn, fac, scale
+
+
+def _derivative_rows(sb, comb, raised, lowered, M, maps=None):
+    """For matrix M over (combined x original) functions, D[x][i, j] = d M_ij / d(centre of i)_x."""
+    up, dn, fac, scale = maps if maps is not None else _derivative_maps(sb, comb, raised, lowered)
+    n = sb.nbf
+    return scale[None, :, None] * (M[up, :n] - fac[:, :, None] * M[dn, :n])
 
 
 def one_electron_gradient(sb, mol, shell_atom, P, W):
     comb, raised, lowered = combined_basis(sb)
     func_atom = np.repeat(shell_atom, sb.nfunc)
     g = np.zeros((len(mol.symbols), 3))
+    maps = _derivative_maps(sb, comb, raised, lowered)
     S, T, _ = one_electron(comb, mol.coords[:1], np.zeros(1))
-    dS = _derivative_rows(sb, comb, raised, lowered, S)
-    dT = _derivative_rows(sb, comb, raised, lowered, T)
+    dS = _derivative_rows(sb, comb, raised, lowered, S, maps)
+    dT = _derivative_rows(sb, comb, raised, lowered, T, maps)
     for x in range(3):
         contrib = 2.0 * np.sum(P * dT[x] - W * dS[x], axis=1)
         np.add.at(g[:, x], func_atom, contrib)
     for c in range(len(mol.symbols)):
         _, _, Vc = one_electron(comb, mol.coords[c:c + 1], mol.charges[c:c + 1])
-        dV = _derivative_rows(sb, comb, raised, lowered, Vc)
+        dV = _derivative_rows(sb, comb, raised, lowered, Vc, maps)
         for x in range(3):
             h = 2.0 * np.sum(P * dV[x], axis=1)
             np.add.at(g[:, x], func_atom, h)
@@ -118,6 +129,27 @@ def nuclear_repulsion_gradient(mol):
 
 
 def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom):
+    """Two-electron gradient through the fused adjoint kernel (gs_eri_grad), one launch per
+    class over the engine's Schwarz-screened unique quartets."""
+    if np.any(sb.l >= 2):
+        raise NotImplementedError("the fused gradient kernels cover s/p shells")
+    dev = engine.dev
+    grad = torch.zeros(natom * 3, dtype=torch.float64, device=dev)
+    pt = torch.as_tensor(np.ascontiguousarray(P)).to(dev)
+    sa = torch.as_tensor(np.ascontiguousarray(shell_atom, dtype=np.int32)).to(dev)
+    L = _lib.lib()
+    base = engine.tasks.data_ptr()
+    for cls, s, e in engine.segments:
+        _lib.check(L.gs_eri_grad(*cls, _lib.ptr(engine.pairs.rec), _lib.ptr(engine.pairs.p64),
+                                 _lib.ptr(engine.ds.comp_scale), _lib.ptr(engine.ds.func_off),
+                                 _lib.ptr(sa), e - s, base + s * 8, sb.nbf, _lib.ptr(pt),
+                                 _lib.ptr(grad), _lib.stream()), f"gs_eri_grad{cls}")
+    return grad.view(natom, 3).cpu().numpy()
+
+
+def eri_gradient_blocks(sb, engine: JKEngine, shell_atom, P, natom):
+    """The same two-electron gradient from explicit raised/lowered blocks (gs_eri_blocks)
+    contracted by gs_eri_grad_contract; slower, kept as an independent cross-check."""
     comb, raised, lowered = combined_basis(sb)
     tasks = engine.tasks[:engine.ntasks].cpu().numpy()
     ps = engine.pairs.host_shells

@@ -43,3 +43,18 @@ def test_autograd_function(gpu_lib):
     e.backward()
     _, g, _ = rhf_energy_gradient(m, "6-31G")
     assert np.allclose(c.grad.numpy(), g, atol=1e-12)
+
+
+def test_fused_adjoint_matches_block_path(gpu_lib):
+    from gaussium_gb300 import gradient, molecules
+    from gaussium_gb300.engine import JKEngine
+    mol = molecules.water_cluster(2, seed=9)
+    sb = molecules.shell_basis(mol, "6-31G")
+    eng = JKEngine(sb, schwarz_thr=1e-14)
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal((sb.nbf, sb.nbf))
+    P = (a + a.T) / 8
+    sa = gradient.shell_atoms(mol, sb)
+    g1 = gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
+    g2 = gradient.eri_gradient_blocks(sb, eng, sa, P, len(mol.symbols))
+    assert np.max(np.abs(g1 - g2)) < 1e-10
