@@ -466,13 +466,17 @@ def run_gradient(args, rank, world):
     eps, C = scf.LinearAlgebra(S).diagonalize(res.fock)
     W = 2.0 * (C[:, :nocc] * eps[:nocc]) @ C[:, :nocc].T
     sa = gradient.shell_atoms(mol, sb)
+    gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ge = gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
     torch.cuda.synchronize()
     t_eri_grad = time.perf_counter() - t0
+    gradient.one_electron_gradient_kernel(sb, mol, sa, P, W)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    g1 = gradient.one_electron_gradient(sb, mol, sa, P, W)
+    g1 = gradient.one_electron_gradient_kernel(sb, mol, sa, P, W)
+    torch.cuda.synchronize()
     t_one_grad = time.perf_counter() - t0
     # finite differences
     rng = np.random.default_rng(0)

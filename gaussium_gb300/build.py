@@ -24,7 +24,7 @@ LMAX = 2
 # Classes with total angular momentum L >= WIDE64_MIN (FP64) or >= WIDE32_MIN (FP32) use the
 # warp-cooperative kernel (csrc/eri_wide.cuh); the others one thread per quartet
 # (csrc/eri_kernels.cuh); csrc/eri_launch.cuh dispatches.
-WIDE64_MIN = int(os.environ.get("GS_WIDE64_MIN", "3"))
+WIDE64_MIN = int(os.environ.get("GS_WIDE64_MIN", "2"))
 WIDE32_MIN = int(os.environ.get("GS_WIDE32_MIN", "8"))
 WIDE_PROG_MIN = 2          # classes that get generated warp programs
 

@@ -25,7 +25,7 @@ launch_fn find_class(int la, int lb, int lc, int ld) {
 
 inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
 
-int check_launch() { return cudaPeekAtLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA; }
+int check_launch() { return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA; }
 
 __global__ void k_pairs_build(gs::ShellView sv, int npairs, const int* __restrict__ pair_shells,
                               const int* __restrict__ pair_prim_off, gs::PairRec* pairs,

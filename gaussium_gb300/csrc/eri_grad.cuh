@@ -242,9 +242,9 @@ int launch_grad(const GradArgs& a, cudaStream_t st) {
     if (a.ntask <= 0) return 0;
     using Lay = GradLayout<LA, LB, LC, LD>;
     auto k = k_eri_grad<LA, LB, LC, LD>;
-    if (set_smem(k, Lay::BYTES)) return GS_ERR_CUDA;
+    if (set_smem<k_eri_grad<LA, LB, LC, LD>>(Lay::BYTES)) return GS_ERR_CUDA;
     k<<<(a.ntask + kGradWarps - 1) / kGradWarps, 32 * kGradWarps, Lay::BYTES, st>>>(a);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 
 }  // namespace gs

@@ -215,7 +215,7 @@ int launch_class(int kind, const void* args, cudaStream_t st) {
     } else {
         return GS_ERR_ARG;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 
 }  // namespace gs

@@ -335,11 +335,12 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
 
 // Raise a kernel's dynamic shared-memory limit once (the first launch happens before any
 // stream capture, so later launches inside a captured graph make no attribute call).
-template <typename K>
-int set_smem(K k, size_t sh) {
-    static bool done = false;
+template <auto Kernel>
+int set_smem(size_t sh) {
+    static bool done = false;     // one flag per kernel instantiation
     if (done) return 0;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh)) return GS_ERR_CUDA;
+    if (cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh))
+        return GS_ERR_CUDA;
     done = true;
     return 0;
 }
@@ -353,20 +354,20 @@ int launch_wide(int kind, const void* args, cudaStream_t st) {
         const WriteArgs& a = *(const WriteArgs*)args;
         if (a.ntask <= 0) return 0;
         auto k = k_wide_write<LA, LB, LC, LD, T>;
-        if (set_smem(k, Lay::BYTES_W)) return GS_ERR_CUDA;
+        if (set_smem<k_wide_write<LA, LB, LC, LD, T>>(Lay::BYTES_W)) return GS_ERR_CUDA;
         k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_W, st>>>(a);
     } else if (kind == GS_KIND_JK) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
         auto k = k_wide_jk<LA, LB, LC, LD, T>;
-        if (set_smem(k, Lay::BYTES_JK)) return GS_ERR_CUDA;
+        if (set_smem<k_wide_jk<LA, LB, LC, LD, T>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
         k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_JK, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
         if constexpr (LA == LC && LB == LD && PREC == 64) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;
             if (a.npair <= 0) return 0;
             auto k = k_wide_schwarz<LA, LB, double>;
-            if (set_smem(k, Lay::BYTES_W)) return GS_ERR_CUDA;
+            if (set_smem<k_wide_schwarz<LA, LB, double>>(Lay::BYTES_W)) return GS_ERR_CUDA;
             k<<<(a.npair + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_W, st>>>(a);
         } else {
             return GS_ERR_CLASS;
@@ -374,7 +375,7 @@ int launch_wide(int kind, const void* args, cudaStream_t st) {
     } else {
         return GS_ERR_ARG;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 
 }  // namespace gs

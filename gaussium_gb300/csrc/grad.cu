@@ -130,5 +130,5 @@ extern "C" int gs_eri_grad_contract(int nq, const int* quartets, const long long
     if (nq == 0) return GS_OK;
     k_grad_contract<<<(nq + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
         nq, quartets, block_off, blocks, l, func_off, comp_scale, shell_atom, nbf, density, grad);
-    return cudaPeekAtLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA;
 }

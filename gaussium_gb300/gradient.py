@@ -117,6 +117,26 @@ def one_electron_gradient(sb, mol, shell_atom, P, W):
     return g
 
 
+def one_electron_gradient_kernel(sb, mol, shell_atom, P, W, device="cuda"):
+    """The one-electron gradient terms in one launch (gs_one_electron_grad)."""
+    ds = DeviceShells(sb, device)
+    dev = ds.device
+    i, j = np.tril_indices(sb.nshell)
+    t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt)).to(dev)
+    pairs = t(np.stack([i, j], 1), np.int32)
+    grad = torch.zeros(len(mol.symbols) * 3, dtype=torch.float64, device=dev)
+    L = _lib.lib()
+    _lib.check(L.gs_one_electron_grad(_lib.ptr(ds.centre), _lib.ptr(ds.l), _lib.ptr(ds.prim_off),
+                                      _lib.ptr(ds.expo), _lib.ptr(ds.coef), _lib.ptr(ds.comp_scale),
+                                      _lib.ptr(ds.func_off), _lib.ptr(t(shell_atom, np.int32)),
+                                      len(i), _lib.ptr(pairs), sb.nbf, len(mol.symbols),
+                                      _lib.ptr(t(mol.coords, np.float64)),
+                                      _lib.ptr(t(mol.charges, np.float64)), _lib.ptr(t(P, np.float64)),
+                                      _lib.ptr(t(W, np.float64)), _lib.ptr(grad), _lib.stream()),
+               "gs_one_electron_grad")
+    return grad.view(-1, 3).cpu().numpy()
+
+
 def nuclear_repulsion_gradient(mol):
     R, Z = mol.coords, mol.charges
     g = np.zeros_like(R)
@@ -218,7 +238,7 @@ def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
     P = 2.0 * C[:, :nocc] @ C[:, :nocc].T
     W = 2.0 * (C[:, :nocc] * eps[:nocc]) @ C[:, :nocc].T
     sa = shell_atoms(mol, sb)
-    g = one_electron_gradient(sb, mol, sa, P, W)
+    g = one_electron_gradient_kernel(sb, mol, sa, P, W)
     g += eri_gradient(sb, eng, sa, P, len(mol.symbols))
     g += nuclear_repulsion_gradient(mol)
     energy = res.energy + mol.nuclear_repulsion()

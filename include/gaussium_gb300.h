@@ -179,6 +179,20 @@ int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec, const void
                 const double* comp_scale, const int* func_off, const int* shell_atom, int ntask,
                 const int* tasks, int nbf, const double* density, double* grad, void* stream);
 
+/* One-electron part of the RHF gradient: for npairs unique shell pairs (a >= b) adds
+ *   f sum_ij [P_ij (dT_ij + dV_ij) - W_ij dS_ij]   (f = 2 for a != b, 1 for a == b)
+ * to grad[natom*3] through shell_atom[], including the nuclear-attraction operator term
+ * of every nucleus.  density P and energy_weighted W are nbf x nbf.  No reference
+ * counterpart (the reference has no gradients); it differentiates the integrals of
+ * integrals/orbital_overlap_integral.py, matrixelements/kinetic_energy_matrix.py and
+ * integrals/nuclear_attraction_integral.py. */
+int gs_one_electron_grad(const double* centre, const int* l, const int* prim_off,
+                         const double* expo, const double* coef, const double* comp_scale,
+                         const int* func_off, const int* shell_atom, int npairs,
+                         const int* pair_shells, int nbf, int natom, const double* atom_xyz,
+                         const double* atom_z, const double* density,
+                         const double* energy_weighted, double* grad, void* stream);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);

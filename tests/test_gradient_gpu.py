@@ -58,3 +58,16 @@ def test_fused_adjoint_matches_block_path(gpu_lib):
     g1 = gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
     g2 = gradient.eri_gradient_blocks(sb, eng, sa, P, len(mol.symbols))
     assert np.max(np.abs(g1 - g2)) < 1e-10
+
+
+def test_one_electron_gradient_kernel_matches_host_assembly(gpu_lib):
+    from gaussium_gb300 import gradient, molecules
+    mol = molecules.water_cluster(2, seed=12)
+    sb = molecules.shell_basis(mol, "6-31G")
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((sb.nbf, sb.nbf)); P = (a + a.T) / 8
+    b = rng.standard_normal((sb.nbf, sb.nbf)); W = (b + b.T) / 8
+    sa = gradient.shell_atoms(mol, sb)
+    g1 = gradient.one_electron_gradient_kernel(sb, mol, sa, P, W)
+    g2 = gradient.one_electron_gradient(sb, mol, sa, P, W)
+    assert np.max(np.abs(g1 - g2)) < 1e-9

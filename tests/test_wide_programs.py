@@ -68,7 +68,7 @@ def emulate(cls, pr, pd, bra, ket):
     return H[np.array(p["outslot"])]
 
 
-@pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(2) if sum(c) >= 3])
+@pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(2) if sum(c) >= 2])
 def test_wide_program_matches_generated_code(cls):
     shells = synthetic_shells()
     sb = ShellBasis.from_shell_dicts(shells)
