@@ -28,6 +28,9 @@ _SIGS = {
     "gs_fock_jk_mixed_workspace": (ctypes.c_longlong, [I]),
     "gs_fock_jk_mixed": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, P,
                              ctypes.c_longlong, P]),
+    "gs_fock_jk_mixed_noalloc": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D,
+                                     D, P]),
+    "gs_fock_jk_mixed_noalloc_max_tasks": (I, []),
     "gs_boys_eval": (I, [I, I, I, P, P, P]),
     "gs_fma_probe": (I, [I, I, I, I, P, P]),
     "gs_one_electron": (I, [P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),

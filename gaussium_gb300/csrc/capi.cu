@@ -125,6 +125,9 @@ const char* gs_status_string(int status) {
         case GS_ERR_CLASS: return "angular-momentum class not built into this library";
         case GS_ERR_DEVICE: return "device-side status error";
         case GS_ERR_NOMEM: return "workspace too small";
+        case GS_ERR_LIMIT:
+            return "task count exceeds the fixed workspace of the no-allocation entry point "
+                   "(gs_fock_jk_mixed_noalloc_max_tasks)";
         default: return "unknown status";
     }
 }
@@ -331,6 +334,48 @@ int gs_fock_jk_mixed(int la, int lb, int lc, int ld, const void* pair_rec, const
     return fock_jk_mixed_impl(la, lb, lc, ld, pair_rec, prim64, prim32, comp_scale, func_off,
                               nshell, nbf, ntask, tasks, pj, j, nk, pk, k, shell_dmax, screen_thr,
                               mixed_cut, workspace, ws_bytes, stream);
+}
+
+// ---------------------------------------------------------------------- no-allocation form
+// Workspace of gs_fock_jk_mixed_noalloc: a fixed array in device memory that every GPU
+// loading this library holds until the process exits.  Host code only ever sees the
+// array's host-side stand-in symbol, so the device address is looked up per device with
+// cudaGetSymbolAddress before use.
+#define GS_NOALLOC_MAX_TASKS (1 << 20)
+static __device__ __align__(256) unsigned char g_noalloc_ws[256 + 2 * (size_t)GS_NOALLOC_MAX_TASKS * 8];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+int noalloc_workspace(void** ptr) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GS_ERR_CUDA;
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_ws) != cudaSuccess || !p) return GS_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *ptr = g_noalloc_ptr[dev];
+    return GS_OK;
+}
+}  // namespace
+
+int gs_fock_jk_mixed_noalloc_max_tasks(void) { return GS_NOALLOC_MAX_TASKS; }
+
+int gs_fock_jk_mixed_noalloc(int la, int lb, int lc, int ld, const void* pair_rec,
+                             const void* prim64, const void* prim32, const double* comp_scale,
+                             const int* func_off, int nshell, int nbf, int ntask, const int* tasks,
+                             const double* pj, double* j, int nk, const double* pk, double* k,
+                             const double* shell_dmax, double screen_thr, double mixed_cut,
+                             void* stream) {
+    if (ntask > GS_NOALLOC_MAX_TASKS) return GS_ERR_LIMIT;
+    void* ws = nullptr;
+    const int rc = noalloc_workspace(&ws);
+    if (rc) return rc;
+    return fock_jk_mixed_impl(la, lb, lc, ld, pair_rec, prim64, prim32, comp_scale, func_off,
+                              nshell, nbf, ntask, tasks, pj, j, nk, pk, k, shell_dmax, screen_thr,
+                              mixed_cut, ws, (long long)sizeof(g_noalloc_ws), stream);
 }
 
 int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream) {

@@ -12,6 +12,7 @@
 #define GS_ERR_CLASS 3
 #define GS_ERR_DEVICE 4
 #define GS_ERR_NOMEM 5
+#define GS_ERR_LIMIT 6
 
 namespace gs {
 struct PairRec;

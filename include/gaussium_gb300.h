@@ -36,6 +36,7 @@ extern "C" {
 #define GS_ERR_CLASS 3
 #define GS_ERR_DEVICE 4
 #define GS_ERR_NOMEM 5
+#define GS_ERR_LIMIT 6
 
 /* Library version (1). */
 int gs_version(void);
@@ -120,6 +121,27 @@ int gs_fock_jk_mixed(int la, int lb, int lc, int ld, const void* pair_rec, const
                      int nk, const double* pk, double* k, const double* shell_dmax,
                      double screen_thr, double mixed_cut, void* workspace, long long ws_bytes,
                      void* stream);
+
+/* gs_fock_jk_mixed without a workspace argument, for callers that cannot allocate device
+ * memory: a host whose memory manager owns every device allocation and forbids further
+ * ones, or a C/C++ caller with no device allocator of its own.  It makes no cudaMalloc,
+ * cudaFree or other allocating call.  Its scratch (the two partitioned task lists and
+ * their counts) lives in one fixed array of 16 MiB + 256 B in device memory, held by
+ * every GPU that loads the library until the process exits; ntask above
+ * gs_fock_jk_mixed_noalloc_max_tasks() (2^20) returns GS_ERR_LIMIT.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make that first call before any stream capture.  All calls share the one
+ * array: the counts are cleared at the start of every call, and calls that overlap on
+ * the GPU (different streams, no ordering) race.  No counterpart in the reference. */
+int gs_fock_jk_mixed_noalloc(int la, int lb, int lc, int ld, const void* pair_rec,
+                             const void* prim64, const void* prim32, const double* comp_scale,
+                             const int* func_off, int nshell, int nbf, int ntask, const int* tasks,
+                             const double* pj, double* j, int nk, const double* pk, double* k,
+                             const double* shell_dmax, double screen_thr, double mixed_cut,
+                             void* stream);
+
+/* Largest ntask gs_fock_jk_mixed_noalloc accepts (2^20). */
+int gs_fock_jk_mixed_noalloc_max_tasks(void);
 
 /* Batched form of gs_fock_jk for many molecules in one launch (the reference builds one
  * molecule at a time; same replaced functions as gs_fock_jk).  shell_mol[s] is the
