@@ -31,6 +31,8 @@ _SIGS = {
     "gs_fock_jk_mixed_noalloc": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D,
                                      D, P]),
     "gs_fock_jk_mixed_noalloc_max_tasks": (I, []),
+    "gs_class_variants": (I, [I, I, I, I, I]),
+    "gs_set_class_variant": (I, [I, I, I, I, I, I]),
     "gs_boys_eval": (I, [I, I, I, P, P, P]),
     "gs_fma_probe": (I, [I, I, I, I, P, P]),
     "gs_one_electron": (I, [P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),

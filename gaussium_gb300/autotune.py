@@ -1,0 +1,107 @@
+"""Per-class kernel-form autotuner.
+
+A class (la lb|lc ld) whose total angular momentum lies in the overlap of the two kernel
+families is built both as the one-thread-per-quartet kernel and as the warp-per-quartet
+kernel (``gs_class_variants``).  Which is faster depends on the workload, chiefly on the
+primitive counts of the quartets: a warp spends its lanes on primitive quartets, so it
+wins on highly contracted quartets and loses on quartets of one or two primitives.  The
+tuner times both forms of every such class on the caller's own task lists (CUDA events on
+the launching stream, after a warm-up launch, median of ``reps``) and selects the faster
+with ``gs_set_class_variant``.  The choice is process-wide and stays until changed.
+"""
+import json
+
+import torch
+
+from . import _lib
+
+THREAD, WARP = 1, 2
+
+
+def forms(cls, precision):
+    """Kernel forms built for a class: a subset of {THREAD, WARP}."""
+    m = _lib.lib().gs_class_variants(*cls, precision)
+    if m < 0:
+        _lib.check(-m, f"gs_class_variants{cls}")
+    return [v for v in (THREAD, WARP) if m & (1 << (v - 1))]
+
+
+def set_form(cls, precision, variant):
+    _lib.check(_lib.lib().gs_set_class_variant(*cls, precision, variant),
+               f"gs_set_class_variant{cls}")
+
+
+def _time(fn, reps):
+    st = torch.cuda.current_stream()
+    fn()                                         # warm-up
+    out = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        fn()
+        b.record(st)
+        b.synchronize()
+        out.append(a.elapsed_time(b))
+    out.sort()
+    return out[len(out) // 2]
+
+
+def tune(segments, run_class, precisions=(64, 32), reps=3, min_tasks=1):
+    """Choose the faster form for every class of ``segments`` ([(cls, start, end)]) that
+    has two; ``run_class(cls, precision)`` launches that class's work once on the current
+    stream.  Returns {(cls, precision): {"form": v, "ms": {v: t}}}."""
+    chosen = {}
+    for prec in precisions:
+        for cls, s, e in segments:
+            if e - s < min_tasks:
+                continue
+            fs = forms(cls, prec)
+            if len(fs) < 2:
+                continue
+            times = {}
+            for v in fs:
+                set_form(cls, prec, v)
+                times[v] = _time(lambda: run_class(cls, prec), reps)
+            best = min(times, key=times.get)
+            set_form(cls, prec, best)
+            chosen[(cls, prec)] = {"form": best, "ms": times}
+    return chosen
+
+
+def tune_jk(engine, density, precisions=(64, 32), reps=3):
+    """Tune the J/K class launches of a JKEngine on its task list with one density."""
+    P = density if torch.is_tensor(density) else torch.as_tensor(density).to(engine.dev)
+    return tune(engine.segments, lambda cls, prec: engine.jk(P, [P], precision=prec, classes=[cls]),
+                precisions, reps)
+
+
+def tune_blocks(batch, out, precisions=(64, 32), reps=3):
+    """Tune the integral-block class launches of a QuartetBatch writing into ``out``."""
+    return tune(batch.segments, lambda cls, prec: batch.run(out, prec, classes=[cls]),
+                precisions, reps)
+
+
+def reset(segments, precisions=(64, 32)):
+    """Back to the built-in default form for every class of ``segments``."""
+    for prec in precisions:
+        for cls, _, _ in segments:
+            set_form(cls, prec, 0)
+
+
+def save(chosen, path):
+    rows = [{"class": list(cls), "precision": prec, "form": r["form"],
+             "ms": {str(k): v for k, v in r["ms"].items()}} for (cls, prec), r in chosen.items()]
+    with open(path, "w") as f:
+        json.dump(rows, f, indent=1)
+
+
+def load(path):
+    """Apply a saved choice; returns it in the form ``tune`` returns."""
+    with open(path) as f:
+        rows = json.load(f)
+    chosen = {}
+    for r in rows:
+        cls, prec = tuple(r["class"]), r["precision"]
+        set_form(cls, prec, r["form"])
+        chosen[(cls, prec)] = {"form": r["form"], "ms": {int(k): v for k, v in r["ms"].items()}}
+    return chosen

@@ -70,7 +70,7 @@ class BatchedRHF:
                 _lib.check(L.gs_schwarz(la, lb, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
                                         _lib.ptr(self.ds.comp_scale), len(idx), _lib.ptr(it),
                                         _lib.ptr(q), len(pairs), _lib.stream()), "gs_schwarz")
-        self._tasks(q.cpu().numpy(), pc, pair_mol, schwarz_thr)
+        self._tasks(q, pc, pair_mol, schwarz_thr)
         # one-electron matrices, orthogonalisers, padded index maps
         self.S, self.H = [], []
         for m, (mol, sb) in enumerate(zip(molecules, sbs)):
@@ -78,41 +78,15 @@ class BatchedRHF:
             self.S.append(S)
             self.H.append(T + V)
         self._padded_setup()
-        self.graph = None
+        self._graphs = {}           # (mixed_cut, screen_thr) -> (P_static, graph, G_static)
 
     def _tasks(self, q, pc, pair_mol, thr):
-        nprim = self.pairs.nprim
-        out = {}
-        for m in range(len(self.sbs)):
-            pm = np.flatnonzero(pair_mol == m)
-            for cb in range(len(PAIR_ORDER)):
-                bra = pm[pc[pm] == cb]
-                if len(bra) == 0:
-                    continue
-                for ck in range(cb + 1):
-                    ket = pm[pc[pm] == ck]
-                    if len(ket) == 0:
-                        continue
-                    bi, ki = np.meshgrid(bra, ket, indexing="ij")
-                    bi, ki = bi.ravel(), ki.ravel()
-                    keep = q[bi] * q[ki] >= thr
-                    if cb == ck:
-                        keep &= bi >= ki
-                    out.setdefault((cb, ck), []).append(np.stack([bi[keep], ki[keep]], 1))
-        segs, chunks, n = [], [], 0
-        for (cb, ck), lst in sorted(out.items()):
-            tk = np.concatenate(lst)
-            if len(tk) == 0:
-                continue
-            order = np.lexsort((nprim[tk[:, 1]], nprim[tk[:, 0]]))
-            tk = tk[order]
-            (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
-            segs.append(((la, lb, lc, ld), n, n + len(tk)))
-            chunks.append(tk)
-            n += len(tk)
-        self.segments = segs
-        self.ntasks = n
-        self.tasks = torch.as_tensor(np.concatenate(chunks).astype(np.int32)).to(self.dev)
+        nprim = torch.as_tensor(np.asarray(self.pairs.nprim, dtype=np.int64)).to(self.dev)
+        pc_d = torch.as_tensor(np.asarray(pc, dtype=np.int64)).to(self.dev)
+        pm_d = torch.as_tensor(np.asarray(pair_mol, dtype=np.int64)).to(self.dev)
+        self.segments, self.tasks = batched_task_list(q, pc_d, pm_d, nprim, thr, len(PAIR_ORDER),
+                                                      len(self.sbs))
+        self.ntasks = int(self.tasks.shape[0])
 
     def _padded_setup(self):
         B, N = len(self.sbs), self.nmax
@@ -125,25 +99,8 @@ class BatchedRHF:
         pos = np.flatnonzero(flat >= 0)
         self.pos_padded = torch.as_tensor(pos).to(dev)          # into [B*N*N]
         self.pos_packed = torch.as_tensor(flat[pos]).to(dev)    # into packed storage
-        S = torch.zeros((B, N, N), dtype=torch.float64, device=dev)
-        H = torch.zeros_like(S)
-        for m, n in enumerate(self.nbf):
-            S[m, :n, :n] = torch.as_tensor(self.S[m]).to(dev)
-            H[m, :n, :n] = torch.as_tensor(self.H[m]).to(dev)
-            S[m, n:, n:] = torch.eye(N - n, dtype=torch.float64, device=dev)
-        self.Sb, self.Hb = S, H
-        # canonical orthogonaliser per molecule (eigenvalues ascending, as the reference
-        # sorts them); padded orbitals are zero columns at positions n..N-1
-        X = torch.zeros_like(S)
-        for m, n in enumerate(self.nbf):
-            s, u = torch.linalg.eigh(S[m, :n, :n])
-            X[m, :n, :n] = u * s.rsqrt().unsqueeze(0)
-        self.X = X
-        self.nocc = torch.as_tensor([mol.electrons // 2 for mol in self.mols], device=dev)
-        self.occ_mask = (torch.arange(N, device=dev)[None, :] < self.nocc[:, None]).double()
-        self.pad_orb = torch.zeros((B, N), dtype=torch.float64, device=dev)
-        for m, n in enumerate(self.nbf):
-            self.pad_orb[m, n:] = 1.0
+        self.Sb, self.Hb, self.X, self.occ_mask, self.pad_orb = padded_system(
+            self.S, self.H, [mol.electrons // 2 for mol in self.mols], dev)
 
     def to_packed(self, Pb):
         out = torch.zeros(self.mat_stride, dtype=torch.float64, device=self.dev)
@@ -155,16 +112,20 @@ class BatchedRHF:
         Pb.index_copy_(0, self.pos_padded, v.index_select(0, self.pos_packed))
         return Pb.view(len(self.sbs), self.nmax, self.nmax)
 
-    def _jk_launch(self, P, J, K, precision=64, mixed_cut=None, dmax=None):
+    def _jk_launch(self, P, J, K, precision=64, mixed_cut=None, dmax=None, screen_thr=0.0,
+                   classes=None):
         L = _lib.lib()
         st = _lib.stream()
         base = self.tasks.data_ptr()
-        runs = [(precision, 0.0, float("inf"), 0.0)]
+        thr = screen_thr if screen_thr > 0 else (1e-300 if mixed_cut is not None else 0.0)
+        runs = [(precision, 0.0, float("inf"))]
         if mixed_cut is not None:
-            runs = [(64, mixed_cut, float("inf"), 1e-300), (32, 0.0, mixed_cut, 1e-300)]
-        for prec, lo, hi, thr in runs:
+            runs = [(64, mixed_cut, float("inf")), (32, 0.0, mixed_cut)]
+        for prec, lo, hi in runs:
             prims = self.pairs.prims(prec)
             for cls, s, e in self.segments:
+                if classes is not None and cls not in classes:
+                    continue
                 rc = L.gs_fock_jk_batched(*cls, prec, _lib.ptr(self.pairs.rec), _lib.ptr(prims),
                                           _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
                                           _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base),
@@ -173,81 +134,219 @@ class BatchedRHF:
                                           _lib.ptr(P), _lib.ptr(K), thr, lo, hi, st)
                 _lib.check(rc, f"gs_fock_jk_batched{cls}")
 
-    def fock_packed(self, P, precision=64, mixed_cut=None):
-        """G = J - K/2 (packed, symmetric) for packed densities P, all molecules."""
+    def tune(self, precisions=(64, 32), reps=3):
+        """Choose the kernel form of every class with two on this batch's task lists."""
+        from . import autotune
+        P = torch.zeros(self.mat_stride, dtype=torch.float64, device=self.dev)
+        J, K = torch.zeros_like(P), torch.zeros_like(P)
+        return autotune.tune(self.segments,
+                             lambda cls, prec: self._jk_launch(P, J, K, prec, classes=[cls]),
+                             precisions, reps)
+
+    def density(self, m):
+        """Converged density of molecule m (host nbf_m x nbf_m) after ``run``."""
+        n = int(self.nbf[m])
+        return self.densities[m, :n, :n].cpu().numpy()
+
+    def fock_packed(self, P, precision=64, mixed_cut=None, screen_thr=0.0):
+        """G = J - K/2 (padded [B, N, N], symmetric) for packed densities P, all molecules.
+        With ``screen_thr`` a quartet is skipped when its Schwarz bound times the largest
+        |P| element of its molecule is below it; with ``mixed_cut`` the quartets whose such
+        bound is below the cut run in FP32 (FP64 accumulation)."""
         J = torch.zeros_like(P)
         K = torch.zeros_like(P)
         dmax = None
-        if mixed_cut is not None:
-            Pb = self.to_padded(P).abs().amax(dim=(1, 2))
-            dmax = Pb.contiguous()
-        self._jk_launch(P, J, K, precision, mixed_cut, dmax)
+        if mixed_cut is not None or screen_thr > 0:
+            dmax = self.to_padded(P).abs().amax(dim=(1, 2)).contiguous()
+        self._jk_launch(P, J, K, precision, mixed_cut, dmax, screen_thr)
         Jb, Kb = self.to_padded(J), self.to_padded(K)
         G = (Jb + Jb.transpose(1, 2)) - 0.5 * (Kb + Kb.transpose(1, 2))
         return G
 
-    def run(self, threshold=1e-10, max_iter=60, mixed_cut=None, use_graph=True):
-        """Batched SCF; returns total energies (numpy) and the iteration count."""
-        dev = self.dev
-        B, N = len(self.sbs), self.nmax
-        P_static = torch.zeros(self.mat_stride, dtype=torch.float64, device=dev)
-        G_static = None
+    def run(self, threshold=1e-10, max_iter=60, mixed_cut=None, screen_thr=0.0,
+            incremental=False, reset_every=8, final_fp64=None, use_graph=True):
+        """Batched SCF; returns total energies (numpy) and the iteration count.
+
+        With ``incremental`` the Fock build of iteration i evaluates G(P_i - P_ref) and adds
+        it to G(P_ref) (a full build every ``reset_every`` iterations); with screening this
+        skips most quartets once the densities settle, and a converged molecule (dP = 0)
+        costs nothing.  ``final_fp64`` (default: on whenever a build is approximate)
+        evaluates the reported energies from one full, unscreened FP64 build at the final
+        densities."""
+        key = (mixed_cut, screen_thr)
+        if key in self._graphs:
+            P_static, g, G_static = self._graphs[key]
+        else:
+            P_static = torch.zeros(self.mat_stride, dtype=torch.float64, device=self.dev)
+            g = G_static = None
 
         def build():
-            return self.fock_packed(P_static, mixed_cut=mixed_cut)
+            return self.fock_packed(P_static, mixed_cut=mixed_cut, screen_thr=screen_thr)
 
-        if use_graph:
+        if use_graph and g is None:
             build()                                  # warm-up outside capture
             torch.cuda.synchronize()
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
                 G_static = build()
-            self.graph = g
-        Xb, Hb, Sb = self.X, self.Hb, self.Sb
-        big = 1e6 * self.pad_orb
+            self._graphs[key] = (P_static, g, G_static)
+        state = {"n": 0, "P": None, "G": None}
 
-        def diag(F):
-            Fo = Xb.transpose(1, 2) @ F @ Xb + torch.diag_embed(big)
-            e, c = torch.linalg.eigh(Fo)
-            return e, Xb @ c
-
-        e_orb, C = diag(Hb)
-        prev = torch.zeros(B, dtype=torch.float64, device=dev)
-        hist_f, hist_e = [], []
-        energies = None
-        for it in range(1, max_iter + 1):
-            Cocc = C * self.occ_mask[:, None, :]
-            Pb = 2.0 * Cocc @ Cocc.transpose(1, 2)
-            P_static.copy_(self.to_packed(Pb))
+        def two_electron(Pb):
+            inc = incremental and state["P"] is not None and state["n"] % reset_every != 0
+            P_static.copy_(self.to_packed(Pb - state["P"] if inc else Pb))
             if use_graph:
-                self.graph.replay()
-                G = G_static
+                g.replay()
+                G = G_static.clone()
             else:
                 G = build()
-            F = Hb + G
-            energies = 0.5 * torch.sum(Pb * (Hb + F), dim=(1, 2))
-            de = (energies - prev).abs()
-            prev = energies
-            if it > 1 and bool((de < threshold).all()):
-                break
-            err = Sb @ Pb @ F - F @ Pb @ Sb
-            err = Xb.transpose(1, 2) @ err @ Xb
-            hist_f.append(F)
-            hist_e.append(err)
-            if len(hist_f) > 8:
-                hist_f.pop(0)
-                hist_e.pop(0)
-            if len(hist_f) > 1:
-                k = len(hist_f)
-                Bm = torch.zeros((B, k + 1, k + 1), dtype=torch.float64, device=dev)
-                E = torch.stack(hist_e, 1)                       # [B, k, N, N]
-                Bm[:, :k, :k] = torch.einsum("bkij,blij->bkl", E, E)
-                Bm[:, :k, k] = 1
-                Bm[:, k, :k] = 1
-                rhs = torch.zeros((B, k + 1), dtype=torch.float64, device=dev)
-                rhs[:, k] = 1
-                c = torch.linalg.solve(Bm, rhs)[:, :k]
-                F = torch.einsum("bk,bkij->bij", c, torch.stack(hist_f, 1))
-            e_orb, C = diag(F)
-        e_nuc = torch.as_tensor([m.nuclear_repulsion() for m in self.mols], device=dev)
+            if inc:
+                G = G + state["G"]
+            state.update(n=state["n"] + 1, P=Pb.clone(), G=G)
+            return G
+
+        energies, it, self.converged, Pb = batched_rhf_iterations(
+            self.Sb, self.Hb, self.X, self.occ_mask, self.pad_orb, two_electron,
+            threshold=threshold, max_iter=max_iter)
+        self.iterations = it
+        self.densities = Pb
+        if final_fp64 is None:
+            final_fp64 = incremental or mixed_cut is not None or screen_thr > 0
+        if final_fp64:
+            G = self.fock_packed(self.to_packed(Pb))
+            energies = 0.5 * torch.sum(Pb * (2.0 * self.Hb + G), dim=(1, 2))
+        e_nuc = torch.as_tensor([m.nuclear_repulsion() for m in self.mols], device=self.dev)
         return (energies + e_nuc).cpu().numpy(), it
+
+
+def batched_task_list(q, pair_class, pair_mol, nprim, thr, nclass, nmol):
+    """Unique shell-quartet tasks (bra pair, ket pair) of many molecules, on the device of
+    the inputs: for every class pair (cb >= ck) and every molecule, the pairs of that
+    molecule with q_bra q_ket >= thr (bra >= ket within one class), quartets never
+    crossing molecules.  Each class segment is ordered by (primitive pairs of the bra, of
+    the ket), molecule by molecule otherwise.  Returns [((la, lb, lc, ld), start, end)]
+    and the [ntask, 2] int32 task array."""
+    dev = q.device
+    key = pair_mol * nclass + pair_class
+    order = torch.argsort(key, stable=True)
+    cnt = torch.bincount(key, minlength=nmol * nclass).view(nmol, nclass)
+    start = (torch.cumsum(cnt.reshape(-1), 0) - cnt.reshape(-1)).view(nmol, nclass)
+    cnt_h = cnt.cpu().numpy()
+    mols = torch.arange(nmol, device=dev)
+    segs, chunks, n = [], [], 0
+    for cb in range(nclass):
+        for ck in range(cb + 1):
+            nb, nk = cnt[:, cb], cnt[:, ck]
+            total = int((cnt_h[:, cb] * cnt_h[:, ck]).sum())
+            if total == 0:
+                continue
+            tot = nb * nk
+            mol = torch.repeat_interleave(mols, tot)
+            local = torch.arange(total, device=dev) - (torch.cumsum(tot, 0) - tot)[mol]
+            nk_m = nk[mol]
+            bra = order[start[mol, cb] + local // nk_m]
+            ket = order[start[mol, ck] + local % nk_m]
+            del mol, local, nk_m
+            keep = q[bra] * q[ket] >= thr
+            if cb == ck:
+                keep &= bra >= ket
+            bra, ket = bra[keep], ket[keep]
+            if bra.numel() == 0:
+                continue
+            perm = torch.argsort(nprim[bra] * 4096 + nprim[ket], stable=True)
+            tk = torch.stack([bra[perm], ket[perm]], 1).to(torch.int32)
+            (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
+            segs.append(((la, lb, lc, ld), n, n + tk.shape[0]))
+            chunks.append(tk)
+            n += tk.shape[0]
+    tasks = torch.cat(chunks) if chunks else torch.zeros((0, 2), dtype=torch.int32, device=dev)
+    return segs, tasks.contiguous()
+
+
+def padded_system(S_list, H_list, nocc, device):
+    """Zero-padded [B, N, N] overlap and core Hamiltonian (identity overlap on the padding),
+    the canonical orthogonaliser of each molecule (eigenvalues ascending, as the reference
+    sorts them, hartreefock/linear_algebra.py:18-25; padded orbitals are zero columns at
+    positions n..N-1), the occupied-orbital mask and the padded-orbital indicator."""
+    dev = torch.device(device)
+    B, N = len(S_list), max(s.shape[0] for s in S_list)
+    S = torch.zeros((B, N, N), dtype=torch.float64, device=dev)
+    H = torch.zeros_like(S)
+    X = torch.zeros_like(S)
+    pad = torch.zeros((B, N), dtype=torch.float64, device=dev)
+    for m, (Sm, Hm) in enumerate(zip(S_list, H_list)):
+        n = Sm.shape[0]
+        S[m, :n, :n] = torch.as_tensor(np.asarray(Sm, dtype=np.float64)).to(dev)
+        H[m, :n, :n] = torch.as_tensor(np.asarray(Hm, dtype=np.float64)).to(dev)
+        S[m, n:, n:] = torch.eye(N - n, dtype=torch.float64, device=dev)
+        s, u = torch.linalg.eigh(S[m, :n, :n])
+        X[m, :n, :n] = u * s.rsqrt().unsqueeze(0)
+        pad[m, n:] = 1.0
+    nocc = torch.as_tensor(np.asarray(nocc), device=dev)
+    occ = (torch.arange(N, device=dev)[None, :] < nocc[:, None]).double()
+    return S, H, X, occ, pad
+
+
+def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold=1e-10,
+                           max_iter=60, diis_subspace=8):
+    """Restricted SCF of B molecules at once over zero-padded [B, N, N] FP64 matrices.
+
+    ``two_electron(P)`` returns G = J - K/2 for the padded densities.  Per molecule: the
+    core-Hamiltonian guess, canonical orthogonaliser ``X`` (zero columns for padded
+    orbitals, which ``pad_orb`` lifts to the top of the spectrum), Pulay DIIS on the
+    orthogonalised commutator SPF - FPS, and the reference's stopping rule |dE| <
+    threshold (hartreefock/scf_procedure.py:24-42).  A molecule that has converged keeps
+    its density (its energy is final) while the others iterate; the DIIS matrix of each
+    molecule is scaled by its largest diagonal element so that a nearly converged
+    molecule does not make the batched solve singular.  Returns the electronic energies,
+    the iteration count, the per-molecule converged flags and the last densities."""
+    dev = Hb.device
+    B = Hb.shape[0]
+    big = 1e6 * pad_orb
+
+    def diag(F):
+        Fo = X.transpose(1, 2) @ F @ X + torch.diag_embed(big)
+        e, c = torch.linalg.eigh(Fo)
+        return e, X @ c
+
+    _, C = diag(Hb)
+    prev = torch.zeros(B, dtype=torch.float64, device=dev)
+    done = torch.zeros(B, dtype=torch.bool, device=dev)
+    hist_f, hist_e = [], []
+    energies = None
+    it = 0
+    for it in range(1, max_iter + 1):
+        Cocc = C * occ_mask[:, None, :]
+        Pb = 2.0 * Cocc @ Cocc.transpose(1, 2)
+        F = Hb + two_electron(Pb)
+        e_now = 0.5 * torch.sum(Pb * (Hb + F), dim=(1, 2))
+        energies = e_now if energies is None else torch.where(done, energies, e_now)
+        if it > 1:
+            done = done | ((e_now - prev).abs() < threshold)
+        prev = e_now
+        if bool(done.all()):
+            break
+        err = Sb @ Pb @ F - F @ Pb @ Sb
+        err = X.transpose(1, 2) @ err @ X
+        hist_f.append(F)
+        hist_e.append(err)
+        if len(hist_f) > diis_subspace:
+            hist_f.pop(0)
+            hist_e.pop(0)
+        if len(hist_f) > 1:
+            k = len(hist_f)
+            E = torch.stack(hist_e, 1)                       # [B, k, N, N]
+            Bk = torch.einsum("bkij,blij->bkl", E, E)
+            scale = Bk.diagonal(dim1=1, dim2=2).amax(-1).clamp_min(1e-300)
+            eye = torch.eye(k, dtype=torch.float64, device=dev)
+            Bm = torch.zeros((B, k + 1, k + 1), dtype=torch.float64, device=dev)
+            Bm[:, :k, :k] = Bk / scale[:, None, None] + 1e-12 * eye
+            Bm[:, :k, k] = 1
+            Bm[:, k, :k] = 1
+            rhs = torch.zeros((B, k + 1), dtype=torch.float64, device=dev)
+            rhs[:, k] = 1
+            c = torch.linalg.solve(Bm, rhs)[:, :k]
+            F = torch.einsum("bk,bkij->bij", c, torch.stack(hist_f, 1))
+        _, C_new = diag(F)
+        C = torch.where(done[:, None, None], C, C_new)
+    return energies, it, done.cpu().numpy(), Pb

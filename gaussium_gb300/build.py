@@ -21,11 +21,17 @@ GEN = os.path.join(BUILD, "gen")
 LIB = os.environ.get("GS_LIB_PATH", os.path.join(PKG, "libgaussium_gb300.so"))
 HOSTCHECK = os.path.join(BUILD, "libhostcheck.so")
 LMAX = 2
-# Classes with total angular momentum L >= WIDE64_MIN (FP64) or >= WIDE32_MIN (FP32) use the
-# warp-cooperative kernel (csrc/eri_wide.cuh); the others one thread per quartet
-# (csrc/eri_kernels.cuh); csrc/eri_launch.cuh dispatches.
-WIDE64_MIN = int(os.environ.get("GS_WIDE64_MIN", "2"))
+# Kernel forms per class (csrc/eri_launch.cuh dispatches): classes with total angular
+# momentum L <= THREAD64_MAX / THREAD32_MAX get the one-thread-per-quartet kernel
+# (csrc/eri_kernels.cuh) in FP64 / FP32, classes with L >= WIDE_PROG_MIN (FP64) or
+# L >= WIDE32_FROM (FP32) the warp-cooperative kernel (csrc/eri_wide.cuh).  Where a class
+# has both, WIDE64_MIN / WIDE32_MIN set the default and gs_set_class_variant (the
+# autotuner) can choose per class at run time.
+WIDE64_MIN = int(os.environ.get("GS_WIDE64_MIN", "3"))
 WIDE32_MIN = int(os.environ.get("GS_WIDE32_MIN", "8"))
+THREAD64_MAX = int(os.environ.get("GS_THREAD64_MAX", "4"))
+THREAD32_MAX = 7
+WIDE32_FROM = 5
 WIDE_PROG_MIN = 2          # classes that get generated warp programs
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -94,10 +100,15 @@ def generate():
                    'static __device__ const int* hlev() { return nullptr; } '
                    'static __device__ const unsigned short* outslot() { return nullptr; } }; }\n'
                    % (tag, *cls))
-        code = ('#define GS_WIDE64_MIN %d\n#define GS_WIDE32_MIN %d\n#include "eri_launch.cuh"\n%s'
+        code = ('#define GS_WIDE64_MIN %d\n#define GS_WIDE32_MIN %d\n#define GS_THREAD64_MAX %d\n'
+                '#define GS_THREAD32_MAX %d\n#define GS_WIDE_FROM %d\n#define GS_WIDE32_FROM %d\n'
+                '#include "eri_launch.cuh"\n%s'
                 'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
                 '    return gs::launch_any<%d, %d, %d, %d>(kind, prec, args, st);\n}\n'
-                % (max(WIDE64_MIN, WIDE_PROG_MIN), max(WIDE32_MIN, WIDE_PROG_MIN), inc, tag, *cls))
+                'int gs_variants_%s(int prec) { return gs::variants<%d, %d, %d, %d>(prec); }\n'
+                % (max(WIDE64_MIN, WIDE_PROG_MIN), max(WIDE32_MIN, WIDE_PROG_MIN), THREAD64_MAX,
+                   THREAD32_MAX, WIDE_PROG_MIN, max(WIDE32_FROM, WIDE_PROG_MIN), inc, tag, *cls,
+                   tag, *cls))
         if not os.path.exists(path) or open(path).read() != code:
             with open(path, "w") as f:
                 f.write(code)

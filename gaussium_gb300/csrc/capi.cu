@@ -7,7 +7,9 @@
 #include "gs_args.h"
 #include "gs_built_classes.h"
 
-#define GS_DECL(A, B, C, D) int gs_launch_##A##B##C##D(int, int, const void*, cudaStream_t);
+#define GS_DECL(A, B, C, D)                                                \
+    int gs_launch_##A##B##C##D(int, int, const void*, cudaStream_t); \
+    int gs_variants_##A##B##C##D(int);
 GS_FOR_EACH_BUILT(GS_DECL)
 #undef GS_DECL
 
@@ -21,6 +23,23 @@ launch_fn find_class(int la, int lb, int lc, int ld) {
     GS_FOR_EACH_BUILT(GS_FIND)
 #undef GS_FIND
     return nullptr;
+}
+
+int find_variants(int la, int lb, int lc, int ld, int prec) {
+#define GS_FIND(A, B, C, D) \
+    if (la == A && lb == B && lc == C && ld == D) return gs_variants_##A##B##C##D(prec);
+    GS_FOR_EACH_BUILT(GS_FIND)
+#undef GS_FIND
+    return 0;
+}
+
+// Kernel form per class and precision chosen at run time: 0 = the built-in default by
+// total angular momentum, 1 = one thread per quartet, 2 = one warp per quartet.  It rides
+// in bits 8.. of the precision argument of the class launchers.
+int g_variant[3][3][3][3][2] = {};
+
+inline int pv(int la, int lb, int lc, int ld, int prec) {
+    return prec | (g_variant[la][lb][lc][ld][prec == 64 ? 0 : 1] << 8);
 }
 
 inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
@@ -145,6 +164,21 @@ int gs_class_available(int la, int lb, int lc, int ld) {
     return find_class(la, lb, lc, ld) != nullptr;
 }
 
+int gs_class_variants(int la, int lb, int lc, int ld, int precision) {
+    if (!find_class(la, lb, lc, ld)) return -GS_ERR_CLASS;
+    if (precision != 64 && precision != 32) return -GS_ERR_ARG;
+    return find_variants(la, lb, lc, ld, precision);
+}
+
+int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant) {
+    if (!find_class(la, lb, lc, ld)) return GS_ERR_CLASS;
+    if ((precision != 64 && precision != 32) || variant < 0 || variant > 2) return GS_ERR_ARG;
+    if (variant && !(find_variants(la, lb, lc, ld, precision) & (1 << (variant - 1))))
+        return GS_ERR_ARG;
+    g_variant[la][lb][lc][ld][precision == 64 ? 0 : 1] = variant;
+    return GS_OK;
+}
+
 int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
                    const double* coef, int npairs, const int* pair_shells,
                    const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
@@ -165,7 +199,7 @@ int gs_schwarz(int la, int lb, void* pair_rec, const void* prim64, const double*
     if (!f) return GS_ERR_CLASS;
     if (npair < 0 || !pair_rec || !prim64 || !comp_scale || !q) return GS_ERR_ARG;
     gs::SchwarzArgs a{(const gs::PairRec*)pair_rec, prim64, comp_scale, pair_index, npair, q};
-    int rc = f(GS_KIND_SCHWARZ, 64, &a, S(stream));
+    int rc = f(GS_KIND_SCHWARZ, pv(la, lb, la, lb, 64), &a, S(stream));
     if (rc) return rc;
     if (npairs_total > 0)
         k_set_qmax<<<(npairs_total + 127) / 128, 128, 0, S(stream)>>>((gs::PairRec*)pair_rec, q,
@@ -183,7 +217,7 @@ int gs_eri_blocks(int la, int lb, int lc, int ld, int precision, const void* pai
         return GS_ERR_ARG;
     gs::WriteArgs a{(const gs::PairRec*)pair_rec, prim, comp_scale, (const gs::WriteTask*)tasks,
                     ntask, out};
-    return f(GS_KIND_WRITE, precision, &a, S(stream));
+    return f(GS_KIND_WRITE, pv(la, lb, lc, ld, precision), &a, S(stream));
 }
 
 int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
@@ -221,7 +255,7 @@ int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_r
     a.mol_dmax = nullptr;
     a.mat_stride = (long long)nbf * nbf;
     a.ntask_dev = nullptr;
-    return f(GS_KIND_JK, precision, &a, S(stream));
+    return f(GS_KIND_JK, pv(la, lb, lc, ld, precision), &a, S(stream));
 }
 
 int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
@@ -261,7 +295,7 @@ int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void
     a.mol_dmax = mol_dmax;
     a.mat_stride = mat_stride;
     a.ntask_dev = nullptr;
-    return f(GS_KIND_JK, precision, &a, S(stream));
+    return f(GS_KIND_JK, pv(la, lb, lc, ld, precision), &a, S(stream));
 }
 
 // Bytes of workspace gs_fock_jk_mixed needs for ntask tasks.
@@ -316,12 +350,12 @@ int fock_jk_mixed_impl(int la, int lb, int lc, int ld, const void* pair_rec, con
     a.prims = prim64;
     a.tasks = l64;
     a.ntask_dev = counts;
-    int rc = f(GS_KIND_JK, 64, &a, S(stream));
+    int rc = f(GS_KIND_JK, pv(la, lb, lc, ld, 64), &a, S(stream));
     if (rc) return rc;
     a.prims = prim32;
     a.tasks = l32;
     a.ntask_dev = counts + 1;
-    return f(GS_KIND_JK, 32, &a, S(stream));
+    return f(GS_KIND_JK, pv(la, lb, lc, ld, 32), &a, S(stream));
 }
 }  // namespace
 

@@ -378,9 +378,11 @@ __global__ void k_one_electron_grad(gs::ShellView sv, const double* __restrict__
             }
         }
     }
+    const int atom_a = shell_atom[sa], atom_b = shell_atom[sb];
+    if ((unsigned)atom_a >= (unsigned)natom || (unsigned)atom_b >= (unsigned)natom) return;
     for (int x = 0; x < 3; ++x) {
-        atomicAdd(grad + 3 * shell_atom[sa] + x, gA[x]);
-        atomicAdd(grad + 3 * shell_atom[sb] + x, gB[x]);
+        atomicAdd(grad + 3 * atom_a + x, gA[x]);
+        atomicAdd(grad + 3 * atom_b + x, gB[x]);
     }
 }
 

@@ -125,14 +125,16 @@ def one_electron_gradient_kernel(sb, mol, shell_atom, P, W, device="cuda"):
     t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt)).to(dev)
     pairs = t(np.stack([i, j], 1), np.int32)
     grad = torch.zeros(len(mol.symbols) * 3, dtype=torch.float64, device=dev)
+    # every buffer the launch reads stays referenced until after it: a temporary freed to
+    # the caching allocator inside the argument list would be handed to the next one
+    sa_d, xyz_d, z_d = t(shell_atom, np.int32), t(mol.coords, np.float64), t(mol.charges, np.float64)
+    p_d, w_d = t(P, np.float64), t(W, np.float64)
     L = _lib.lib()
     _lib.check(L.gs_one_electron_grad(_lib.ptr(ds.centre), _lib.ptr(ds.l), _lib.ptr(ds.prim_off),
                                       _lib.ptr(ds.expo), _lib.ptr(ds.coef), _lib.ptr(ds.comp_scale),
-                                      _lib.ptr(ds.func_off), _lib.ptr(t(shell_atom, np.int32)),
-                                      len(i), _lib.ptr(pairs), sb.nbf, len(mol.symbols),
-                                      _lib.ptr(t(mol.coords, np.float64)),
-                                      _lib.ptr(t(mol.charges, np.float64)), _lib.ptr(t(P, np.float64)),
-                                      _lib.ptr(t(W, np.float64)), _lib.ptr(grad), _lib.stream()),
+                                      _lib.ptr(ds.func_off), _lib.ptr(sa_d), len(i), _lib.ptr(pairs),
+                                      sb.nbf, len(mol.symbols), _lib.ptr(xyz_d), _lib.ptr(z_d),
+                                      _lib.ptr(p_d), _lib.ptr(w_d), _lib.ptr(grad), _lib.stream()),
                "gs_one_electron_grad")
     return grad.view(-1, 3).cpu().numpy()
 
@@ -148,9 +150,16 @@ def nuclear_repulsion_gradient(mol):
     return g
 
 
+def _check_atoms(shell_atom, natom):
+    sa = np.asarray(shell_atom)
+    if sa.size and (sa.min() < 0 or sa.max() >= natom):
+        raise ValueError("shell_atom holds an atom index outside [0, natom)")
+
+
 def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom):
     """Two-electron gradient through the fused adjoint kernel (gs_eri_grad), one launch per
     class over the engine's Schwarz-screened unique quartets."""
+    _check_atoms(shell_atom, natom)
     if np.any(sb.l >= 2):
         raise NotImplementedError("the fused gradient kernels cover s/p shells")
     dev = engine.dev
@@ -170,6 +179,7 @@ def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom):
 def eri_gradient_blocks(sb, engine: JKEngine, shell_atom, P, natom):
     """The same two-electron gradient from explicit raised/lowered blocks (gs_eri_blocks)
     contracted by gs_eri_grad_contract; slower, kept as an independent cross-check."""
+    _check_atoms(shell_atom, natom)
     comb, raised, lowered = combined_basis(sb)
     tasks = engine.tasks[:engine.ntasks].cpu().numpy()
     ps = engine.pairs.host_shells
@@ -200,12 +210,11 @@ def eri_gradient_blocks(sb, engine: JKEngine, shell_atom, P, natom):
     t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt)).to(dev)
     grad = torch.zeros(natom * 3, dtype=torch.float64, device=dev)
     pt = torch.as_tensor(np.ascontiguousarray(P)).to(dev)
-    qd, bd = t(quart, np.int32), t(boff, np.int64)
+    qd, bd, sa_d = t(quart, np.int32), t(boff, np.int64), t(shell_atom, np.int32)
     L = _lib.lib()
     _lib.check(L.gs_eri_grad_contract(nq, _lib.ptr(qd), _lib.ptr(bd), _lib.ptr(blocks),
                                       _lib.ptr(engine.ds.l), _lib.ptr(engine.ds.func_off),
-                                      _lib.ptr(engine.ds.comp_scale),
-                                      _lib.ptr(t(shell_atom, np.int32)), sb.nbf, _lib.ptr(pt),
+                                      _lib.ptr(engine.ds.comp_scale), _lib.ptr(sa_d), sb.nbf, _lib.ptr(pt),
                                       _lib.ptr(grad), _lib.stream()), "gs_eri_grad_contract")
     return grad.view(natom, 3).cpu().numpy()
 

@@ -92,6 +92,14 @@ def water_cluster(n, seed=None, min_oo=2.6, density=1.0):
     return Molecule(["O", "H", "H"] * n, np.array(coords) * BOHR_PER_ANGSTROM)
 
 
+def perturbed(mol, amplitude_angstrom=0.1, seed=4):
+    """Every nucleus moved by ``amplitude_angstrom`` in a seeded random direction."""
+    rng = np.random.default_rng(seed)
+    d = rng.standard_normal(mol.coords.shape)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return Molecule(mol.symbols, mol.coords + amplitude_angstrom * BOHR_PER_ANGSTROM * d)
+
+
 def random_chain(seed, min_heavy=2, max_atoms=30):
     """Random bonded C/N/O chain with hydrogens filling free valences; even electron count."""
     rng = np.random.default_rng(seed)

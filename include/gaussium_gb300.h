@@ -50,6 +50,18 @@ int gs_record_sizes(int* sizes);
 /* 1 if the (la lb | lc ld) class kernel is built into this library, else 0. */
 int gs_class_available(int la, int lb, int lc, int ld);
 
+/* Kernel forms built for class (la lb|lc ld) in the given precision (64 or 32): bit 0 the
+ * one-thread-per-quartet kernel, bit 1 the warp-per-quartet kernel; negative status on a
+ * bad class or precision.  No reference counterpart (the reference has one code path). */
+int gs_class_variants(int la, int lb, int lc, int ld, int precision);
+
+/* Chooses the kernel form later calls use for (la lb|lc ld) in that precision, process-wide:
+ * 0 = the built-in default by total angular momentum, 1 = thread per quartet, 2 = warp per
+ * quartet (a form the class was not built with is GS_ERR_ARG).  Results do not depend on
+ * the form beyond rounding; the autotuner times both on the caller's task lists.  No
+ * reference counterpart. */
+int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant);
+
 /* K0 shell-pair builder.  Replaces the per-primitive-quartet prologue of
  * ObaraSaika.integrate (integrals/twoelectronrepulsion/obara_saika_scheme.py:52-70:
  * Gaussian product centre, exponent sums, exp(-ab/p |AB|^2) and the contraction/

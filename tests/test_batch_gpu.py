@@ -6,13 +6,33 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_batched_energies_match_single(gpu_lib):
+@pytest.fixture(scope="module")
+def batch_case():
     from gaussium_gb300 import batch, driver, molecules
     mols = [molecules.water_cluster(1, seed=1), molecules.random_chain(3),
             molecules.random_chain(1), molecules.water_cluster(2, seed=5)]
-    single = [driver.rhf(m, threshold=1e-11)["energy"] for m in mols]
-    b = batch.BatchedRHF(mols)
+    single = np.array([driver.rhf(m, threshold=1e-11)["energy"] for m in mols])
+    return batch.BatchedRHF(mols), single
+
+
+def test_batched_energies_match_single(gpu_lib, batch_case):
+    b, single = batch_case
     e, it = b.run(threshold=1e-11)
-    assert np.max(np.abs(e - np.array(single))) < 1e-7
+    assert b.converged.all() and it < 60
+    assert np.max(np.abs(e - single)) < 1e-8
     e2, _ = b.run(threshold=1e-11, use_graph=False)
     assert np.max(np.abs(e2 - e)) < 1e-9
+
+
+def test_batched_mixed_incremental_within_target(gpu_lib, batch_case):
+    b, single = batch_case
+    e, it = b.run(threshold=1e-10, mixed_cut=1e-2, screen_thr=1e-12, incremental=True)
+    assert b.converged.all()
+    assert np.max(np.abs(e - single)) < 1e-6
+
+
+def test_batched_task_list_matches_engine_count(gpu_lib, batch_case):
+    from gaussium_gb300.engine import JKEngine
+    b, _ = batch_case
+    total = sum(JKEngine(sb, schwarz_thr=1e-12).ntasks for sb in b.sbs)
+    assert b.ntasks == total
