@@ -35,6 +35,11 @@ WORKLOAD = "synthetic ERI microbench: 2,000,000 seeded shell quartets, l uniform
            "K uniform 1-6, exponents log-uniform [0.05,1e4], centres in a 10 A cube"
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of k_wide_write<2,2,2,1,double> on the
+# 200,000-quartet case (9,922 quartets of the class): 11,945,472 + 5,819,392 bytes
+NCU_DRAM_BYTES_PER_QUARTET = {(2, 2, 2, 1): (11945472 + 5819392) / 9922}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,6 +333,15 @@ def run_gpu(args, rank, world):
 
     n_all = args.quartets * world
     ms64, ms32 = res[64]["ms"], res[32]["ms"]
+    # DRAM bytes per quartet of the dominant kernel from one ncu capture of a 200,000-quartet
+    # case of this workload (dram__bytes_read.sum + dram__bytes_write.sum), scaled by the
+    # class's quartet count here
+    traffic, traffic_src = None, None
+    if dom in NCU_DRAM_BYTES_PER_QUARTET:
+        nq_dom = sum(e - s for c, s, e in batch.segments if c == dom)
+        traffic = NCU_DRAM_BYTES_PER_QUARTET[dom] * nq_dom
+        traffic_src = ("ncu capture of the 200,000-quartet case, scaled by quartets "
+                       f"({nq_dom} of this class)")
     line = {
         "metric": METRIC,
         "value": n_all / (ms64 * 1e-3),
@@ -353,8 +367,11 @@ def run_gpu(args, rank, world):
                    "kernel_forms_autotuned": forms},
         "roofline": {"bound": "fp64", "kernel": "eri class " + "".join(map(str, dom)) + " FP64",
                      "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": achieved / peak64, "traffic": None,
-                     "peak_source": "gs_fma_probe FP64 FMA rate measured in this run"},
+                     "frac": achieved / peak64, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (dram read + write)",
+                     "traffic_source": traffic_src,
+                     "peak_source": "gs_fma_probe FP64 FMA rate measured in this run "
+                                    "(no FP64 figure among the pool's measured peaks)"},
         "fp64": {"value": n_all / (ms64 * 1e-3), "ms_per_step": ms64,
                  "tflops": total_flops / (ms64 * 1e-3) / 1e12,
                  "frac_of_fp64_peak": total_flops / (ms64 * 1e-3) / 1e12 / peak64},
@@ -513,12 +530,27 @@ def run_gradient(args, rank, world):
     eps, C = scf.LinearAlgebra(S).diagonalize(res.fock)
     W = 2.0 * (C[:, :nocc] * eps[:nocc]) @ C[:, :nocc].T
     sa = gradient.shell_atoms(mol, sb)
-    gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
+    natom = len(mol.symbols)
+    forms = {}
+    if not args.no_tune:
+        chosen = gradient.tune_eri_gradient(sb, eng, sa, P, natom, reps=2)
+        forms = {"%d%d%d%d" % c: ("warp" if r["form"] == 2 else "thread") for c, r in chosen.items()}
+    gradient.eri_gradient(sb, eng, sa, P, natom)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ge = gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
+    ge = gradient.eri_gradient(sb, eng, sa, P, natom)
     torch.cuda.synchronize()
     t_eri_grad = time.perf_counter() - t0
+    # per-class device time of the ERI gradient launches
+    per_cls = {}
+    st = torch.cuda.current_stream()
+    for cls, s0, s1 in eng.segments:
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        gradient.eri_gradient(sb, eng, sa, P, natom, classes=[cls], host=False)
+        a1.record(st)
+        a1.synchronize()
+        per_cls["%d%d%d%d" % cls] = round(a0.elapsed_time(a1), 3)
     gradient.one_electron_gradient_kernel(sb, mol, sa, P, W)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -548,6 +580,7 @@ def run_gradient(args, rank, world):
                    "fd_coordinates_checked": int(ncoord), "fd_step_bohr": h},
         "energy": e, "max_abs_grad_minus_fd": err,
         "eri_gradient_ms": t_eri_grad * 1e3, "one_electron_gradient_ms": t_one_grad * 1e3,
+        "eri_gradient_ms_per_class": per_cls, "gradient_kernel_forms_autotuned": forms,
         "fock_build_ms": t_fock * 1e3, "scf_plus_gradient_s": t_total,
     }
     if rank == 0:

@@ -81,6 +81,36 @@ def tune_blocks(batch, out, precisions=(64, 32), reps=3):
                 precisions, reps)
 
 
+def grad_forms(cls):
+    """Kernel forms built for a gradient class: a subset of {THREAD, WARP}."""
+    m = _lib.lib().gs_eri_grad_variants(*cls)
+    if m < 0:
+        _lib.check(-m, f"gs_eri_grad_variants{cls}")
+    return [v for v in (THREAD, WARP) if m & (1 << (v - 1))]
+
+
+def set_grad_form(cls, variant):
+    _lib.check(_lib.lib().gs_set_eri_grad_variant(*cls, variant), f"gs_set_eri_grad_variant{cls}")
+
+
+def tune_gradient(segments, run_class, reps=3):
+    """Choose the faster form of every gradient class of ``segments`` that has two;
+    ``run_class(cls)`` launches that class's gradient work once.  Returns {cls: {...}}."""
+    chosen = {}
+    for cls, s, e in segments:
+        fs = grad_forms(cls)
+        if e <= s or len(fs) < 2:
+            continue
+        times = {}
+        for v in fs:
+            set_grad_form(cls, v)
+            times[v] = _time(lambda: run_class(cls), reps)
+        best = min(times, key=times.get)
+        set_grad_form(cls, best)
+        chosen[cls] = {"form": best, "ms": times}
+    return chosen
+
+
 def reset(segments, precisions=(64, 32)):
     """Back to the built-in default form for every class of ``segments``."""
     for prec in precisions:

@@ -215,7 +215,8 @@ class BatchedRHF:
         if final_fp64:
             G = self.fock_packed(self.to_packed(Pb))
             energies = 0.5 * torch.sum(Pb * (2.0 * self.Hb + G), dim=(1, 2))
-        e_nuc = torch.as_tensor([m.nuclear_repulsion() for m in self.mols], device=self.dev)
+        e_nuc = torch.tensor([m.nuclear_repulsion() for m in self.mols], dtype=torch.float64,
+                             device=self.dev)
         return (energies + e_nuc).cpu().numpy(), it
 
 

@@ -143,7 +143,8 @@ def build(jobs=None, verbose=False):
     todo.append((os.path.join(CSRC, "grad.cu"), [], os.path.join(BUILD, "grad.o")))
     todo.append((os.path.join(CSRC, "eri_grad.cu"),
                  [os.path.join(CSRC, "eri_grad.cuh")] +
-                 [os.path.join(GEN, f"eri_grad_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110", "1111")],
+                 [os.path.join(GEN, f"eri_grad_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110", "1111")] +
+                 [os.path.join(GEN, f"eri_gradt_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110")],
                  os.path.join(BUILD, "eri_grad.o")))
     jobs = jobs or max(1, os.cpu_count() or 1)
     changed = False

@@ -46,15 +46,59 @@ inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
 
 int check_launch() { return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA; }
 
-__global__ void k_pairs_build(gs::ShellView sv, int npairs, const int* __restrict__ pair_shells,
-                              const int* __restrict__ pair_prim_off, gs::PairRec* pairs,
-                              gs::PrimRec<double>* p64, gs::PrimRec<float>* p32, double max_exp,
-                              int* __restrict__ kept) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npairs) return;
-    gs::make_pair(sv, pair_shells[2 * i], pair_shells[2 * i + 1], pair_prim_off[i], pairs[i], p64,
-                  p32, max_exp);
-    if (kept) kept[i] = pairs[i].nprim;
+// K0: one warp per shell pair.  Lane k takes primitive pair k (k = i nb + j, then k + 32),
+// a ballot ranks the kept ones so that they are written contiguously in the same order as
+// the host form (make_pair), and consecutive lanes write consecutive records.
+__global__ void __launch_bounds__(256) k_pairs_build(gs::ShellView sv, int npairs,
+                                                     const int* __restrict__ pair_shells,
+                                                     const int* __restrict__ pair_prim_off,
+                                                     gs::PairRec* pairs, gs::PrimRec<double>* p64,
+                                                     gs::PrimRec<float>* p32, double max_exp,
+                                                     int* __restrict__ kept) {
+    const int lane = threadIdx.x & 31;
+    const long long pi = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (pi >= npairs) return;
+    const int sa = pair_shells[2 * pi], sb = pair_shells[2 * pi + 1];
+    const double* A = sv.centre + 3 * sa;
+    const double* B = sv.centre + 3 * sb;
+    const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
+    const double ab2 = ABx * ABx + ABy * ABy + ABz * ABz;
+    const int a0 = sv.prim_off[sa], b0 = sv.prim_off[sb];
+    const int nb = sv.prim_off[sb + 1] - b0;
+    const int ntot = (sv.prim_off[sa + 1] - a0) * nb;
+    const int base = pair_prim_off[pi];
+    int n = 0;
+    for (int k0 = 0; k0 < ntot; k0 += 32) {
+        const int k = k0 + lane;
+        bool keep = false;
+        double a = 0.0, b = 0.0;
+        int i = 0, j = 0;
+        if (k < ntot) {
+            i = a0 + k / nb;
+            j = b0 + k % nb;
+            a = sv.expo[i];
+            b = sv.expo[j];
+            keep = gs::prim_pair_kept(a, b, ab2, max_exp);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int r = base + n + __popc(m & ((1u << lane) - 1u));
+            const gs::PrimRec<double> rec = gs::prim_pair(A, B, a, b, ab2, sv.coef[i], sv.coef[j]);
+            p64[r] = rec;
+            if (p32) p32[r] = gs::prim_pair32(rec);
+        }
+        n += __popc(m);
+    }
+    if (lane == 0) {
+        gs::PairRec pr;
+        pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
+        pr.prim_off = base;
+        pr.nprim = n;
+        pr.sa = sa; pr.sb = sb;
+        pr.qmax = 0.0f; pr.pad = 0;
+        pairs[pi] = pr;
+        if (kept) kept[pi] = n;
+    }
 }
 
 __global__ void k_set_qmax(gs::PairRec* pairs, const double* __restrict__ q, int npairs) {
@@ -187,7 +231,7 @@ int gs_pairs_build(const double* centre, const int* l, const int* prim_off, cons
         return GS_ERR_ARG;
     if (npairs == 0) return GS_OK;
     gs::ShellView sv{centre, l, prim_off, expo, coef};
-    k_pairs_build<<<(npairs + 127) / 128, 128, 0, S(stream)>>>(
+    k_pairs_build<<<(unsigned)(((long long)npairs * 32 + 255) / 256), 256, 0, S(stream)>>>(
         sv, npairs, pair_shells, pair_prim_off, (gs::PairRec*)pair_rec,
         (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32, max_exp, kept);
     return check_launch();

@@ -222,10 +222,42 @@ struct ShellView {
 
 constexpr double kSqrt2Pi52 = 5.914967172795613;  // sqrt(2 pi^(5/2))
 
+// Record of the primitive pair (a at A, b at B) with contraction coefficients ca, cb.
+GS_HD GS_INLINE PrimRec<double> prim_pair(const double* A, const double* B, double a, double b,
+                                          double ab2, double ca, double cb) {
+    const double p = a + b, ip = 1.0 / p;
+    PrimRec<double> r;
+    r.p = p;
+    r.i2p = 0.5 * ip;
+    r.Px = (a * A[0] + b * B[0]) * ip;
+    r.Py = (a * A[1] + b * B[1]) * ip;
+    r.Pz = (a * A[2] + b * B[2]) * ip;
+    r.PAx = r.Px - A[0]; r.PAy = r.Py - A[1]; r.PAz = r.Pz - A[2];
+    r.Kp = kSqrt2Pi52 * ca * cb * exp(-a * b * ip * ab2) * ip;
+    r.pad = a;          // exponent of the first shell (derivative weights)
+    return r;
+}
+
+GS_HD GS_INLINE PrimRec<float> prim_pair32(const PrimRec<double>& r) {
+    PrimRec<float> f;
+    f.p = (float)r.p; f.i2p = (float)r.i2p;
+    f.Px = (float)r.Px; f.Py = (float)r.Py; f.Pz = (float)r.Pz;
+    f.PAx = (float)r.PAx; f.PAy = (float)r.PAy; f.PAz = (float)r.PAz;
+    f.Kp = (float)r.Kp; f.pad0 = f.pad1 = f.pad2 = 0.0f;
+    return f;
+}
+
+// Primitive-pair screen: drop the pair when its Gaussian-product factor exp(-ab/p |AB|^2)
+// is below exp(-max_exp) (max_exp > 0).
+GS_HD GS_INLINE bool prim_pair_kept(double a, double b, double ab2, double max_exp) {
+    return !(max_exp > 0.0 && a * b * (1.0 / (a + b)) * ab2 > max_exp);
+}
+
 // Fill the PairRec and the primitive-pair records of shell pair (sa, sb); la >= lb.
 // Primitive pairs whose Gaussian-product factor exp(-ab/p |AB|^2) is below exp(-max_exp)
 // are dropped when max_exp > 0 (their contributions are below that factor times the
-// normalised block's scale); pr.nprim is the number kept.
+// normalised block's scale); pr.nprim is the number kept.  Host form (tests); the device
+// builds the same records one warp per pair (capi.cu, k_pairs_build).
 GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off, PairRec& pr,
                                PrimRec<double>* pd, PrimRec<float>* pf, double max_exp = 0.0) {
     const double* A = S.centre + 3 * sa;
@@ -236,33 +268,16 @@ GS_HD GS_INLINE void make_pair(const ShellView& S, int sa, int sb, int prim_off,
     const int b0 = S.prim_off[sb], b1 = S.prim_off[sb + 1];
     pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
     pr.prim_off = prim_off;
-    pr.nprim = (a1 - a0) * (b1 - b0);
     pr.sa = sa; pr.sb = sb;
     pr.qmax = 0.0f; pr.pad = 0;
     int n = prim_off;
     for (int i = a0; i < a1; ++i) {
         for (int j = b0; j < b1; ++j) {
             const double a = S.expo[i], b = S.expo[j];
-            const double p = a + b, ip = 1.0 / p;
-            if (max_exp > 0.0 && a * b * ip * ab2 > max_exp) continue;
-            PrimRec<double> r;
-            r.p = p;
-            r.i2p = 0.5 * ip;
-            r.Px = (a * A[0] + b * B[0]) * ip;
-            r.Py = (a * A[1] + b * B[1]) * ip;
-            r.Pz = (a * A[2] + b * B[2]) * ip;
-            r.PAx = r.Px - A[0]; r.PAy = r.Py - A[1]; r.PAz = r.Pz - A[2];
-            r.Kp = kSqrt2Pi52 * S.coef[i] * S.coef[j] * exp(-a * b * ip * ab2) * ip;
-            r.pad = a;          // exponent of the first shell (derivative weights)
+            if (!prim_pair_kept(a, b, ab2, max_exp)) continue;
+            const PrimRec<double> r = prim_pair(A, B, a, b, ab2, S.coef[i], S.coef[j]);
             pd[n] = r;
-            if (pf) {
-                PrimRec<float> f;
-                f.p = (float)r.p; f.i2p = (float)r.i2p;
-                f.Px = (float)r.Px; f.Py = (float)r.Py; f.Pz = (float)r.Pz;
-                f.PAx = (float)r.PAx; f.PAy = (float)r.PAy; f.PAz = (float)r.PAz;
-                f.Kp = (float)r.Kp; f.pad0 = f.pad1 = f.pad2 = 0.0f;
-                pf[n] = f;
-            }
+            if (pf) pf[n] = prim_pair32(r);
             ++n;
         }
     }

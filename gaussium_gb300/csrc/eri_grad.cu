@@ -9,19 +9,61 @@
 #include "eri_grad_1100.h"
 #include "eri_grad_1110.h"
 #include "eri_grad_1111.h"
+#include "eri_gradt_0000.h"
+#include "eri_gradt_1000.h"
+#include "eri_gradt_1010.h"
+#include "eri_gradt_1100.h"
+#include "eri_gradt_1110.h"
+
+namespace {
+// Kernel form per gradient class: 0 = default (thread per quartet up to total angular
+// momentum 2, warp above), 1 = thread per quartet, 2 = warp per quartet.
+int g_grad_variant[2][2][2][2] = {};
+
+constexpr bool has_thread(int la, int lb, int lc, int ld) { return la + lb + lc + ld <= 3; }
+
+bool valid_class(int la, int lb, int lc, int ld) {
+#define GS_GV(A, B, C, D) \
+    if (la == A && lb == B && lc == C && ld == D) return true;
+    GS_FOR_EACH_GRAD(GS_GV)
+#undef GS_GV
+    return false;
+}
+}  // namespace
+
+extern "C" int gs_eri_grad_variants(int la, int lb, int lc, int ld) {
+    if (!valid_class(la, lb, lc, ld)) return -GS_ERR_CLASS;
+    return (has_thread(la, lb, lc, ld) ? 1 : 0) | 2;
+}
+
+extern "C" int gs_set_eri_grad_variant(int la, int lb, int lc, int ld, int variant) {
+    if (!valid_class(la, lb, lc, ld)) return GS_ERR_CLASS;
+    if (variant < 0 || variant > 2 || (variant == 1 && !has_thread(la, lb, lc, ld)))
+        return GS_ERR_ARG;
+    g_grad_variant[la][lb][lc][ld] = variant;
+    return GS_OK;
+}
 
 extern "C" int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
                            const double* comp_scale, const int* func_off, const int* shell_atom,
-                           int ntask, const int* tasks, int nbf, const double* density,
+                           int ntask, const int* tasks, int nbf, int natom, const double* density,
                            double* grad, void* stream) {
-    if (ntask < 0 || nbf <= 0 || !pair_rec || !prim64 || !comp_scale || !func_off || !shell_atom ||
-        (ntask > 0 && !tasks) || !density || !grad)
+    if (ntask < 0 || nbf <= 0 || natom <= 0 || !pair_rec || !prim64 || !comp_scale || !func_off ||
+        !shell_atom || (ntask > 0 && !tasks) || !density || !grad)
         return GS_ERR_ARG;
+    if (!valid_class(la, lb, lc, ld)) return GS_ERR_CLASS;
     gs::GradArgs a{(const gs::PairRec*)pair_rec, (const gs::PrimRec<double>*)prim64, comp_scale,
-                   func_off, shell_atom, (const int2*)tasks, ntask, nbf, density, grad};
+                   func_off, shell_atom, (const int2*)tasks, ntask, nbf, density, grad, natom};
     cudaStream_t st = (cudaStream_t)stream;
-#define GS_GL(A, B, C, D) \
-    if (la == A && lb == B && lc == C && ld == D) return gs::launch_grad<A, B, C, D>(a, st);
+    const int v = g_grad_variant[la][lb][lc][ld];
+    const bool thread = v ? v == 1 : la + lb + lc + ld <= 2;
+#define GS_GL(A, B, C, D)                                                                 \
+    if (la == A && lb == B && lc == C && ld == D) {                                       \
+        if constexpr (A + B + C + D <= 3) {                                               \
+            if (thread) return gs::launch_grad_thread<A, B, C, D>(a, st);                 \
+        }                                                                                 \
+        return gs::launch_grad<A, B, C, D>(a, st);                                        \
+    }
     GS_FOR_EACH_GRAD(GS_GL)
 #undef GS_GL
     return GS_ERR_CLASS;

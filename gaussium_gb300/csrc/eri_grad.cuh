@@ -11,6 +11,7 @@
 namespace gs {
 
 template <int LA, int LB, int LC, int LD> struct GradProg;
+template <int LA, int LB, int LC, int LD> struct GradThread;
 
 struct GradArgs {
     const PairRec* pairs;
@@ -23,6 +24,7 @@ struct GradArgs {
     int nbf;
     const double* P;
     double* grad;
+    int natom;
 };
 
 constexpr int kGradWarps = 2;
@@ -235,6 +237,116 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
                 atomicAdd(a.grad + 3 * a.shell_atom[sh[3]] + x, -g[3 * cen + x]);
             }
     }
+}
+
+// Thread-per-quartet form for the small classes (generated straight-line code, csrc
+// gen_grad.py emit_grad_thread): each thread runs the same VRR, accumulation, HRR and
+// density contraction as the warp form for its own quartet, with node values and
+// accumulators in registers.  Gradient contributions are summed per block in shared
+// memory (3 natom doubles) before one global atomic per atom coordinate.
+constexpr int kGradThreads = 128;
+constexpr int kGradSmemAtoms = 2048;
+
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs a) {
+    using W = GradThread<LA, LB, LC, LD>;
+    constexpr int L = W::L;
+    constexpr int NA = (LA + 1) * (LA + 2) / 2, NB = (LB + 1) * (LB + 2) / 2;
+    constexpr int NC = (LC + 1) * (LC + 2) / 2, ND = (LD + 1) * (LD + 2) / 2;
+    extern __shared__ double sg[];
+    const bool shared_sum = a.natom > 0 && a.natom <= kGradSmemAtoms;
+    if (shared_sum) {
+        for (int i = threadIdx.x; i < 3 * a.natom; i += blockDim.x) sg[i] = 0.0;
+        __syncthreads();
+    }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < a.ntask) {
+        const int2 task = a.tasks[t];
+        const PairRec B = a.pairs[task.x];
+        const PairRec K = a.pairs[task.y];
+        double H[W::HSIZE];
+#pragma unroll
+        for (int k = 0; k < W::NACC; ++k) H[k] = 0.0;
+        const int nK = K.nprim, ntot = B.nprim * nK;
+        for (int i = 0; i < ntot; ++i) {
+            const PrimRec<double> P = a.prims[B.prim_off + i / nK];
+            const PrimRec<double> Q = a.prims[K.prim_off + i % nK];
+            double c[kNCoefG], n[W::NVSLOT];
+            wide_setup_m<L, double>(P, Q, c, n);
+            c[32] = 2.0 * P.pad;               // 2 alpha (first bra shell)
+            c[33] = 2.0 * (P.p - P.pad);       // 2 beta
+            c[34] = 2.0 * Q.pad;               // 2 gamma (first ket shell)
+            W::prim(c, n, H);
+        }
+        const double dv[6] = {B.ABx, B.ABy, B.ABz, K.ABx, K.ABy, K.ABz};
+        W::hrr(H, dv);
+        const int fa = a.func_off[B.sa], fb = a.func_off[B.sb];
+        const int fc = a.func_off[K.sa], fd = a.func_off[K.sb];
+        const int nbf = a.nbf;
+        const double* Pm = a.P;
+        double pab[NA * NB], pcd[NC * ND], pac[NA * NC], pbd[NB * ND], pad[NA * ND], pbc[NB * NC];
+#pragma unroll
+        for (int i = 0; i < NA; ++i) {
+#pragma unroll
+            for (int j = 0; j < NB; ++j) pab[i * NB + j] = Pm[(fa + i) * nbf + fb + j];
+#pragma unroll
+            for (int j = 0; j < NC; ++j) pac[i * NC + j] = Pm[(fa + i) * nbf + fc + j];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) pad[i * ND + j] = Pm[(fa + i) * nbf + fd + j];
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+#pragma unroll
+            for (int j = 0; j < ND; ++j) pbd[i * ND + j] = Pm[(fb + i) * nbf + fd + j];
+#pragma unroll
+            for (int j = 0; j < NC; ++j) pbc[i * NC + j] = Pm[(fb + i) * nbf + fc + j];
+        }
+#pragma unroll
+        for (int i = 0; i < NC; ++i)
+#pragma unroll
+            for (int j = 0; j < ND; ++j) pcd[i * ND + j] = Pm[(fc + i) * nbf + fd + j];
+        double cs0[NA], cs1[NB], cs2[NC];
+#pragma unroll
+        for (int i = 0; i < NA; ++i) cs0[i] = a.comp_scale[6 * B.sa + i];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) cs1[i] = a.comp_scale[6 * B.sb + i];
+#pragma unroll
+        for (int i = 0; i < NC; ++i) cs2[i] = a.comp_scale[6 * K.sa + i];
+        double w = 8.0;
+        if (B.sa == B.sb) w *= 0.5;
+        if (K.sa == K.sb) w *= 0.5;
+        if (task.x == task.y) w *= 0.5;
+        double g[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) g[k] = 0.0;
+        W::contract(H, w, pab, pcd, pac, pbd, pad, pbc, cs0, cs1, cs2, g);
+        const int at[4] = {a.shell_atom[B.sa], a.shell_atom[B.sb], a.shell_atom[K.sa],
+                           a.shell_atom[K.sb]};
+        double* dst = shared_sum ? sg : a.grad;
+#pragma unroll
+        for (int cen = 0; cen < 3; ++cen)
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                atomicAdd(dst + 3 * at[cen] + x, g[3 * cen + x]);
+                atomicAdd(dst + 3 * at[3] + x, -g[3 * cen + x]);
+            }
+    }
+    if (shared_sum) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * a.natom; i += blockDim.x)
+            if (sg[i] != 0.0) atomicAdd(a.grad + i, sg[i]);
+    }
+}
+
+template <int LA, int LB, int LC, int LD>
+int launch_grad_thread(const GradArgs& a, cudaStream_t st) {
+    if (a.ntask <= 0) return 0;
+    const size_t sh = (a.natom > 0 && a.natom <= kGradSmemAtoms) ? 3 * sizeof(double) * a.natom : 0;
+    if (set_smem<k_eri_grad_thread<LA, LB, LC, LD>>(3 * sizeof(double) * kGradSmemAtoms))
+        return GS_ERR_CUDA;
+    k_eri_grad_thread<LA, LB, LC, LD><<<(a.ntask + kGradThreads - 1) / kGradThreads, kGradThreads,
+                                        sh, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 
 template <int LA, int LB, int LC, int LD>

@@ -248,17 +248,104 @@ def emit_grad(cls):
     return "\n".join(lines), p
 
 
+THREAD_LMAX = 3       # classes with la+lb+lc+ld <= this also get a thread-per-quartet form
+
+
+def emit_grad_thread(cls, p=None):
+    """Straight-line thread-per-quartet form of the same program: per primitive quartet the
+    VRR node program and the weighted accumulation into H[0 .. NACC), then the six HRR
+    sub-programs on H and the contraction with the density weights, all with
+    compile-time indices so that the node values and accumulators live in registers."""
+    p = p or grad_program(cls)
+    la, lb, lc, ld = cls
+    tag = "".join(map(str, cls))
+    L, nacc = p["L"], p["nacc"]
+    vr = p["vrec"]
+    body = []
+    # VRR: records of 8 words: out | nt << 16, then (cid << 16 | slot) per term
+    for r in range(len(vr) // 8):
+        w = vr[8 * r: 8 * r + 8]
+        out, nt = w[0] & 0xffff, w[0] >> 16
+        terms = [(x >> 16, x & 0xffff) for x in w[1:1 + nt]]
+        e = f"c[{terms[0][0]}] * n[{terms[0][1]}]"
+        for cid, sl in terms[1:]:
+            e = f"fma(c[{cid}], n[{sl}], {e})"
+        body.append(f"    n[{out}] = {e};")
+    acc = []
+    for k, (sl, kind, pos) in enumerate(zip(p["acc_slot"], p["acc_kind"], p["acc_pos"])):
+        if kind == 0:
+            acc.append(f"    H[{pos}] += n[{sl}];")
+        else:
+            acc.append(f"    H[{pos}] = fma(c[{31 + kind}], n[{sl}], H[{pos}]);")
+    hrr = [f"    H[{d}] = fma(dv[{dd}], H[{y}], H[{x}]);" for d, x, y, dd in p["hops"]]
+    # contraction: g[3 cen + x] += gamma_e s_cen (H[raised] - e_x H[lowered])
+    ls = [la, lb, lc, ld]
+    n = [ncart(x) for x in ls]
+    con = []
+    for ia in range(n[0]):
+        for ib in range(n[1]):
+            for ic in range(n[2]):
+                for idd in range(n[3]):
+                    idx = [ia, ib, ic, idd]
+                    con.append(f"    gam = w * (0.5 * pab[{ia * n[1] + ib}] * pcd[{ic * n[3] + idd}] - "
+                               f"0.125 * (pac[{ia * n[2] + ic}] * pbd[{ib * n[3] + idd}] + "
+                               f"pad[{ia * n[3] + idd}] * pbc[{ib * n[2] + ic}]));")
+                    for cen in range(3):
+                        ex = cart(ls[cen])[idx[cen]]
+                        con.append(f"    s = gam * cs{cen}[{idx[cen]}];")
+                        for x in range(3):
+                            up = list(ex)
+                            up[x] += 1
+                            ii = list(idx)
+                            nn = list(n)
+                            ii[cen] = cart(ls[cen] + 1).index(tuple(up))
+                            nn[cen] = ncart(ls[cen] + 1)
+                            e_up = ((ii[0] * nn[1] + ii[1]) * nn[2] + ii[2]) * nn[3] + ii[3]
+                            h_up = p["outs"][cen][e_up]
+                            term = f"H[{h_up}]"
+                            if ex[x] > 0:
+                                dn = list(ex)
+                                dn[x] -= 1
+                                jj = list(idx)
+                                mm = list(n)
+                                jj[cen] = cart(ls[cen] - 1).index(tuple(dn))
+                                mm[cen] = ncart(ls[cen] - 1)
+                                e_dn = ((jj[0] * mm[1] + jj[1]) * mm[2] + jj[2]) * mm[3] + jj[3]
+                                h_dn = p["outs"][3 + cen][e_dn]
+                                term = f"(H[{h_up}] - {ex[x]}.0 * H[{h_dn}])"
+                            con.append(f"    g[{3 * cen + x}] = fma(s, {term}, g[{3 * cen + x}]);")
+    lines = [f"// generated by gen_grad.py -- thread-per-quartet gradient code of class ({la}{lb}|{lc}{ld})",
+             "#pragma once", "namespace gs {",
+             f"template <> struct GradThread<{la}, {lb}, {lc}, {ld}> {{",
+             f"  static constexpr int L = {L}, NACC = {nacc}, NVSLOT = {p['nvslot']}, HSIZE = {p['hsize']};",
+             "  static __device__ __forceinline__ void prim(const double* __restrict__ c, double* n, double* H) {",
+             *body, *acc, "  }",
+             "  static __device__ __forceinline__ void hrr(double* H, const double* dv) {",
+             *hrr, "  }",
+             "  static __device__ __forceinline__ void contract(const double* H, double w, const double* pab,",
+             "      const double* pcd, const double* pac, const double* pbd, const double* pad,",
+             "      const double* pbc, const double* cs0, const double* cs1, const double* cs2, double* g) {",
+             "    double gam, s;", *con, "  }", "};", "}  // namespace gs", ""]
+    return "\n".join(lines)
+
+
 def main():
     out = sys.argv[1]
     lmax = int(sys.argv[2]) if len(sys.argv) > 2 else 1
     os.makedirs(out, exist_ok=True)
     classes = gen_eri.canonical_classes(lmax)
     for cls in classes:
-        code, _ = emit_grad(cls)
+        code, prog = emit_grad(cls)
         path = os.path.join(out, "eri_grad_%s.h" % "".join(map(str, cls)))
         if not os.path.exists(path) or open(path).read() != code:
             with open(path, "w") as f:
                 f.write(code)
+        if sum(cls) <= THREAD_LMAX:
+            code = emit_grad_thread(cls, prog)
+            path = os.path.join(out, "eri_gradt_%s.h" % "".join(map(str, cls)))
+            if not os.path.exists(path) or open(path).read() != code:
+                with open(path, "w") as f:
+                    f.write(code)
     lst = ("// generated by gen_grad.py\n#pragma once\n#define GS_FOR_EACH_GRAD(X) " +
            " ".join("X(%d, %d, %d, %d)" % c for c in classes) + "\n")
     path = os.path.join(out, "eri_grad_list.h")

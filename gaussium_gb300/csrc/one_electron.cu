@@ -8,6 +8,7 @@
 // (e|A(0)|0)^(m) from Boys values followed by horizontal transfer to (a|A|b).
 // One thread per shell pair (any order of l), all in FP64.
 #include <cuda_runtime.h>
+#include <climits>
 #include "eri_common.cuh"
 #include "gs_args.h"
 
@@ -232,6 +233,9 @@ __device__ double v_transfer(const double* th0, int ax, int ay, int az, int bx, 
 // S and T by translational invariance (d/dB = -d/dA), V per nucleus C with the operator
 // term d/dC = -(d/dA + d/dB).  Derivatives from raised (2 alpha, l+1) and lowered (l-1)
 // Cartesian components: d phi_a/dA_x = 2 alpha phi_{a+1x} - a_x phi_{a-1x}.
+// One thread per (shell pair, part): part < natom is the nuclear-attraction term of
+// nucleus `part`, part == natom the overlap and kinetic terms; neighbouring threads share
+// a pair, so a warp runs uniform primitive loops.
 __global__ void k_one_electron_grad(gs::ShellView sv, const double* __restrict__ comp_scale,
                                     const int* __restrict__ func_off,
                                     const int* __restrict__ shell_atom, int npairs,
@@ -240,9 +244,13 @@ __global__ void k_one_electron_grad(gs::ShellView sv, const double* __restrict__
                                     const double* __restrict__ atom_z,
                                     const double* __restrict__ P, const double* __restrict__ Wm,
                                     double* grad) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= npairs) return;
+    const int parts = natom + 1;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)npairs * parts) return;
+    const int t = (int)(tid / parts), part = (int)(tid % parts);
     const int sa = pair_shells[2 * t], sb = pair_shells[2 * t + 1];
+    const int atom_a = shell_atom[sa], atom_b = shell_atom[sb];
+    if ((unsigned)atom_a >= (unsigned)natom || (unsigned)atom_b >= (unsigned)natom) return;
     const int la = sv.l[sa], lb = sv.l[sb];
     const int na = ncart(la), nb = ncart(lb);
     const double* A = sv.centre + 3 * sa;
@@ -251,7 +259,7 @@ __global__ void k_one_electron_grad(gs::ShellView sv, const double* __restrict__
     const double ab2 = AB[0] * AB[0] + AB[1] * AB[1] + AB[2] * AB[2];
     const double f = sa == sb ? 1.0 : 2.0;
     const int fa = func_off[sa], fb = func_off[sb];
-    double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
+    double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
     const int L = la + lb + 1;
     for (int i = sv.prim_off[sa]; i < sv.prim_off[sa + 1]; ++i) {
         for (int j = sv.prim_off[sb]; j < sv.prim_off[sb + 1]; ++j) {
@@ -264,92 +272,22 @@ __global__ void k_one_electron_grad(gs::ShellView sv, const double* __restrict__
                 PA[d] = Pc[d] - A[d];
                 PB[d] = Pc[d] - B[d];
             }
-            // 1D overlaps, a <= la+1, b <= lb+2
-            double s1[3][kMaxL + 2][kMaxL + 3];
-            for (int d = 0; d < 3; ++d) {
-                s1[d][0][0] = 1.0;
-                for (int b = 1; b <= lb + 2; ++b)
-                    s1[d][0][b] = PB[d] * s1[d][0][b - 1] + (b > 1 ? (b - 1) * i2p * s1[d][0][b - 2] : 0.0);
-                for (int a = 1; a <= la + 1; ++a)
-                    for (int b = 0; b <= lb + 2; ++b) {
-                        double v = PA[d] * s1[d][a - 1][b];
-                        if (a > 1) v += (a - 1) * i2p * s1[d][a - 2][b];
-                        if (b > 0) v += b * i2p * s1[d][a - 1][b - 1];
-                        s1[d][a][b] = v;
-                    }
-            }
-            const double pref = Kab * ip * sqrt(ip) * 5.568327996831708;
-            for (int ia = 0; ia < na; ++ia) {
-                int ax, ay, az;
-                cart_of(la, ia, ax, ay, az);
-                const int a3[3] = {ax, ay, az};
-                for (int ib = 0; ib < nb; ++ib) {
-                    int bx, by, bz;
-                    cart_of(lb, ib, bx, by, bz);
-                    const int b3[3] = {bx, by, bz};
-                    const double sc = comp_scale[6 * sa + ia] * comp_scale[6 * sb + ib] * pref * f;
-                    const double Pab = P[(fa + ia) * nbf + fb + ib], Wab = Wm[(fa + ia) * nbf + fb + ib];
-                    // per-dimension overlap and kinetic factors for a shifted by -1, 0, +1
-                    double sx[3][3], tx[3][3];
-                    for (int d = 0; d < 3; ++d)
-                        for (int sft = -1; sft <= 1; ++sft) {
-                            const int a = a3[d] + sft, b = b3[d];
-                            if (a < 0) { sx[d][sft + 1] = tx[d][sft + 1] = 0.0; continue; }
-                            sx[d][sft + 1] = s1[d][a][b];
-                            tx[d][sft + 1] = be * (2 * b + 1) * s1[d][a][b] - 2.0 * be * be * s1[d][a][b + 2] -
-                                             (b >= 2 ? 0.5 * b * (b - 1) * s1[d][a][b - 2] : 0.0);
+            if (part == natom) {
+                // 1D overlaps, a <= la+1, b <= lb+2
+                double s1[3][kMaxL + 2][kMaxL + 3];
+                for (int d = 0; d < 3; ++d) {
+                    s1[d][0][0] = 1.0;
+                    for (int b = 1; b <= lb + 2; ++b)
+                        s1[d][0][b] = PB[d] * s1[d][0][b - 1] + (b > 1 ? (b - 1) * i2p * s1[d][0][b - 2] : 0.0);
+                    for (int a = 1; a <= la + 1; ++a)
+                        for (int b = 0; b <= lb + 2; ++b) {
+                            double v = PA[d] * s1[d][a - 1][b];
+                            if (a > 1) v += (a - 1) * i2p * s1[d][a - 2][b];
+                            if (b > 0) v += b * i2p * s1[d][a - 1][b - 1];
+                            s1[d][a][b] = v;
                         }
-                    for (int x = 0; x < 3; ++x) {
-                        const int y = (x + 1) % 3, z = (x + 2) % 3;
-                        // d/dA_x of S and T
-                        const double dsx = 2.0 * al * sx[x][2] - a3[x] * sx[x][0];
-                        const double dtx = 2.0 * al * tx[x][2] - a3[x] * tx[x][0];
-                        const double dS = dsx * sx[y][1] * sx[z][1];
-                        const double dT = dtx * sx[y][1] * sx[z][1] + dsx * (tx[y][1] * sx[z][1] + sx[y][1] * tx[z][1]);
-                        const double gx = sc * (Pab * dT - Wab * dS);
-                        gA[x] += gx;
-                        gB[x] -= gx;
-                    }
                 }
-            }
-            // nuclear attraction
-            const double vpref = Kab * ip * 6.283185307179586;
-            for (int c = 0; c < natom; ++c) {
-                const double* C = atom_xyz + 3 * c;
-                const double PC[3] = {Pc[0] - C[0], Pc[1] - C[1], Pc[2] - C[2]};
-                const double u = p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]);
-                double F[2 * kMaxL + 2];
-                switch (L) {
-                    case 1: gs::boys<1, double>(u, 1.0, F); break;
-                    case 2: gs::boys<2, double>(u, 1.0, F); break;
-                    case 3: gs::boys<3, double>(u, 1.0, F); break;
-                    case 4: gs::boys<4, double>(u, 1.0, F); break;
-                    default: gs::boys<5, double>(u, 1.0, F); break;
-                }
-                double th[2 * kMaxL + 2][56];
-                for (int m = 0; m <= L; ++m) th[m][0] = F[m];
-                for (int Le = 1; Le <= L; ++Le)
-                    for (int k = 0; k < ncart(Le); ++k) {
-                        int e[3];
-                        cart_of(Le, k, e[0], e[1], e[2]);
-                        const int d = e[0] ? 0 : (e[1] ? 1 : 2);
-                        int e1[3] = {e[0], e[1], e[2]};
-                        e1[d] -= 1;
-                        const int i1 = lbase(Le - 1) + cart_index(e1[0], e1[1], e1[2]);
-                        int i2 = -1;
-                        if (e1[d] > 0) {
-                            int e2[3] = {e1[0], e1[1], e1[2]};
-                            e2[d] -= 1;
-                            i2 = lbase(Le - 2) + cart_index(e2[0], e2[1], e2[2]);
-                        }
-                        for (int m = 0; m <= L - Le; ++m) {
-                            double v = PA[d] * th[m][i1] - PC[d] * th[m + 1][i1];
-                            if (i2 >= 0) v += e1[d] * i2p * (th[m][i2] - th[m + 1][i2]);
-                            th[m][lbase(Le) + k] = v;
-                        }
-                    }
-                const double zc = atom_z[c];
-                double gC[3] = {0, 0, 0};
+                const double pref = Kab * ip * sqrt(ip) * 5.568327996831708;
                 for (int ia = 0; ia < na; ++ia) {
                     int ax, ay, az;
                     cart_of(la, ia, ax, ay, az);
@@ -358,31 +296,99 @@ __global__ void k_one_electron_grad(gs::ShellView sv, const double* __restrict__
                         int bx, by, bz;
                         cart_of(lb, ib, bx, by, bz);
                         const int b3[3] = {bx, by, bz};
-                        const double w = -zc * vpref * f * comp_scale[6 * sa + ia] *
-                                         comp_scale[6 * sb + ib] * P[(fa + ia) * nbf + fb + ib];
+                        const double sc = comp_scale[6 * sa + ia] * comp_scale[6 * sb + ib] * pref * f;
+                        const double Pab = P[(fa + ia) * nbf + fb + ib], Wab = Wm[(fa + ia) * nbf + fb + ib];
+                        // per-dimension overlap and kinetic factors for a shifted by -1, 0, +1
+                        double sx[3][3], tx[3][3];
+                        for (int d = 0; d < 3; ++d)
+                            for (int sft = -1; sft <= 1; ++sft) {
+                                const int a = a3[d] + sft, b = b3[d];
+                                if (a < 0) { sx[d][sft + 1] = tx[d][sft + 1] = 0.0; continue; }
+                                sx[d][sft + 1] = s1[d][a][b];
+                                tx[d][sft + 1] = be * (2 * b + 1) * s1[d][a][b] - 2.0 * be * be * s1[d][a][b + 2] -
+                                                 (b >= 2 ? 0.5 * b * (b - 1) * s1[d][a][b - 2] : 0.0);
+                            }
                         for (int x = 0; x < 3; ++x) {
-                            int ap[3] = {a3[0], a3[1], a3[2]}, am[3] = {a3[0], a3[1], a3[2]};
-                            int bp[3] = {b3[0], b3[1], b3[2]}, bm[3] = {b3[0], b3[1], b3[2]};
-                            ap[x] += 1; am[x] -= 1; bp[x] += 1; bm[x] -= 1;
-                            double dA = 2.0 * al * v_transfer(th[0], ap[0], ap[1], ap[2], b3[0], b3[1], b3[2], AB);
-                            if (a3[x] > 0) dA -= a3[x] * v_transfer(th[0], am[0], am[1], am[2], b3[0], b3[1], b3[2], AB);
-                            double dB = 2.0 * be * v_transfer(th[0], a3[0], a3[1], a3[2], bp[0], bp[1], bp[2], AB);
-                            if (b3[x] > 0) dB -= b3[x] * v_transfer(th[0], a3[0], a3[1], a3[2], bm[0], bm[1], bm[2], AB);
-                            gA[x] += w * dA;
-                            gB[x] += w * dB;
-                            gC[x] -= w * (dA + dB);
+                            const int y = (x + 1) % 3, z = (x + 2) % 3;
+                            // d/dA_x of S and T
+                            const double dsx = 2.0 * al * sx[x][2] - a3[x] * sx[x][0];
+                            const double dtx = 2.0 * al * tx[x][2] - a3[x] * tx[x][0];
+                            const double dS = dsx * sx[y][1] * sx[z][1];
+                            const double dT = dtx * sx[y][1] * sx[z][1] + dsx * (tx[y][1] * sx[z][1] + sx[y][1] * tx[z][1]);
+                            const double gx = sc * (Pab * dT - Wab * dS);
+                            gA[x] += gx;
+                            gB[x] -= gx;
                         }
                     }
                 }
-                for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * c + x, gC[x]);
+                continue;
+            }
+            // nuclear attraction of nucleus `part`
+            const double vpref = Kab * ip * 6.283185307179586;
+            const double* C = atom_xyz + 3 * part;
+            const double PC[3] = {Pc[0] - C[0], Pc[1] - C[1], Pc[2] - C[2]};
+            const double u = p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]);
+            double F[2 * kMaxL + 2];
+            switch (L) {
+                case 1: gs::boys<1, double>(u, 1.0, F); break;
+                case 2: gs::boys<2, double>(u, 1.0, F); break;
+                case 3: gs::boys<3, double>(u, 1.0, F); break;
+                case 4: gs::boys<4, double>(u, 1.0, F); break;
+                default: gs::boys<5, double>(u, 1.0, F); break;
+            }
+            double th[2 * kMaxL + 2][56];
+            for (int m = 0; m <= L; ++m) th[m][0] = F[m];
+            for (int Le = 1; Le <= L; ++Le)
+                for (int k = 0; k < ncart(Le); ++k) {
+                    int e[3];
+                    cart_of(Le, k, e[0], e[1], e[2]);
+                    const int d = e[0] ? 0 : (e[1] ? 1 : 2);
+                    int e1[3] = {e[0], e[1], e[2]};
+                    e1[d] -= 1;
+                    const int i1 = lbase(Le - 1) + cart_index(e1[0], e1[1], e1[2]);
+                    int i2 = -1;
+                    if (e1[d] > 0) {
+                        int e2[3] = {e1[0], e1[1], e1[2]};
+                        e2[d] -= 1;
+                        i2 = lbase(Le - 2) + cart_index(e2[0], e2[1], e2[2]);
+                    }
+                    for (int m = 0; m <= L - Le; ++m) {
+                        double v = PA[d] * th[m][i1] - PC[d] * th[m + 1][i1];
+                        if (i2 >= 0) v += e1[d] * i2p * (th[m][i2] - th[m + 1][i2]);
+                        th[m][lbase(Le) + k] = v;
+                    }
+                }
+            const double zc = atom_z[part];
+            for (int ia = 0; ia < na; ++ia) {
+                int ax, ay, az;
+                cart_of(la, ia, ax, ay, az);
+                const int a3[3] = {ax, ay, az};
+                for (int ib = 0; ib < nb; ++ib) {
+                    int bx, by, bz;
+                    cart_of(lb, ib, bx, by, bz);
+                    const int b3[3] = {bx, by, bz};
+                    const double w = -zc * vpref * f * comp_scale[6 * sa + ia] *
+                                     comp_scale[6 * sb + ib] * P[(fa + ia) * nbf + fb + ib];
+                    for (int x = 0; x < 3; ++x) {
+                        int ap[3] = {a3[0], a3[1], a3[2]}, am[3] = {a3[0], a3[1], a3[2]};
+                        int bp[3] = {b3[0], b3[1], b3[2]}, bm[3] = {b3[0], b3[1], b3[2]};
+                        ap[x] += 1; am[x] -= 1; bp[x] += 1; bm[x] -= 1;
+                        double dA = 2.0 * al * v_transfer(th[0], ap[0], ap[1], ap[2], b3[0], b3[1], b3[2], AB);
+                        if (a3[x] > 0) dA -= a3[x] * v_transfer(th[0], am[0], am[1], am[2], b3[0], b3[1], b3[2], AB);
+                        double dB = 2.0 * be * v_transfer(th[0], a3[0], a3[1], a3[2], bp[0], bp[1], bp[2], AB);
+                        if (b3[x] > 0) dB -= b3[x] * v_transfer(th[0], a3[0], a3[1], a3[2], bm[0], bm[1], bm[2], AB);
+                        gA[x] += w * dA;
+                        gB[x] += w * dB;
+                        gC[x] -= w * (dA + dB);
+                    }
+                }
             }
         }
     }
-    const int atom_a = shell_atom[sa], atom_b = shell_atom[sb];
-    if ((unsigned)atom_a >= (unsigned)natom || (unsigned)atom_b >= (unsigned)natom) return;
     for (int x = 0; x < 3; ++x) {
         atomicAdd(grad + 3 * atom_a + x, gA[x]);
         atomicAdd(grad + 3 * atom_b + x, gB[x]);
+        if (part < natom) atomicAdd(grad + 3 * part + x, gC[x]);
     }
 }
 
@@ -416,7 +422,9 @@ extern "C" int gs_one_electron_grad(const double* centre, const int* l, const in
         return GS_ERR_ARG;
     if (npairs == 0) return GS_OK;
     gs::ShellView sv{centre, l, prim_off, expo, coef};
-    k_one_electron_grad<<<(npairs + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
+    const long long nthr = (long long)npairs * (natom + 1);
+    if (nthr > (long long)INT_MAX * 64) return GS_ERR_ARG;
+    k_one_electron_grad<<<(unsigned)((nthr + 63) / 64), 64, 0, (cudaStream_t)stream>>>(
         sv, comp_scale, func_off, shell_atom, npairs, pair_shells, nbf, natom, atom_xyz, atom_z,
         density, energy_weighted, grad);
     return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA;

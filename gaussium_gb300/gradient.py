@@ -117,6 +117,16 @@ def one_electron_gradient(sb, mol, shell_atom, P, W):
     return g
 
 
+def tune_eri_gradient(sb, engine: JKEngine, shell_atom, P, natom, reps=3):
+    """Choose the kernel form (thread or warp per quartet) of every gradient class on this
+    engine's task lists (gaussium_gb300.autotune)."""
+    from . import autotune
+    return autotune.tune_gradient(
+        engine.segments,
+        lambda cls: eri_gradient(sb, engine, shell_atom, P, natom, classes=[cls], host=False),
+        reps)
+
+
 def one_electron_gradient_kernel(sb, mol, shell_atom, P, W, device="cuda"):
     """The one-electron gradient terms in one launch (gs_one_electron_grad)."""
     ds = DeviceShells(sb, device)
@@ -156,9 +166,10 @@ def _check_atoms(shell_atom, natom):
         raise ValueError("shell_atom holds an atom index outside [0, natom)")
 
 
-def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom):
+def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom, classes=None, host=True):
     """Two-electron gradient through the fused adjoint kernel (gs_eri_grad), one launch per
-    class over the engine's Schwarz-screened unique quartets."""
+    class over the engine's Schwarz-screened unique quartets (``classes``: only those).
+    Returns natom x 3 (host numpy, or the device tensor with ``host=False``)."""
     _check_atoms(shell_atom, natom)
     if np.any(sb.l >= 2):
         raise NotImplementedError("the fused gradient kernels cover s/p shells")
@@ -169,11 +180,13 @@ def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom):
     L = _lib.lib()
     base = engine.tasks.data_ptr()
     for cls, s, e in engine.segments:
+        if classes is not None and cls not in classes:
+            continue
         _lib.check(L.gs_eri_grad(*cls, _lib.ptr(engine.pairs.rec), _lib.ptr(engine.pairs.p64),
                                  _lib.ptr(engine.ds.comp_scale), _lib.ptr(engine.ds.func_off),
-                                 _lib.ptr(sa), e - s, base + s * 8, sb.nbf, _lib.ptr(pt),
+                                 _lib.ptr(sa), e - s, base + s * 8, sb.nbf, natom, _lib.ptr(pt),
                                  _lib.ptr(grad), _lib.stream()), f"gs_eri_grad{cls}")
-    return grad.view(natom, 3).cpu().numpy()
+    return grad.view(natom, 3).cpu().numpy() if host else grad.view(natom, 3)
 
 
 def eri_gradient_blocks(sb, engine: JKEngine, shell_atom, P, natom):

@@ -207,11 +207,22 @@ int gs_eri_grad_contract(int nq, const int* quartets, const long long* block_off
  * centres A, B, C in one pass (VRR per primitive quartet into four weighted contraction
  * sets 1, 2 alpha, 2 beta, 2 gamma; six HRR blocks in shared memory), contracts them with
  * the same RHF weights as gs_eri_grad_contract and adds dE/dR to grad[natom*3] through
- * shell_atom[].  prim64 records must carry the first shell's exponent in their pad field
+ * shell_atom[] (every entry in [0, natom)).  prim64 records must carry the first shell's exponent in their pad field
  * (gs_pairs_build writes it).  No reference counterpart (see gs_eri_grad_contract). */
 int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
                 const double* comp_scale, const int* func_off, const int* shell_atom, int ntask,
-                const int* tasks, int nbf, const double* density, double* grad, void* stream);
+                const int* tasks, int nbf, int natom, const double* density, double* grad,
+                void* stream);
+
+/* Kernel forms built for gradient class (la lb|lc ld): bit 0 one thread per quartet
+ * (classes of total angular momentum <= 3), bit 1 one warp per quartet; negative status
+ * for a class without gradient kernels.  No reference counterpart. */
+int gs_eri_grad_variants(int la, int lb, int lc, int ld);
+
+/* Chooses the form later gs_eri_grad calls use for that class, process-wide: 0 = default
+ * (thread per quartet up to total angular momentum 2, warp above), 1 = thread, 2 = warp.
+ * No reference counterpart. */
+int gs_set_eri_grad_variant(int la, int lb, int lc, int ld, int variant);
 
 /* One-electron part of the RHF gradient: for npairs unique shell pairs (a >= b) adds
  *   f sum_ij [P_ij (dT_ij + dV_ij) - W_ij dS_ij]   (f = 2 for a != b, 1 for a == b)

@@ -101,3 +101,91 @@ def test_grad_program_blocks(cls):
         inv = np.argsort(canon)                 # canonical position of original shell k
         ref = blk.transpose(inv).ravel()
         assert np.max(np.abs(outs[which] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), which
+
+
+def _body(code, fn):
+    """Statements of a generated thread-code function, as Python (they are plain
+    assignments over arrays with fma)."""
+    text = code.split(f"void {fn}(")[1]
+    text = text[text.index("{") + 1:]
+    out = []
+    for ln in text.split("\n")[1:]:
+        if ln.startswith("  }"):
+            break
+        ln = ln.strip()
+        if ln and not ln.startswith("double "):
+            out.append(ln.rstrip(";"))
+    return compile("\n".join(out), fn, "exec")
+
+
+def _fma(a, b, c):
+    return a * b + c
+
+
+@pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(1) if sum(c) <= gen_grad.THREAD_LMAX])
+def test_thread_gradient_code_matches_program(cls):
+    rng = np.random.default_rng(sum(cls) + 29)
+    cents = rng.uniform(-1.0, 1.0, size=(4, 3))
+    shells = [_shell(rng, l, int(rng.integers(1, 3)), cents[i]) for i, l in enumerate(cls)]
+    sb = ShellBasis.from_shell_dicts(shells)
+    pr, pd, _ = hostcheck.make_pairs(sb, [(0, 1), (2, 3)])
+    pd[:, 9] = [sb.expo[sb.prim_off[0] + i // sb.nprim[1]] for i in range(sb.nprim[0] * sb.nprim[1])] + \
+        [sb.expo[sb.prim_off[2] + i // sb.nprim[3]] for i in range(sb.nprim[2] * sb.nprim[3])]
+    outs = emulate(cls, pr, pd, None, None)
+    p = gen_grad.grad_program(cls)
+    code = gen_grad.emit_grad_thread(cls, p)
+    prim, hrr, contract = _body(code, "prim"), _body(code, "hrr"), _body(code, "contract")
+    L = p["L"]
+    B, K = pr[0], pr[1]
+    H = np.zeros(p["hsize"])
+    for i in range(B["nprim"]):
+        P = pd[B["prim_off"] + i]
+        for j in range(K["nprim"]):
+            Q = pd[K["prim_off"] + j]
+            pq = P[0] + Q[0]
+            PQ = Q[2:5] - P[2:5]
+            wq, wp = Q[0] / pq, P[0] / pq
+            t = P[0] * wq * PQ @ PQ
+            c = np.zeros(36)
+            c[0:3] = P[5:8]; c[3:6] = wq * PQ; c[6:9] = Q[5:8]; c[9:12] = -wp * PQ
+            for k in range(1, 5):
+                c[11 + k] = k * P[1]; c[15 + k] = -k * wq * P[1]; c[19 + k] = k * Q[1]
+                c[23 + k] = -k * wp * Q[1]; c[27 + k] = k * 0.5 / pq
+            c[32], c[33], c[34] = 2 * P[9], 2 * (P[0] - P[9]), 2 * Q[9]
+            n = np.zeros(p["nvslot"])
+            n[:L + 1] = np.array([oracle.boys_exact(m, t) for m in range(L + 1)]) * P[8] * Q[8] / np.sqrt(pq)
+            exec(prim, {"fma": _fma, "c": c, "n": n, "H": H})
+    exec(hrr, {"fma": _fma, "H": H, "dv": [*B["AB"], *K["AB"]]})
+    for which, o in enumerate(p["outs"]):
+        if o is not None:
+            assert np.max(np.abs(H[np.array(o)] - outs[which])) <= 1e-13 * max(1.0, np.max(np.abs(outs[which])))
+    # contraction against a direct loop over the blocks
+    nc = [gen_eri.ncart(x) for x in cls]
+    dens = {k: rng.standard_normal(nc[a] * nc[b]) for k, (a, b) in
+            {"pab": (0, 1), "pcd": (2, 3), "pac": (0, 2), "pbd": (1, 3), "pad": (0, 3), "pbc": (1, 2)}.items()}
+    cs = [rng.uniform(0.5, 2.0, nc[k]) for k in range(3)]
+    g = np.zeros(9)
+    exec(contract, {"fma": _fma, "H": H, "w": 0.5, **dens, "cs0": cs[0], "cs1": cs[1], "cs2": cs[2], "g": g})
+    ref = np.zeros(9)
+    for ia in range(nc[0]):
+        for ib in range(nc[1]):
+            for ic in range(nc[2]):
+                for idd in range(nc[3]):
+                    idx = [ia, ib, ic, idd]
+                    gam = 0.5 * (0.5 * dens["pab"][ia * nc[1] + ib] * dens["pcd"][ic * nc[3] + idd] -
+                                 0.125 * (dens["pac"][ia * nc[2] + ic] * dens["pbd"][ib * nc[3] + idd] +
+                                          dens["pad"][ia * nc[3] + idd] * dens["pbc"][ib * nc[2] + ic]))
+                    for cen in range(3):
+                        ex = gen_eri.cart(cls[cen])[idx[cen]]
+                        for x in range(3):
+                            up = list(ex); up[x] += 1
+                            ii = list(idx); nn = list(nc)
+                            ii[cen] = gen_eri.cart(cls[cen] + 1).index(tuple(up)); nn[cen] = gen_eri.ncart(cls[cen] + 1)
+                            v = outs[cen][((ii[0] * nn[1] + ii[1]) * nn[2] + ii[2]) * nn[3] + ii[3]]
+                            if ex[x] > 0:
+                                dn = list(ex); dn[x] -= 1
+                                jj = list(idx); mm = list(nc)
+                                jj[cen] = gen_eri.cart(cls[cen] - 1).index(tuple(dn)); mm[cen] = gen_eri.ncart(cls[cen] - 1)
+                                v -= ex[x] * outs[3 + cen][((jj[0] * mm[1] + jj[1]) * mm[2] + jj[2]) * mm[3] + jj[3]]
+                            ref[3 * cen + x] += gam * cs[cen][idx[cen]] * v
+    assert np.max(np.abs(g - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))

@@ -45,8 +45,10 @@ def test_autograd_function(gpu_lib):
     assert np.allclose(c.grad.numpy(), g, atol=1e-12)
 
 
-def test_fused_adjoint_matches_block_path(gpu_lib):
-    from gaussium_gb300 import gradient, molecules
+@pytest.mark.parametrize("form", [0, 1, 2])
+def test_fused_adjoint_matches_block_path(gpu_lib, form):
+    """Default forms, every class with a thread form on threads, every class on warps."""
+    from gaussium_gb300 import autotune, build, gradient, molecules
     from gaussium_gb300.engine import JKEngine
     mol = molecules.water_cluster(2, seed=9)
     sb = molecules.shell_basis(mol, "6-31G")
@@ -55,7 +57,14 @@ def test_fused_adjoint_matches_block_path(gpu_lib):
     a = rng.standard_normal((sb.nbf, sb.nbf))
     P = (a + a.T) / 8
     sa = gradient.shell_atoms(mol, sb)
-    g1 = gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
+    classes = [c for c in build.classes() if max(c) <= 1]
+    try:
+        for c in classes:
+            autotune.set_grad_form(c, form if form in autotune.grad_forms(c) else 0)
+        g1 = gradient.eri_gradient(sb, eng, sa, P, len(mol.symbols))
+    finally:
+        for c in classes:
+            autotune.set_grad_form(c, 0)
     g2 = gradient.eri_gradient_blocks(sb, eng, sa, P, len(mol.symbols))
     assert np.max(np.abs(g1 - g2)) < 1e-10
 
