@@ -248,9 +248,10 @@ GS_HD GS_INLINE PrimRec<float> prim_pair32(const PrimRec<double>& r) {
 }
 
 // Primitive-pair screen: drop the pair when its Gaussian-product factor exp(-ab/p |AB|^2)
-// is below exp(-max_exp) (max_exp > 0).
+// is below exp(-max_exp) (max_exp > 0).  Written without the division (ab |AB|^2 >
+// max_exp p), which on this part costs more FP64 issue slots than the rest of the test.
 GS_HD GS_INLINE bool prim_pair_kept(double a, double b, double ab2, double max_exp) {
-    return !(max_exp > 0.0 && a * b * (1.0 / (a + b)) * ab2 > max_exp);
+    return !(max_exp > 0.0 && a * b * ab2 > max_exp * (a + b));
 }
 
 // Fill the PairRec and the primitive-pair records of shell pair (sa, sb); la >= lb.

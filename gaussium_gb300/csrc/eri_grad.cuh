@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
     const int* __restrict__ vseg = W::vseg();
     for (int base = 0; base < ntot; base += kSetupBatch) {
         const int i = base + lane;
-        if (i < ntot) {
+        if (lane < kSetupBatch && i < ntot) {
             const PrimRec<double> P = a.prims[B.prim_off + i / nK];
             const PrimRec<double> Q = a.prims[K.prim_off + i % nK];
             double* c = sC + lane * kNCoefG;

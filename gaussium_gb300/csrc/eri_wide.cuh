@@ -19,9 +19,17 @@ namespace gs {
 
 template <int LA, int LB, int LC, int LD> struct WideProg;
 
-constexpr int kWideWarps = 2;     // warps per block
-constexpr int kNCoef = 32;        // coefficient slots per primitive quartet
-constexpr int kSetupBatch = 32;   // primitive quartets prepared per setup round
+#ifndef GS_WIDE_WARPS
+#define GS_WIDE_WARPS 2
+#endif
+#ifndef GS_SETUP_BATCH
+#define GS_SETUP_BATCH 32
+#endif
+constexpr int kWideWarps = GS_WIDE_WARPS;     // warps per block
+constexpr int kNCoef = 32;                    // coefficient slots per primitive quartet
+constexpr int kSetupBatch = GS_SETUP_BATCH;   // primitive quartets prepared per setup round
+static_assert(kSetupBatch >= 1 && kSetupBatch <= 32, "one primitive quartet per lane at most");
+static_assert(kWideWarps >= 1 && kWideWarps <= 32, "warps per block");
 
 template <int LA, int LB, int LC, int LD, typename T> struct WideLayout {
     using G = ClassGen<LA, LB, LC, LD>;
@@ -96,7 +104,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     const unsigned short* __restrict__ vtgt = W::vtgt();
     for (int base = 0; base < ntot; base += kSetupBatch) {
         const int i = base + lane;
-        if (i < ntot) {
+        if (lane < kSetupBatch && i < ntot) {
             const PrimRec<T> P = prims[B.prim_off + i / nK];
             const PrimRec<T> Q = prims[K.prim_off + i % nK];
             wide_setup_m<L, T>(P, Q, sC + lane * kNCoef, sF + lane * (L + 1));
