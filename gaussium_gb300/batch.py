@@ -192,9 +192,17 @@ class BatchedRHF:
             self._graphs[key] = (P_static, g, G_static)
         state = {"n": 0, "P": None, "G": None}
 
-        def two_electron(Pb):
+        def two_electron(Pb, active):
+            # incremental: G(P_ref) + G(P - P_ref); a full build (first, and every
+            # reset_every-th) evaluates only the molecules still iterating
             inc = incremental and state["P"] is not None and state["n"] % reset_every != 0
-            P_static.copy_(self.to_packed(Pb - state["P"] if inc else Pb))
+            if inc:
+                Pin = Pb - state["P"]
+            elif state["G"] is not None:
+                Pin = torch.where(active[:, None, None], Pb, torch.zeros_like(Pb))
+            else:
+                Pin = Pb
+            P_static.copy_(self.to_packed(Pin))
             if use_graph:
                 g.replay()
                 G = G_static.clone()
@@ -202,6 +210,8 @@ class BatchedRHF:
                 G = build()
             if inc:
                 G = G + state["G"]
+            elif state["G"] is not None:
+                G = torch.where(active[:, None, None], G, state["G"])
             state.update(n=state["n"] + 1, P=Pb.clone(), G=G)
             return G
 
@@ -289,18 +299,24 @@ def padded_system(S_list, H_list, nocc, device):
 
 
 def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold=1e-10,
-                           max_iter=60, diis_subspace=8):
+                           max_iter=60, diis_subspace=8, level_shift=0.5, shift_after=15,
+                           shifted_error=1e-5):
     """Restricted SCF of B molecules at once over zero-padded [B, N, N] FP64 matrices.
 
-    ``two_electron(P)`` returns G = J - K/2 for the padded densities.  Per molecule: the
-    core-Hamiltonian guess, canonical orthogonaliser ``X`` (zero columns for padded
-    orbitals, which ``pad_orb`` lifts to the top of the spectrum), Pulay DIIS on the
+    ``two_electron(P, active)`` returns G = J - K/2 for the padded densities; ``active``
+    flags the molecules still iterating (the others' densities no longer change).  Per
+    molecule: the core-Hamiltonian guess, canonical orthogonaliser ``X`` (zero columns for
+    padded orbitals, which ``pad_orb`` lifts to the top of the spectrum), Pulay DIIS on the
     orthogonalised commutator SPF - FPS, and the reference's stopping rule |dE| <
     threshold (hartreefock/scf_procedure.py:24-42).  A molecule that has converged keeps
     its density (its energy is final) while the others iterate; the DIIS matrix of each
-    molecule is scaled by its largest diagonal element so that a nearly converged
-    molecule does not make the batched solve singular.  Returns the electronic energies,
-    the iteration count, the per-molecule converged flags and the last densities."""
+    molecule is scaled by its largest diagonal element so that a nearly converged molecule
+    does not make the batched solve singular.  A molecule still iterating after
+    ``shift_after`` iterations gets a level shift of its virtual orbitals,
+    F + level_shift (S - S P S / 2) (the converged density is unchanged by it), and must then
+    also bring its largest commutator element below ``shifted_error`` to stop, since the
+    shift slows the energy change.  Returns the electronic energies, the iteration count,
+    the per-molecule converged flags and the last densities."""
     dev = Hb.device
     B = Hb.shape[0]
     big = 1e6 * pad_orb
@@ -313,22 +329,25 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
     _, C = diag(Hb)
     prev = torch.zeros(B, dtype=torch.float64, device=dev)
     done = torch.zeros(B, dtype=torch.bool, device=dev)
+    shifted = torch.zeros(B, dtype=torch.bool, device=dev)
     hist_f, hist_e = [], []
     energies = None
     it = 0
     for it in range(1, max_iter + 1):
         Cocc = C * occ_mask[:, None, :]
         Pb = 2.0 * Cocc @ Cocc.transpose(1, 2)
-        F = Hb + two_electron(Pb)
+        F = Hb + two_electron(Pb, ~done)
         e_now = 0.5 * torch.sum(Pb * (Hb + F), dim=(1, 2))
         energies = e_now if energies is None else torch.where(done, energies, e_now)
+        err = Sb @ Pb @ F - F @ Pb @ Sb
+        err = X.transpose(1, 2) @ err @ X
         if it > 1:
-            done = done | ((e_now - prev).abs() < threshold)
+            small = (e_now - prev).abs() < threshold
+            small &= ~shifted | (err.abs().amax(dim=(1, 2)) < shifted_error)
+            done = done | small
         prev = e_now
         if bool(done.all()):
             break
-        err = Sb @ Pb @ F - F @ Pb @ Sb
-        err = X.transpose(1, 2) @ err @ X
         hist_f.append(F)
         hist_e.append(err)
         if len(hist_f) > diis_subspace:
@@ -348,6 +367,10 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
             rhs[:, k] = 1
             c = torch.linalg.solve(Bm, rhs)[:, :k]
             F = torch.einsum("bk,bkij->bij", c, torch.stack(hist_f, 1))
+        if level_shift > 0 and it >= shift_after:
+            shifted = ~done
+            sigma = level_shift * shifted.double()
+            F = F + sigma[:, None, None] * (Sb - 0.5 * Sb @ Pb @ Sb)
         _, C_new = diag(F)
         C = torch.where(done[:, None, None], C, C_new)
     return energies, it, done.cpu().numpy(), Pb

@@ -48,7 +48,7 @@ def test_batched_loop_matches_single_loop(systems):
                                         [s[3] // 2 for s in systems], "cpu")
     N = Sb.shape[1]
 
-    def two_electron(Pb):
+    def two_electron(Pb, active=None):
         out = torch.zeros_like(Pb)
         for m, (S, H, eri, ne) in enumerate(systems):
             n = S.shape[0]
@@ -68,7 +68,7 @@ def test_reference_energy_of_water_sto3g_through_batched_loop(systems):
     S, H, eri, ne = systems[0]
     g = golden("h2o_sto3g")
     Sb, Hb, X, occ, pad = padded_system([S], [H], [ne // 2], "cpu")
-    two = lambda Pb: torch.as_tensor(oracle.fock_restricted(np.zeros_like(H), eri,
+    two = lambda Pb, active=None: torch.as_tensor(oracle.fock_restricted(np.zeros_like(H), eri,
                                                             Pb[0].numpy()))[None]
     e, it, done, _ = batched_rhf_iterations(Sb, Hb, X, occ, pad, two, threshold=1e-12)
     e_nuc = scf.nuclear_repulsion(g["charges"], g["coords"])
@@ -110,3 +110,25 @@ def test_batched_task_list_matches_loops():
     segs_ref, tasks_ref = _task_list_loops(q, pc, pair_mol, nprim, 1e-9, 6)
     assert segs == segs_ref
     assert np.array_equal(tasks.numpy(), tasks_ref)
+
+
+def test_level_shifted_loop_reaches_the_same_energies(systems):
+    """With the level shift switched on from the second iteration the loop converges to
+    the same energies (the shift changes the path, not the fixed point)."""
+    single = [scf.restricted_scf(S, H, ne, _OracleFock(H, eri), threshold=1e-12).energy
+              for S, H, eri, ne in systems]
+    Sb, Hb, X, occ, pad = padded_system([s[0] for s in systems], [s[1] for s in systems],
+                                        [s[3] // 2 for s in systems], "cpu")
+
+    def two_electron(Pb, active=None):
+        out = torch.zeros_like(Pb)
+        for m, (S, H, eri, ne) in enumerate(systems):
+            n = S.shape[0]
+            out[m, :n, :n] = torch.as_tensor(oracle.fock_restricted(np.zeros_like(H), eri,
+                                                                    Pb[m, :n, :n].numpy()))
+        return out
+
+    e, it, done, _ = batched_rhf_iterations(Sb, Hb, X, occ, pad, two_electron, threshold=1e-12,
+                                            max_iter=200, shift_after=2)
+    assert done.all()
+    assert np.max(np.abs(e.numpy() - np.array(single))) < 1e-9
