@@ -299,7 +299,7 @@ def padded_system(S_list, H_list, nocc, device):
 
 
 def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold=1e-10,
-                           max_iter=60, diis_subspace=8, level_shift=0.5, shift_after=15,
+                           max_iter=60, diis_subspace=8, level_shift=0.3, shift_after=30,
                            shifted_error=1e-5):
     """Restricted SCF of B molecules at once over zero-padded [B, N, N] FP64 matrices.
 

@@ -92,7 +92,7 @@ def generate():
         else:
             # no warp program: the warp kernels are never selected below WIDE_PROG_MIN
             inc = ('#include "eri_class_%s.h"\nnamespace gs { template <> struct WideProg<%d, %d, %d, %d> '
-                   '{ static constexpr int NVSLOT = 1, NVSEG = 0, HSIZE = 1, NHLEV = 0; '
+                   '{ static constexpr int NVSLOT = 1, NVSEG = 0, VGROUP = 1, HSIZE = 1, NHLEV = 0; '
                    'static __device__ const uint4* vrec() { return nullptr; } '
                    'static __device__ const int* vseg() { return nullptr; } '
                    'static __device__ const unsigned short* vtgt() { return nullptr; } '

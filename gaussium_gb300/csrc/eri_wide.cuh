@@ -30,13 +30,22 @@ constexpr int kNCoef = 32;                    // coefficient slots per primitive
 constexpr int kSetupBatch = GS_SETUP_BATCH;   // primitive quartets prepared per setup round
 static_assert(kSetupBatch >= 1 && kSetupBatch <= 32, "one primitive quartet per lane at most");
 static_assert(kWideWarps >= 1 && kWideWarps <= 32, "warps per block");
+// Upper bound on the primitive quartets a warp pushes through the VRR node program at once
+// (the generator picks each class's group, WideProg::VGROUP, to fill the lanes of its
+// narrow levels; 1 runs them one at a time).
+#ifndef GS_VRR_GROUP_MAX
+#define GS_VRR_GROUP_MAX 1
+#endif
+
+template <class W>
+constexpr int vrr_group() { return W::VGROUP < GS_VRR_GROUP_MAX ? W::VGROUP : GS_VRR_GROUP_MAX; }
 
 template <int LA, int LB, int LC, int LD, typename T> struct WideLayout {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
     static constexpr int SC = kSetupBatch * kNCoef;              // coefficients
     static constexpr int SF = kSetupBatch * (G::L + 1);          // Boys values
-    static constexpr int VRR = SC + SF + W::NVSLOT;
+    static constexpr int VRR = SC + SF + vrr_group<W>() * W::NVSLOT;
     // write/Schwarz epilogues need the HRR buffer and the scale vectors; the J/K epilogue
     // also a scaled copy of the block
     static constexpr int HR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
@@ -91,6 +100,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     constexpr int L = G::L;
     constexpr int NACC = G::NACC;
     constexpr int NACCW = (NACC + 31) / 32;
+    constexpr int VG = vrr_group<W>();
     T acc[NACCW];
 #pragma unroll
     for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
@@ -111,6 +121,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
         }
         __syncwarp();
         const int nb = min(kSetupBatch, ntot - base);
+        if constexpr (VG == 1) {
         for (int j = 0; j < nb; ++j) {
             const T* __restrict__ c = sC + j * kNCoef;
             if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
@@ -146,6 +157,48 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                 if (t < NACC) acc[k] += node[__ldg(vtgt + t)];
             }
             __syncwarp();
+        }
+        } else {
+        // VG primitive quartets at a time: the (quartet, node) pairs of a level form one
+        // index space spread over the lanes; quartet g has its own node buffer.  The
+        // accumulators add the quartets in order, so the sums match the one-at-a-time form.
+        for (int j0 = 0; j0 < nb; j0 += VG) {
+            const int ng = min(VG, nb - j0);
+            for (int x = lane; x < ng * (L + 1); x += 32) {
+                const int g = x / (L + 1), m = x - g * (L + 1);
+                node[g * W::NVSLOT + m] = sF[(j0 + g) * (L + 1) + m];
+            }
+            __syncwarp();
+            for (int s = 0; s < W::NVSEG; ++s) {
+                const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
+                const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
+                if (sync && s > 0) __syncwarp();
+                const int tot = ng * cnt;
+                for (int x = lane; x < tot; x += 32) {
+                    const int g = x / cnt, n = x - g * cnt;
+                    const uint4 a = __ldg(vrec + 2 * (noff + n));
+                    const uint4 b = __ldg(vrec + 2 * (noff + n) + 1);
+                    const T* __restrict__ c = sC + (j0 + g) * kNCoef;
+                    T* nd = node + g * W::NVSLOT;
+                    T r = c[a.y >> 16] * nd[a.y & 0xffff];
+                    r = fma(c[a.z >> 16], nd[a.z & 0xffff], r);
+                    if (nt > 2) r = fma(c[a.w >> 16], nd[a.w & 0xffff], r);
+                    if (nt > 3) r = fma(c[b.x >> 16], nd[b.x & 0xffff], r);
+                    if (nt > 4) r = fma(c[b.y >> 16], nd[b.y & 0xffff], r);
+                    nd[a.x & 0xffff] = r;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < NACCW; ++k) {
+                const int t = lane + 32 * k;
+                if (t < NACC) {
+                    const int v = __ldg(vtgt + t);
+                    for (int g = 0; g < ng; ++g) acc[k] += node[g * W::NVSLOT + v];
+                }
+            }
+            __syncwarp();
+        }
         }
     }
     // horizontal recursion in shared memory

@@ -563,6 +563,31 @@ def wide_program(cls):
                 vrr_flops=v.em.flops, hrr_flops=h.em.flops)
 
 
+VGROUP_SLOT_BUDGET = 1536     # node slots (doubles) the grouped VRR buffers may take per warp
+
+
+def vrr_group(vseg, nvslot):
+    """Primitive quartets a warp runs through the VRR node program at once: the smallest
+    of 1, 2, 4, 8 that fills at least 85 % of the lanes of the program's segments (or the
+    best within the buffer budget)."""
+    def eff(g):
+        useful = slots = 0
+        for s in vseg:
+            cnt, nt = s[2], s[3]
+            useful += g * cnt * nt
+            slots += -(-g * cnt // 32) * 32 * nt
+        return useful / max(1, slots)
+    best = 1
+    for g in (1, 2, 4, 8):
+        if g * nvslot > VGROUP_SLOT_BUDGET and g > 1:
+            break
+        if eff(g) > eff(best) + 0.02:
+            best = g
+        if eff(g) >= 0.85:
+            break
+    return best
+
+
 def emit_wide(cls):
     p = wide_program(cls)
     tag = "".join(map(str, cls))
@@ -582,7 +607,8 @@ def emit_wide(cls):
            arr("int", f"w{tag}_hlev", p["hlev"]),
            arr("unsigned short", f"w{tag}_out", p["outslot"]),
            f"template <> struct WideProg<{la}, {lb}, {lc}, {ld}> {{",
-           f"  static constexpr int NVSLOT = {p['nvslot']}, NVSEG = {len(p['vseg'])};",
+           f"  static constexpr int NVSLOT = {p['nvslot']}, NVSEG = {len(p['vseg'])}, "
+           f"VGROUP = {vrr_group(p['vseg'], p['nvslot'])};",
            f"  static constexpr int HSIZE = {p['hsize']}, NHLEV = {len(p['hlev']) - 1};",
            f"  static __device__ const uint4* vrec() {{ return reinterpret_cast<const uint4*>(w{tag}_vrec); }}",
            f"  static __device__ const int* vseg() {{ return w{tag}_vseg; }}",
