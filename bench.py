@@ -241,7 +241,7 @@ def run_gpu(args, rank, world):
         from gaussium_gb300 import autotune
         batch.pairs.build()
         chosen = autotune.tune_blocks(batch, out, reps=2)
-        forms = {"%d%d%d%d/fp%d" % (*c, p): ("warp" if r["form"] == 2 else "thread")
+        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
                  for (c, p), r in chosen.items()}
 
     def step(precision, timing=None):
@@ -408,7 +408,7 @@ def run_water(args, rank, world):
         rng = np.random.default_rng(0)
         a = rng.standard_normal((eng.sb.nbf, eng.sb.nbf)) * 0.1
         chosen = autotune.tune_jk(eng, torch.tensor(a + a.T, device="cuda"), reps=2)
-        forms = {"%d%d%d%d/fp%d" % (*c, p): ("warp" if r["form"] == 2 else "thread")
+        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
                  for (c, p), r in chosen.items()}
     with ClockSampler() as clk:
         r64 = driver.rhf(mol, engine=eng, threshold=1e-10)
@@ -456,8 +456,9 @@ def run_batch(args, rank, world):
     opts = dict(mixed_cut=args.mixed_cut, screen_thr=1e-12, incremental=True)
     forms = {}
     if not args.no_tune:
+        from gaussium_gb300 import autotune
         chosen = eng.tune(reps=2)
-        forms = {"%d%d%d%d/fp%d" % (*c, p): ("warp" if r["form"] == 2 else "thread")
+        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
                  for (c, p), r in chosen.items()}
     eng.run(max_iter=2, **opts)              # warm-up and graph capture
     torch.cuda.synchronize()
@@ -551,8 +552,9 @@ def run_gradient(args, rank, world):
     natom = len(mol.symbols)
     forms = {}
     if not args.no_tune:
+        from gaussium_gb300 import autotune
         chosen = gradient.tune_eri_gradient(sb, eng, sa, P, natom, reps=2)
-        forms = {"%d%d%d%d" % c: ("warp" if r["form"] == 2 else "thread") for c, r in chosen.items()}
+        forms = {"%d%d%d%d" % c: autotune.NAMES[r["form"]] for c, r in chosen.items()}
     gradient.eri_gradient(sb, eng, sa, P, natom)
     torch.cuda.synchronize()
     t0 = time.perf_counter()

@@ -1,10 +1,11 @@
 """Per-class kernel-form autotuner.
 
-A class (la lb|lc ld) whose total angular momentum lies in the overlap of the two kernel
-families is built both as the one-thread-per-quartet kernel and as the warp-per-quartet
-kernel (``gs_class_variants``).  Which is faster depends on the workload, chiefly on the
-primitive counts of the quartets: a warp spends its lanes on primitive quartets, so it
-wins on highly contracted quartets and loses on quartets of one or two primitives.  The
+A class (la lb|lc ld) whose total angular momentum lies in the overlap of the kernel
+families is built as the one-thread-per-quartet kernel, as the warp-per-quartet kernel
+and, where its narrow recursion levels leave lanes idle, as the warp kernel that pushes
+several primitive quartets through each pass (``gs_class_variants``).  Which is faster
+depends on the workload, chiefly on the primitive counts of the quartets and on how much
+shared memory the grouped buffers take from occupancy.  The
 tuner times both forms of every such class on the caller's own task lists (CUDA events on
 the launching stream, after a warm-up launch, median of ``reps``) and selects the faster
 with ``gs_set_class_variant``.  The choice is process-wide and stays until changed.
@@ -15,15 +16,16 @@ import torch
 
 from . import _lib
 
-THREAD, WARP = 1, 2
+THREAD, WARP, GROUPED = 1, 2, 3
+NAMES = {THREAD: "thread", WARP: "warp", GROUPED: "warp-grouped"}
 
 
 def forms(cls, precision):
-    """Kernel forms built for a class: a subset of {THREAD, WARP}."""
+    """Kernel forms built for a class: a subset of {THREAD, WARP, GROUPED}."""
     m = _lib.lib().gs_class_variants(*cls, precision)
     if m < 0:
         _lib.check(-m, f"gs_class_variants{cls}")
-    return [v for v in (THREAD, WARP) if m & (1 << (v - 1))]
+    return [v for v in (THREAD, WARP, GROUPED) if m & (1 << (v - 1))]
 
 
 def set_form(cls, precision, variant):

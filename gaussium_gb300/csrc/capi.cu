@@ -34,8 +34,9 @@ int find_variants(int la, int lb, int lc, int ld, int prec) {
 }
 
 // Kernel form per class and precision chosen at run time: 0 = the built-in default by
-// total angular momentum, 1 = one thread per quartet, 2 = one warp per quartet.  It rides
-// in bits 8.. of the precision argument of the class launchers.
+// total angular momentum, 1 = one thread per quartet, 2 = one warp per quartet, 3 = one warp
+// per quartet with several primitive quartets per VRR pass.  It rides in bits 8.. of the
+// precision argument of the class launchers.
 int g_variant[3][3][3][3][2] = {};
 
 inline int pv(int la, int lb, int lc, int ld, int prec) {
@@ -160,18 +161,17 @@ __global__ void k_partition(int ntask, const int2* __restrict__ tasks,
 // Peak-rate probe: each thread runs `iters` rounds of 8 independent FMA chains.
 template <typename T>
 __global__ void k_fma(int iters, T seed, T* __restrict__ sink) {
-    T a0 = seed + threadIdx.x, a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
-    T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
-    const T b = T(0.999999), c = T(1e-7);
+    // eight independent accumulator chains c_k <- a c_k + b per thread (a, b per thread)
+    const T a = seed + T(1e-7) * threadIdx.x, b = seed * T(0.5);
+    T c0 = T(1), c1 = T(2), c2 = T(3), c3 = T(4), c4 = T(5), c5 = T(6), c6 = T(7), c7 = T(8);
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
-            a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+            c0 = fma(a, c0, b); c1 = fma(a, c1, b); c2 = fma(a, c2, b); c3 = fma(a, c3, b);
+            c4 = fma(a, c4, b); c5 = fma(a, c5, b); c6 = fma(a, c6, b); c7 = fma(a, c7, b);
         }
     }
-    const T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
-    if (s == T(-12345)) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the work live
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = c0 + c1 + c2 + c3 + c4 + c5 + c6 + c7;
 }
 
 }  // namespace
@@ -216,7 +216,7 @@ int gs_class_variants(int la, int lb, int lc, int ld, int precision) {
 
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant) {
     if (!find_class(la, lb, lc, ld)) return GS_ERR_CLASS;
-    if ((precision != 64 && precision != 32) || variant < 0 || variant > 2) return GS_ERR_ARG;
+    if ((precision != 64 && precision != 32) || variant < 0 || variant > 3) return GS_ERR_ARG;
     if (variant && !(find_variants(la, lb, lc, ld, precision) & (1 << (variant - 1))))
         return GS_ERR_ARG;
     g_variant[la][lb][lc][ld][precision == 64 ? 0 : 1] = variant;

@@ -1,11 +1,14 @@
-// Per-class launcher: the one-thread-per-quartet kernel or the warp-cooperative kernel.
+// Per-class launcher: the one-thread-per-quartet kernel, the warp-cooperative kernel, or the
+// warp kernel in its grouped form (WideProg::VGROUP primitive quartets per VRR pass).
 // Which forms a class is built with depends on its total angular momentum L:
 //   FP64 thread kernel for L <= GS_THREAD64_MAX, FP64 warp kernel for L >= GS_WIDE_FROM,
-//   FP32 thread kernel for L <= GS_THREAD32_MAX, FP32 warp kernel for L >= GS_WIDE32_FROM.
-// Where both exist the caller's choice (bits 8.. of the precision argument: 1 = thread,
-// 2 = warp) wins, else the default: warp from L = GS_WIDE64_MIN (FP64) or GS_WIDE32_MIN
-// (FP32) up.  On GB300 the FP64 pipe is the limit and the warp kernel keeps it busier for
-// the larger classes; in FP32 the thread kernel is faster until its state no longer fits.
+//   FP32 thread kernel for L <= GS_THREAD32_MAX, FP32 warp kernel for L >= GS_WIDE32_FROM,
+//   grouped form wherever the warp kernel is built and the class's group is above 1.
+// Where several exist the caller's choice (bits 8.. of the precision argument: 1 = thread,
+// 2 = warp, 3 = grouped warp) wins, else the default: the warp kernel from L = GS_WIDE64_MIN
+// (FP64) or GS_WIDE32_MIN (FP32) up, grouped when its group is at least 4.  On GB300 a
+// warp-wide FP64 instruction holds the pipe for the same time whatever its active lanes, so
+// narrow recursion levels are filled with several primitive quartets.
 #pragma once
 #include "eri_kernels.cuh"
 #include "eri_wide.cuh"
@@ -31,50 +34,54 @@
 
 namespace gs {
 
-template <int L>
+template <int LA, int LB, int LC, int LD>
 struct ClassForms {
+    static constexpr int L = LA + LB + LC + LD;
+    static constexpr int VG = WideProg<LA, LB, LC, LD>::VGROUP;
     // a class always has at least one form in each precision
     static constexpr bool wide64 = L >= GS_WIDE_FROM;
     static constexpr bool thread64 = L <= GS_THREAD64_MAX || !wide64;
     static constexpr bool wide32 = L >= GS_WIDE32_FROM && L >= GS_WIDE_FROM;
     static constexpr bool thread32 = L <= GS_THREAD32_MAX || !wide32;
+    static constexpr bool grouped64 = wide64 && VG > 1;
+    static constexpr bool grouped32 = wide32 && VG > 1;
 };
 
-// bit 0: thread kernel built, bit 1: warp kernel built
+// bit 0: thread kernel built, bit 1: warp kernel built, bit 2: grouped warp kernel built
 template <int LA, int LB, int LC, int LD>
 int variants(int prec) {
-    using F = ClassForms<LA + LB + LC + LD>;
-    if (prec == 64) return (F::thread64 ? 1 : 0) | (F::wide64 ? 2 : 0);
-    return (F::thread32 ? 1 : 0) | (F::wide32 ? 2 : 0);
+    using F = ClassForms<LA, LB, LC, LD>;
+    if (prec == 64) return (F::thread64 ? 1 : 0) | (F::wide64 ? 2 : 0) | (F::grouped64 ? 4 : 0);
+    return (F::thread32 ? 1 : 0) | (F::wide32 ? 2 : 0) | (F::grouped32 ? 4 : 0);
+}
+
+template <int LA, int LB, int LC, int LD, int PREC>
+int launch_prec(int kind, int variant, const void* args, cudaStream_t st) {
+    using F = ClassForms<LA, LB, LC, LD>;
+    constexpr bool thread = PREC == 64 ? F::thread64 : F::thread32;
+    constexpr bool wide = PREC == 64 ? F::wide64 : F::wide32;
+    constexpr bool grouped = PREC == 64 ? F::grouped64 : F::grouped32;
+    constexpr int wide_min = PREC == 64 ? GS_WIDE64_MIN : GS_WIDE32_MIN;
+    int v = variant;
+    if (v == 0) v = (!thread || F::L >= wide_min) ? (grouped && F::VG >= 4 ? 3 : 2) : 1;
+    if (kind == GS_KIND_SCHWARZ && v == 3) v = 2;
+    if constexpr (grouped) {
+        if (v == 3) return launch_wide<LA, LB, LC, LD, PREC, F::VG>(kind, args, st);
+    }
+    if constexpr (wide) {
+        if (v >= 2 || !thread) return launch_wide<LA, LB, LC, LD, PREC>(kind, args, st);
+    }
+    if constexpr (thread) return launch_class<LA, LB, LC, LD, PREC>(kind, args, st);
+    return GS_ERR_CLASS;
 }
 
 template <int LA, int LB, int LC, int LD>
 int launch_any(int kind, int prec_variant, const void* args, cudaStream_t st) {
-    constexpr int L = LA + LB + LC + LD;
-    using F = ClassForms<L>;
     const int variant = prec_variant >> 8;
     int prec = prec_variant & 0xff;
     if (kind == GS_KIND_SCHWARZ) prec = 64;
-    if (prec == 64) {
-        if constexpr (F::wide64 && F::thread64) {
-            const bool wide = variant ? variant == 2 : L >= GS_WIDE64_MIN;
-            if (wide) return launch_wide<LA, LB, LC, LD, 64>(kind, args, st);
-            return launch_class<LA, LB, LC, LD, 64>(kind, args, st);
-        } else if constexpr (F::wide64) {
-            return launch_wide<LA, LB, LC, LD, 64>(kind, args, st);
-        } else {
-            return launch_class<LA, LB, LC, LD, 64>(kind, args, st);
-        }
-    }
-    if constexpr (F::wide32 && F::thread32) {
-        const bool wide = variant ? variant == 2 : L >= GS_WIDE32_MIN;
-        if (wide) return launch_wide<LA, LB, LC, LD, 32>(kind, args, st);
-        return launch_class<LA, LB, LC, LD, 32>(kind, args, st);
-    } else if constexpr (F::wide32) {
-        return launch_wide<LA, LB, LC, LD, 32>(kind, args, st);
-    } else {
-        return launch_class<LA, LB, LC, LD, 32>(kind, args, st);
-    }
+    if (prec == 64) return launch_prec<LA, LB, LC, LD, 64>(kind, variant, args, st);
+    return launch_prec<LA, LB, LC, LD, 32>(kind, variant, args, st);
 }
 
 }  // namespace gs

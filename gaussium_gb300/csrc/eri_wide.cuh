@@ -30,22 +30,14 @@ constexpr int kNCoef = 32;                    // coefficient slots per primitive
 constexpr int kSetupBatch = GS_SETUP_BATCH;   // primitive quartets prepared per setup round
 static_assert(kSetupBatch >= 1 && kSetupBatch <= 32, "one primitive quartet per lane at most");
 static_assert(kWideWarps >= 1 && kWideWarps <= 32, "warps per block");
-// Upper bound on the primitive quartets a warp pushes through the VRR node program at once
-// (the generator picks each class's group, WideProg::VGROUP, to fill the lanes of its
-// narrow levels; 1 runs them one at a time).
-#ifndef GS_VRR_GROUP_MAX
-#define GS_VRR_GROUP_MAX 1
-#endif
-
-template <class W>
-constexpr int vrr_group() { return W::VGROUP < GS_VRR_GROUP_MAX ? W::VGROUP : GS_VRR_GROUP_MAX; }
-
-template <int LA, int LB, int LC, int LD, typename T> struct WideLayout {
+// VG: primitive quartets a warp pushes through the VRR node program at once (1, or the
+// class's WideProg::VGROUP for the grouped form).
+template <int LA, int LB, int LC, int LD, typename T, int VG = 1> struct WideLayout {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
     static constexpr int SC = kSetupBatch * kNCoef;              // coefficients
     static constexpr int SF = kSetupBatch * (G::L + 1);          // Boys values
-    static constexpr int VRR = SC + SF + vrr_group<W>() * W::NVSLOT;
+    static constexpr int VRR = SC + SF + VG * W::NVSLOT;
     // write/Schwarz epilogues need the HRR buffer and the scale vectors; the J/K epilogue
     // also a scaled copy of the block
     static constexpr int HR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
@@ -90,17 +82,16 @@ __device__ __forceinline__ void wide_setup_m(const PrimRec<T>& P, const PrimRec<
 
 // Evaluate one contracted quartet; on return sm[0 .. HSIZE) holds the HRR buffer whose
 // output slots are W::outslot().
-template <int LA, int LB, int LC, int LD, typename T>
+template <int LA, int LB, int LC, int LD, typename T, int VG>
 __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                                              const PrimRec<T>* __restrict__ prims,
                                              T* __restrict__ sm, int lane) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     constexpr int L = G::L;
     constexpr int NACC = G::NACC;
     constexpr int NACCW = (NACC + 31) / 32;
-    constexpr int VG = vrr_group<W>();
     T acc[NACCW];
 #pragma unroll
     for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
@@ -225,11 +216,11 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     }
 }
 
-template <int LA, int LB, int LC, int LD, typename T>
+template <int LA, int LB, int LC, int LD, typename T, int VG>
 __global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs a) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_W;
@@ -238,7 +229,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs 
     const WriteTask task = a.tasks[t];
     const PairRec B = a.pairs[task.bra];
     const PairRec K = a.pairs[task.ket];
-    wide_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     long long s[4];
     block_strides(task.code, G::NA, G::NB, G::NC, G::ND, s);
     T* sab = sm + W::HSIZE;
@@ -259,11 +250,11 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs 
     }
 }
 
-template <int LA, int LB, int LC, int LD, typename T>
+template <int LA, int LB, int LC, int LD, typename T, int VG>
 __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
     constexpr int NAB = NA * NB, NCD = NC * ND;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -298,7 +289,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
         const double est = bound * dm;
         if (est < a.screen_thr || est < a.prec_lo || est >= a.prec_hi) return;
     }
-    wide_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     const double deg = (B.sa == B.sb ? 0.5 : 1.0) * (K.sa == K.sb ? 0.5 : 1.0) *
                        (task.x == task.y ? 0.5 : 1.0);
     T* V = sm + W::HSIZE;
@@ -381,7 +372,7 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
     if (t >= a.npair) return;
     const int p = a.pair_index[t];
     const PairRec B = a.pairs[p];
-    wide_quartet<LA, LB, LA, LB, T>(B, B, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_quartet<LA, LB, LA, LB, T, 1>(B, B, (const PrimRec<T>*)a.prims, sm, lane);
     const unsigned short* __restrict__ os = W::outslot();
     double m = 0.0;
     constexpr int NAB = G::NA * G::NB;
@@ -406,25 +397,25 @@ int set_smem(size_t sh) {
     return 0;
 }
 
-template <int LA, int LB, int LC, int LD, int PREC>
+template <int LA, int LB, int LC, int LD, int PREC, int VG = 1>
 int launch_wide(int kind, const void* args, cudaStream_t st) {
     using T = typename std::conditional<PREC == 64, double, float>::type;
-    using Lay = WideLayout<LA, LB, LC, LD, T>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     constexpr int TPB = 32 * kWideWarps;
     if (kind == GS_KIND_WRITE) {
         const WriteArgs& a = *(const WriteArgs*)args;
         if (a.ntask <= 0) return 0;
-        auto k = k_wide_write<LA, LB, LC, LD, T>;
-        if (set_smem<k_wide_write<LA, LB, LC, LD, T>>(Lay::BYTES_W)) return GS_ERR_CUDA;
+        auto k = k_wide_write<LA, LB, LC, LD, T, VG>;
+        if (set_smem<k_wide_write<LA, LB, LC, LD, T, VG>>(Lay::BYTES_W)) return GS_ERR_CUDA;
         k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_W, st>>>(a);
     } else if (kind == GS_KIND_JK) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
-        auto k = k_wide_jk<LA, LB, LC, LD, T>;
-        if (set_smem<k_wide_jk<LA, LB, LC, LD, T>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
+        auto k = k_wide_jk<LA, LB, LC, LD, T, VG>;
+        if (set_smem<k_wide_jk<LA, LB, LC, LD, T, VG>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
         k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_JK, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
-        if constexpr (LA == LC && LB == LD && PREC == 64) {
+        if constexpr (LA == LC && LB == LD && PREC == 64 && VG == 1) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;
             if (a.npair <= 0) return 0;
             auto k = k_wide_schwarz<LA, LB, double>;

@@ -51,15 +51,16 @@ int gs_record_sizes(int* sizes);
 int gs_class_available(int la, int lb, int lc, int ld);
 
 /* Kernel forms built for class (la lb|lc ld) in the given precision (64 or 32): bit 0 the
- * one-thread-per-quartet kernel, bit 1 the warp-per-quartet kernel; negative status on a
+ * one-thread-per-quartet kernel, bit 1 the warp-per-quartet kernel, bit 2 the warp kernel
+ * that runs several primitive quartets through each recursion pass; negative status on a
  * bad class or precision.  No reference counterpart (the reference has one code path). */
 int gs_class_variants(int la, int lb, int lc, int ld, int precision);
 
 /* Chooses the kernel form later calls use for (la lb|lc ld) in that precision, process-wide:
  * 0 = the built-in default by total angular momentum, 1 = thread per quartet, 2 = warp per
- * quartet (a form the class was not built with is GS_ERR_ARG).  Results do not depend on
- * the form beyond rounding; the autotuner times both on the caller's task lists.  No
- * reference counterpart. */
+ * quartet, 3 = grouped warp per quartet (a form the class was not built with is
+ * GS_ERR_ARG).  Results do not depend on the form beyond rounding; the autotuner times the
+ * forms on the caller's task lists.  No reference counterpart. */
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant);
 
 /* K0 shell-pair builder.  Replaces the per-primitive-quartet prologue of

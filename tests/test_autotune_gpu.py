@@ -10,34 +10,43 @@ from molecules import load, random_density
 pytestmark = pytest.mark.gpu
 
 
-def _two_form_classes(precision):
+def _multi_form_classes(precision):
     from gaussium_gb300 import autotune, build
-    return [c for c in build.classes() if len(autotune.forms(c, precision)) == 2]
+    return [c for c in build.classes() if len(autotune.forms(c, precision)) >= 2]
 
 
 @pytest.mark.parametrize("precision,rtol", [(64, 1e-12), (32, 1e-5)])
 def test_forms_agree_on_synthetic_blocks(gpu_lib, precision, rtol):
+    """Every class built with more than one form gives the same blocks in each."""
     from gaussium_gb300 import autotune
     from gaussium_gb300.basis import ShellBasis
     from gaussium_gb300.engine import DeviceShells, QuartetBatch
-    both = _two_form_classes(precision)
-    assert both, "no class is built with both forms"
+    multi = _multi_form_classes(precision)
+    assert multi, "no class is built with more than one form"
     sb = ShellBasis.from_shell_dicts(synthetic_shells())
     q = golden("synthetic")["quartets"]
     ds = DeviceShells(sb)
     batch = QuartetBatch(ds, q, want32=precision == 32)
-    out = {}
+
+    def run():
+        buf = torch.zeros(max(1, batch.total), dtype=torch.float64, device="cuda")
+        batch.run(buf, precision)
+        return buf.cpu().numpy()
+
+    ref = run()
+    tried = set()
     try:
-        for v in (autotune.THREAD, autotune.WARP):
-            for cls in both:
-                autotune.set_form(cls, precision, v)
-            buf = torch.zeros(max(1, batch.total), dtype=torch.float64, device="cuda")
-            batch.run(buf, precision)
-            out[v] = buf.cpu().numpy()
+        for v in (autotune.THREAD, autotune.WARP, autotune.GROUPED):
+            for cls in multi:
+                autotune.set_form(cls, precision, v if v in autotune.forms(cls, precision) else 0)
+                if v in autotune.forms(cls, precision):
+                    tried.add((cls, v))
+            got = run()
+            assert np.max(np.abs(got - ref)) <= rtol * np.max(np.abs(ref)), v
     finally:
-        autotune.reset([(c, 0, 0) for c in both], (precision,))
-    a, b = out[autotune.THREAD], out[autotune.WARP]
-    assert np.max(np.abs(a - b)) <= rtol * np.max(np.abs(a))
+        autotune.reset([(c, 0, 0) for c in multi], (precision,))
+    if precision == 64:
+        assert any(v == autotune.GROUPED for _, v in tried)
 
 
 def test_tuner_chooses_and_jk_unchanged(gpu_lib):
@@ -53,7 +62,7 @@ def test_tuner_chooses_and_jk_unchanged(gpu_lib):
         assert chosen
         for (cls, prec), r in chosen.items():
             assert r["form"] in (autotune.THREAD, autotune.WARP)
-            assert set(r["ms"]) == {autotune.THREAD, autotune.WARP}
+            assert set(r["ms"]) == set(autotune.forms(cls, prec))
         J1, (K1,) = eng.jk(p, [p])
     finally:
         autotune.reset(eng.segments)
