@@ -290,37 +290,35 @@ def run_gpu(args, rank, world):
     achieved = fl[dom] / (res[64]["per_cls"][dom] * 1e-3) / 1e12
     total_flops = sum(fl.values())
 
-    # e2e: host shells -> device, pair build, kernels, blocks -> host, every step
+    # e2e: host shells and tasks -> device, pair build, kernels, blocks -> host, every
+    # step, through the pipelined host-to-host API (copies of batch i+1 in and of batch
+    # i-1 out overlap the kernels of batch i)
     e2e = None
     if not args.no_e2e:
-        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
-                (("centre", sb.centre), ("l", sb.l), ("prim_off", sb.prim_off), ("expo", sb.expo),
-                 ("coef", sb.coef), ("comp_scale", sb.comp_scale))}
-        host_out = torch.empty(batch.total, dtype=torch.float64).pin_memory()
-        h2d = sum(t.numel() * t.element_size() for t in host.values()) + batch.tasks.numel()
-        task_host = batch.tasks.cpu().pin_memory()
-
-        def e2e_step():
-            for k, t in host.items():
-                getattr(ds, k).copy_(t, non_blocking=True)
-            batch.tasks.copy_(task_host, non_blocking=True)
-            batch.pairs.build()
-            batch.run(out, 64)
-            host_out.copy_(out, non_blocking=True)
-
-        for _ in range(args.warmup):
-            e2e_step()
+        from gaussium_gb300.pipeline import BlockPipeline
+        del out
+        torch.cuda.empty_cache()
+        pipe = BlockPipeline(sb, quartets, precision=64, max_exp=args.prim_screen)
+        host_in = BlockPipeline.pinned_shells(sb)
+        host_out = [torch.empty(pipe.total, dtype=torch.float64).pin_memory() for _ in range(2)]
+        for i in range(args.warmup):
+            pipe.submit(host_in, host_out[i % 2])
+        pipe.synchronize()
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
+        for i in range(args.steps):
+            pipe.submit(host_in, host_out[i % 2])
+        pipe.synchronize()
         torch.cuda.synchronize()
         barrier(world)
         e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world)
         e2e = {"value": args.quartets * world / (e2e_ms * 1e-3), "unit": UNIT,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(batch.total * 8),
-               "ms_per_step": e2e_ms}
+               "h2d_bytes_per_step": int(pipe.h2d_bytes(host_in)),
+               "d2h_bytes_per_step": int(pipe.total * 8), "ms_per_step": e2e_ms,
+               "api": "gaussium_gb300.pipeline.BlockPipeline.submit (two device slots, "
+                      "copy-in and copy-out streams overlapping the kernels)"}
+        del pipe
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
