@@ -61,7 +61,7 @@ def test_tuner_chooses_and_jk_unchanged(gpu_lib):
         chosen = autotune.tune_jk(eng, p, precisions=(64,), reps=2)
         assert chosen
         for (cls, prec), r in chosen.items():
-            assert r["form"] in (autotune.THREAD, autotune.WARP)
+            assert r["form"] in (autotune.THREAD, autotune.WARP, autotune.GROUPED)
             assert set(r["ms"]) == set(autotune.forms(cls, prec))
         J1, (K1,) = eng.jk(p, [p])
     finally:
