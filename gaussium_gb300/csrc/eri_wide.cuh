@@ -25,9 +25,6 @@ template <int LA, int LB, int LC, int LD> struct WideProg;
 #ifndef GS_SETUP_BATCH
 #define GS_SETUP_BATCH 32
 #endif
-#ifndef GS_VRR_ILP
-#define GS_VRR_ILP 1      // nodes of a VRR level a lane computes at a time (1 or 2)
-#endif
 constexpr int kWideWarps = GS_WIDE_WARPS;     // warps per block
 constexpr int kNCoef = 32;                    // coefficient slots per primitive quartet
 constexpr int kSetupBatch = GS_SETUP_BATCH;   // primitive quartets prepared per setup round
@@ -125,33 +122,6 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                 const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
                 if (sync && s > 0) __syncwarp();
                 int n = lane;
-#if GS_VRR_ILP == 2
-                // two nodes of the level per lane at a time: their loads and FMA chains
-                // interleave (nodes of one level never read each other)
-                for (; n + 32 < cnt; n += 64) {
-                    const uint4 a0 = __ldg(vrec + 2 * (noff + n)), b0 = __ldg(vrec + 2 * (noff + n) + 1);
-                    const uint4 a1 = __ldg(vrec + 2 * (noff + n + 32));
-                    const uint4 b1 = __ldg(vrec + 2 * (noff + n + 32) + 1);
-                    T r0 = c[a0.y >> 16] * node[a0.y & 0xffff];
-                    T r1 = c[a1.y >> 16] * node[a1.y & 0xffff];
-                    r0 = fma(c[a0.z >> 16], node[a0.z & 0xffff], r0);
-                    r1 = fma(c[a1.z >> 16], node[a1.z & 0xffff], r1);
-                    if (nt > 2) {
-                        r0 = fma(c[a0.w >> 16], node[a0.w & 0xffff], r0);
-                        r1 = fma(c[a1.w >> 16], node[a1.w & 0xffff], r1);
-                    }
-                    if (nt > 3) {
-                        r0 = fma(c[b0.x >> 16], node[b0.x & 0xffff], r0);
-                        r1 = fma(c[b1.x >> 16], node[b1.x & 0xffff], r1);
-                    }
-                    if (nt > 4) {
-                        r0 = fma(c[b0.y >> 16], node[b0.y & 0xffff], r0);
-                        r1 = fma(c[b1.y >> 16], node[b1.y & 0xffff], r1);
-                    }
-                    node[a0.x & 0xffff] = r0;
-                    node[a1.x & 0xffff] = r1;
-                }
-#endif
                 uint4 ra = make_uint4(0, 0, 0, 0), rb = ra;
                 if (n < cnt) {
                     ra = __ldg(vrec + 2 * (noff + n));
