@@ -198,7 +198,8 @@ def flops_model(batch, opcount):
     return out
 
 
-def fma_peak(precision):
+def fma_peak(precision, lanes=32):
+    """FMA rate of the gs_fma_probe kernel (TFLOP/s counted over the active lanes)."""
     import torch
     from gaussium_gb300 import _lib
     L = _lib.lib()
@@ -206,17 +207,18 @@ def fma_peak(precision):
     blocks, threads = sm * 8, 256
     sink = torch.zeros(blocks * threads, dtype=torch.float64, device="cuda")
     iters = 400 if precision == 64 else 8000
-    L.gs_fma_probe(precision, blocks, threads, 10, _lib.ptr(sink), _lib.stream())
+    L.gs_fma_probe_lanes(precision, blocks, threads, 10, lanes, _lib.ptr(sink), _lib.stream())
     best = 0.0
     for _ in range(3):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        _lib.check(L.gs_fma_probe(precision, blocks, threads, iters, _lib.ptr(sink), _lib.stream()),
-                   "fma")
+        _lib.check(L.gs_fma_probe_lanes(precision, blocks, threads, iters, lanes, _lib.ptr(sink),
+                                        _lib.stream()), "fma")
         e1.record()
         torch.cuda.synchronize()
-        best = max(best, blocks * threads * iters * 16 * 8 * 2 / (e0.elapsed_time(e1) * 1e-3))
+        best = max(best, blocks * threads * lanes / 32 * iters * 16 * 8 * 2 /
+                   (e0.elapsed_time(e1) * 1e-3))
     return best / 1e12
 
 
@@ -285,6 +287,9 @@ def run_gpu(args, rank, world):
     # roofline of the dominant FP64 kernel
     peak64 = fma_peak(64)
     peak32 = fma_peak(32)
+    # FP64 rate with 8 of 32 lanes active: equal time per warp instruction means a quarter
+    # of the rate, the reason narrow recursion levels are filled with several quartets
+    peak64_8lanes = fma_peak(64, lanes=8)
     fl = flops_model(batch, opcount)
     dom = max(res[64]["per_cls"], key=res[64]["per_cls"].get)
     achieved = fl[dom] / (res[64]["per_cls"][dom] * 1e-3) / 1e12
@@ -373,6 +378,7 @@ def run_gpu(args, rank, world):
         "fp64": {"value": n_all / (ms64 * 1e-3), "ms_per_step": ms64,
                  "tflops": total_flops / (ms64 * 1e-3) / 1e12,
                  "frac_of_fp64_peak": total_flops / (ms64 * 1e-3) / 1e12 / peak64},
+        "fp64_rate_with_8_of_32_lanes_active_tflops": peak64_8lanes,
         "fp32": {"value": n_all / (ms32 * 1e-3), "ms_per_step": ms32,
                  "max_abs_err_vs_fp64": err32, "fp32_peak_tflops": peak32},
         "per_class_ms_fp64": {"".join(map(str, c)): round(v, 3) for c, v in res[64]["per_cls"].items()},

@@ -35,6 +35,7 @@ _SIGS = {
     "gs_set_class_variant": (I, [I, I, I, I, I, I]),
     "gs_boys_eval": (I, [I, I, I, P, P, P]),
     "gs_fma_probe": (I, [I, I, I, I, P, P]),
+    "gs_fma_probe_lanes": (I, [I, I, I, I, I, P, P]),
     "gs_one_electron": (I, [P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),
     "gs_eri_grad_contract": (I, [I, P, P, P, P, P, P, P, I, P, P, P]),
     "gs_eri_grad": (I, [I, I, I, I, P, P, P, P, P, I, P, I, I, P, P, P]),

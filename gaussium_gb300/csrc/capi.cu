@@ -160,10 +160,12 @@ __global__ void k_partition(int ntask, const int2* __restrict__ tasks,
 
 // Peak-rate probe: each thread runs `iters` rounds of 8 independent FMA chains.
 template <typename T>
-__global__ void k_fma(int iters, T seed, T* __restrict__ sink) {
-    // eight independent accumulator chains c_k <- a c_k + b per thread (a, b per thread)
+__global__ void k_fma(int iters, int lanes, T seed, T* __restrict__ sink) {
+    // eight independent accumulator chains c_k <- a c_k + b per thread (a, b per thread);
+    // only the first `lanes` lanes of each warp run them
     const T a = seed + T(1e-7) * threadIdx.x, b = seed * T(0.5);
     T c0 = T(1), c1 = T(2), c2 = T(3), c3 = T(4), c4 = T(5), c5 = T(6), c6 = T(7), c7 = T(8);
+    if ((int)(threadIdx.x & 31) >= lanes) iters = 0;
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -474,12 +476,22 @@ int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* 
     return check_launch();
 }
 
-int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream) {
-    if (blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0 || !sink) return GS_ERR_ARG;
-    if (precision == 64) k_fma<double><<<blocks, threads, 0, S(stream)>>>(iters, 1.0, (double*)sink);
-    else if (precision == 32) k_fma<float><<<blocks, threads, 0, S(stream)>>>(iters, 1.0f, (float*)sink);
-    else return GS_ERR_ARG;
+int gs_fma_probe_lanes(int precision, int blocks, int threads, int iters, int lanes, void* sink,
+                       void* stream) {
+    if (blocks <= 0 || threads <= 0 || threads > 1024 || iters < 0 || lanes < 1 || lanes > 32 ||
+        !sink)
+        return GS_ERR_ARG;
+    if (precision == 64)
+        k_fma<double><<<blocks, threads, 0, S(stream)>>>(iters, lanes, 1.0, (double*)sink);
+    else if (precision == 32)
+        k_fma<float><<<blocks, threads, 0, S(stream)>>>(iters, lanes, 1.0f, (float*)sink);
+    else
+        return GS_ERR_ARG;
     return check_launch();
+}
+
+int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream) {
+    return gs_fma_probe_lanes(precision, blocks, threads, iters, 32, sink, stream);
 }
 
 }  // extern "C"
