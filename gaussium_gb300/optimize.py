@@ -9,7 +9,7 @@ beta = 2 + 2/m, gamma = 0.75 + 1/(2m), delta = 0.5 - 1/m, and the stop when the 
 deviation of the simplex energies is <= threshold.
 
 ``optimize_bfgs`` minimises the RHF energy with scipy's BFGS on the analytic gradient
-(gaussium_gb300.gradient), in Cartesian coordinates.
+(gaussium_gb300.gradient), over the same internal-frame variables.
 """
 import numpy as np
 
@@ -126,17 +126,28 @@ class NelderMead:
         return simplex, [self.energy(p) for p in simplex]
 
 
-def optimize_bfgs(mol, basis="6-31G", gtol=1e-5, max_iter=200):
-    """Gradient-driven minimisation; returns (energy, coordinates, evaluations)."""
+def optimize_bfgs(mol, basis="6-31G", gtol=1e-5, max_iter=500, energy_gradient=None):
+    """Gradient-driven minimisation in the Nelder-Mead driver's internal frame (first nucleus
+    at the origin, second on z, third in the yz plane: 3N-6 variables, so the six zero
+    modes of overall translation and rotation are not searched).  The energy is invariant
+    under those motions, so the derivative with respect to each free variable is the
+    Cartesian gradient component that variable sets.  Returns (energy, coordinates,
+    evaluations, max |gradient| at the end).  ``energy_gradient(molecule) -> (E, dE/dR)``
+    defaults to the RHF energy and analytic gradient in ``basis``."""
     from scipy.optimize import minimize
     symbols = mol.symbols
+    frame = NelderMead(symbols, mol.coords, None)
     count = [0]
 
-    def fg(x):
+    def fg(v):
         count[0] += 1
-        e, g, _ = rhf_energy_gradient(Molecule(symbols, x.reshape(-1, 3)), basis)
-        return e, g.ravel()
+        c = frame.coordinates(v)
+        if energy_gradient is None:
+            e, g, _ = rhf_energy_gradient(Molecule(symbols, c), basis)
+        else:
+            e, g = energy_gradient(Molecule(symbols, c))
+        return e, frame._vector(np.asarray(g))
 
-    r = minimize(fg, mol.coords.ravel(), jac=True, method="BFGS",
-                 options={"gtol": gtol, "maxiter": max_iter})
-    return float(r.fun), r.x.reshape(-1, 3), count[0]
+    x0 = frame._vector(frame.frame)
+    r = minimize(fg, x0, jac=True, method="BFGS", options={"gtol": gtol, "maxiter": max_iter})
+    return float(r.fun), frame.coordinates(r.x), count[0], float(np.abs(r.jac).max())

@@ -10,7 +10,7 @@ def test_h2_bfgs_and_nelder_mead_agree(gpu_lib):
     from gaussium_gb300.optimize import NelderMead, optimize_bfgs
     from gaussium_gb300.gradient import rhf_energy_gradient
     mol = Molecule(["H", "H"], np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 1.6]]))
-    e_b, x_b, n_b = optimize_bfgs(mol, "6-31G", gtol=1e-6)
+    e_b, x_b, n_b, g_b = optimize_bfgs(mol, "6-31G", gtol=1e-6)
     nm = NelderMead(mol.symbols, mol.coords, lambda m: rhf_energy_gradient(m, "6-31G", want_gradient=False)[0],
                     threshold=1e-9)
     e_n, x_n = nm.optimize()
