@@ -35,8 +35,11 @@ static_assert(kWideWarps >= 1 && kWideWarps <= 32, "warps per block");
 template <int LA, int LB, int LC, int LD, typename T, int VG = 1> struct WideLayout {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    static constexpr int SC = kSetupBatch * kNCoef;              // coefficients
-    static constexpr int SF = kSetupBatch * (G::L + 1);          // Boys values
+    // primitive quartets set up per round: a grouped form with large node buffers prepares
+    // half as many, so that its shared memory stays near the ungrouped form's
+    static constexpr int SB = (VG > 1 && VG * W::NVSLOT > 1024 && kSetupBatch > 16) ? 16 : kSetupBatch;
+    static constexpr int SC = SB * kNCoef;                       // coefficients
+    static constexpr int SF = SB * (G::L + 1);                   // Boys values
     static constexpr int VRR = SC + SF + VG * W::NVSLOT;
     // write/Schwarz epilogues need the HRR buffer and the scale vectors; the J/K epilogue
     // also a scaled copy of the block
@@ -103,15 +106,15 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     const uint4* __restrict__ vrec = W::vrec();
     const int* __restrict__ vseg = W::vseg();
     const unsigned short* __restrict__ vtgt = W::vtgt();
-    for (int base = 0; base < ntot; base += kSetupBatch) {
+    for (int base = 0; base < ntot; base += Lay::SB) {
         const int i = base + lane;
-        if (lane < kSetupBatch && i < ntot) {
+        if (lane < Lay::SB && i < ntot) {
             const PrimRec<T> P = prims[B.prim_off + i / nK];
             const PrimRec<T> Q = prims[K.prim_off + i % nK];
             wide_setup_m<L, T>(P, Q, sC + lane * kNCoef, sF + lane * (L + 1));
         }
         __syncwarp();
-        const int nb = min(kSetupBatch, ntot - base);
+        const int nb = min(Lay::SB, ntot - base);
         if constexpr (VG == 1) {
         for (int j = 0; j < nb; ++j) {
             const T* __restrict__ c = sC + j * kNCoef;

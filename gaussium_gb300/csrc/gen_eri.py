@@ -563,7 +563,7 @@ def wide_program(cls):
                 vrr_flops=v.em.flops, hrr_flops=h.em.flops)
 
 
-VGROUP_SLOT_BUDGET = 1536     # node slots (doubles) the grouped VRR buffers may take per warp
+VGROUP_SLOT_BUDGET = 2600     # node slots (doubles) the grouped VRR buffers may take per warp
 
 
 def vrr_group(vseg, nvslot):
