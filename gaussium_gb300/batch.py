@@ -164,7 +164,8 @@ class BatchedRHF:
         return G
 
     def run(self, threshold=1e-10, max_iter=60, mixed_cut=None, screen_thr=0.0,
-            incremental=False, reset_every=8, final_fp64=None, use_graph=True):
+            incremental=False, reset_every=8, final_fp64=None, use_graph=True,
+            log_iterations=False):
         """Batched SCF; returns total energies (numpy) and the iteration count.
 
         With ``incremental`` the Fock build of iteration i evaluates G(P_i - P_ref) and adds
@@ -172,7 +173,8 @@ class BatchedRHF:
         skips most quartets once the densities settle, and a converged molecule (dP = 0)
         costs nothing.  ``final_fp64`` (default: on whenever a build is approximate)
         evaluates the reported energies from one full, unscreened FP64 build at the final
-        densities."""
+        densities.  ``log_iterations`` records (iteration, seconds, converged molecules) in
+        ``iteration_log`` (it synchronises the device once per iteration)."""
         key = (mixed_cut, screen_thr)
         if key in self._graphs:
             P_static, g, G_static = self._graphs[key]
@@ -215,9 +217,19 @@ class BatchedRHF:
             state.update(n=state["n"] + 1, P=Pb.clone(), G=G)
             return G
 
+        import time
+        self.iteration_log = []
+        t_start = [time.perf_counter()]
+
+        def log(it, done):
+            torch.cuda.synchronize()
+            now = time.perf_counter()
+            self.iteration_log.append((it, now - t_start[0], int(done.sum())))
+            t_start[0] = now
+
         energies, it, self.converged, Pb = batched_rhf_iterations(
             self.Sb, self.Hb, self.X, self.occ_mask, self.pad_orb, two_electron,
-            threshold=threshold, max_iter=max_iter)
+            threshold=threshold, max_iter=max_iter, on_iteration=log if log_iterations else None)
         self.iterations = it
         self.densities = Pb
         if final_fp64 is None:
@@ -300,7 +312,7 @@ def padded_system(S_list, H_list, nocc, device):
 
 def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold=1e-10,
                            max_iter=60, diis_subspace=8, level_shift=0.3, shift_after=30,
-                           shifted_error=1e-5):
+                           shifted_error=1e-5, on_iteration=None):
     """Restricted SCF of B molecules at once over zero-padded [B, N, N] FP64 matrices.
 
     ``two_electron(P, active)`` returns G = J - K/2 for the padded densities; ``active``
@@ -315,7 +327,8 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
     ``shift_after`` iterations gets a level shift of its virtual orbitals,
     F + level_shift (S - S P S / 2) (the converged density is unchanged by it), and must then
     also bring its largest commutator element below ``shifted_error`` to stop, since the
-    shift slows the energy change.  Returns the electronic energies, the iteration count,
+    shift slows the energy change.  ``on_iteration(it, done)`` is called after each
+    iteration's convergence test.  Returns the electronic energies, the iteration count,
     the per-molecule converged flags and the last densities."""
     dev = Hb.device
     B = Hb.shape[0]
@@ -346,6 +359,8 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
             small &= ~shifted | (err.abs().amax(dim=(1, 2)) < shifted_error)
             done = done | small
         prev = e_now
+        if on_iteration is not None:
+            on_iteration(it, done)
         if bool(done.all()):
             break
         hist_f.append(F)

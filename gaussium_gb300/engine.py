@@ -93,14 +93,16 @@ class PairSet:
         # primitive pairs kept per shell pair (the work per pair after screening)
         self.nprim = self.kept[:self.n].cpu().numpy().astype(np.int64)
 
-    def build(self, stream=None):
-        """(Re)compute the pair records (kernel K0) from the device shells."""
+    def build(self, stream=None, want32=True):
+        """(Re)compute the pair records (kernel K0) from the device shells; with
+        ``want32=False`` only the FP64 records (enough for FP64-only evaluation)."""
         ds = self.ds
         L = _lib.lib()
+        p32 = self.p32 if want32 else None
         _lib.check(L.gs_pairs_build(_lib.ptr(ds.centre), _lib.ptr(ds.l), _lib.ptr(ds.prim_off),
                                     _lib.ptr(ds.expo), _lib.ptr(ds.coef), self.n,
                                     _lib.ptr(self.shells), _lib.ptr(self.prim_start),
-                                    _lib.ptr(self.rec), _lib.ptr(self.p64), _lib.ptr(self.p32),
+                                    _lib.ptr(self.rec), _lib.ptr(self.p64), _lib.ptr(p32),
                                     float(self.max_exp), _lib.ptr(self.kept),
                                     _lib.stream(stream)), "gs_pairs_build")
 

@@ -67,7 +67,7 @@ class BlockPipeline:
         compute.wait_event(slot["h2d"])
         if slot["used"]:
             compute.wait_event(slot["d2h"])
-        slot["batch"].pairs.build(stream=compute)
+        slot["batch"].pairs.build(stream=compute, want32=self.precision == 32)
         slot["batch"].run(slot["out"], self.precision, stream=compute)
         slot["computed"].record(compute)
         self.d2h_stream.wait_event(slot["computed"])
