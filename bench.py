@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--fd-coords", type=int, default=72)
     ap.add_argument("--molecules", type=int, default=256)
     ap.add_argument("--waters", type=int, default=16)
+    ap.add_argument("--guess", default="sad", choices=["core", "sad"],
+                    help="starting density of the batch workload's SCF")
     ap.add_argument("--batch-check", type=int, default=16,
                     help="molecules of the batch workload checked against single FP64 RHF")
     ap.add_argument("--mixed-cut", type=float, default=1e-4)
@@ -458,7 +460,11 @@ def run_batch(args, rank, world):
     eng = batch.BatchedRHF(mols)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
-    opts = dict(mixed_cut=args.mixed_cut, screen_thr=1e-12, incremental=True)
+    opts = dict(mixed_cut=args.mixed_cut, screen_thr=1e-12, incremental=True, guess=args.guess)
+    if args.guess == "sad":
+        from gaussium_gb300 import guess
+        for sym in sorted(set(s for m in mols for s in m.symbols)):
+            guess.element_density(sym, "6-31G*")          # per-element atoms, once
     forms = {}
     if not args.no_tune:
         from gaussium_gb300 import autotune
@@ -488,7 +494,7 @@ def run_batch(args, rank, world):
     # the all-FP64 batched SCF (no density screening, no incremental builds): per-molecule
     # |dE| of the mixed run against it
     t1 = time.perf_counter()
-    e64, it64 = eng.run(threshold=1e-10)
+    e64, it64 = eng.run(threshold=1e-10, guess=args.guess)
     torch.cuda.synchronize()
     t_fp64_scf = time.perf_counter() - t1
     conv64 = eng.converged.copy()
@@ -509,6 +515,7 @@ def run_batch(args, rank, world):
                    "scf_iterations": iters, "converged": int(conv_mixed.sum()),
                    "unique_quartets": int(eng.ntasks), "setup_s": t_setup,
                    "mixed_cut": args.mixed_cut, "screen_thr": 1e-12, "incremental_reset_every": 8,
+                   "guess": args.guess,
                    "final_energy": "one full FP64 build at the converged densities",
                    "kernel_forms_autotuned": forms},
         "fp64_full_build_ms_all_molecules": t_fp64_build * 1e3,

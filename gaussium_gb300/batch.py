@@ -24,6 +24,7 @@ class BatchedRHF:
     def __init__(self, molecules, basis="6-31G*", schwarz_thr=1e-12, device="cuda",
                  max_exp=PRIM_SCREEN):
         self.mols = molecules
+        self.basis = basis
         self.dev = torch.device(device)
         sbs = [shell_basis(m, basis) for m in molecules]
         self.sbs = sbs
@@ -165,7 +166,7 @@ class BatchedRHF:
 
     def run(self, threshold=1e-10, max_iter=60, mixed_cut=None, screen_thr=0.0,
             incremental=False, reset_every=8, final_fp64=None, use_graph=True,
-            log_iterations=False):
+            log_iterations=False, guess="core"):
         """Batched SCF; returns total energies (numpy) and the iteration count.
 
         With ``incremental`` the Fock build of iteration i evaluates G(P_i - P_ref) and adds
@@ -174,7 +175,9 @@ class BatchedRHF:
         costs nothing.  ``final_fp64`` (default: on whenever a build is approximate)
         evaluates the reported energies from one full, unscreened FP64 build at the final
         densities.  ``log_iterations`` records (iteration, seconds, converged molecules) in
-        ``iteration_log`` (it synchronises the device once per iteration)."""
+        ``iteration_log`` (it synchronises the device once per iteration).  ``guess`` is
+        "core" (the reference's core-Hamiltonian start) or "sad" (superposed atomic
+        densities, gaussium_gb300.guess)."""
         key = (mixed_cut, screen_thr)
         if key in self._graphs:
             P_static, g, G_static = self._graphs[key]
@@ -227,9 +230,19 @@ class BatchedRHF:
             self.iteration_log.append((it, now - t_start[0], int(done.sum())))
             t_start[0] = now
 
+        P_init = None
+        if guess == "sad":
+            from .guess import sad_density
+            P_init = torch.zeros_like(self.Hb)
+            for m, mol in enumerate(self.mols):
+                n = int(self.nbf[m])
+                P_init[m, :n, :n] = torch.as_tensor(sad_density(mol, self.basis)).to(self.dev)
+        elif guess != "core":
+            raise ValueError(f"unknown guess {guess!r}")
         energies, it, self.converged, Pb = batched_rhf_iterations(
             self.Sb, self.Hb, self.X, self.occ_mask, self.pad_orb, two_electron,
-            threshold=threshold, max_iter=max_iter, on_iteration=log if log_iterations else None)
+            threshold=threshold, max_iter=max_iter, on_iteration=log if log_iterations else None,
+            P_init=P_init)
         self.iterations = it
         self.densities = Pb
         if final_fp64 is None:
@@ -312,7 +325,7 @@ def padded_system(S_list, H_list, nocc, device):
 
 def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold=1e-10,
                            max_iter=60, diis_subspace=8, level_shift=0.3, shift_after=30,
-                           shifted_error=1e-5, on_iteration=None):
+                           shifted_error=1e-5, on_iteration=None, P_init=None):
     """Restricted SCF of B molecules at once over zero-padded [B, N, N] FP64 matrices.
 
     ``two_electron(P, active)`` returns G = J - K/2 for the padded densities; ``active``
@@ -328,8 +341,10 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
     F + level_shift (S - S P S / 2) (the converged density is unchanged by it), and must then
     also bring its largest commutator element below ``shifted_error`` to stop, since the
     shift slows the energy change.  ``on_iteration(it, done)`` is called after each
-    iteration's convergence test.  Returns the electronic energies, the iteration count,
-    the per-molecule converged flags and the last densities."""
+    iteration's convergence test.  ``P_init`` ([B, N, N], optional) replaces the
+    core-Hamiltonian guess as the first iteration's densities.  Returns the electronic
+    energies, the iteration count, the per-molecule converged flags and the last
+    densities."""
     dev = Hb.device
     B = Hb.shape[0]
     big = 1e6 * pad_orb
@@ -347,8 +362,11 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
     energies = None
     it = 0
     for it in range(1, max_iter + 1):
-        Cocc = C * occ_mask[:, None, :]
-        Pb = 2.0 * Cocc @ Cocc.transpose(1, 2)
+        if it == 1 and P_init is not None:
+            Pb = P_init
+        else:
+            Cocc = C * occ_mask[:, None, :]
+            Pb = 2.0 * Cocc @ Cocc.transpose(1, 2)
         F = Hb + two_electron(Pb, ~done)
         e_now = 0.5 * torch.sum(Pb * (Hb + F), dim=(1, 2))
         energies = e_now if energies is None else torch.where(done, energies, e_now)

@@ -36,3 +36,10 @@ def test_batched_task_list_matches_engine_count(gpu_lib, batch_case):
     b, _ = batch_case
     total = sum(JKEngine(sb, schwarz_thr=1e-12).ntasks for sb in b.sbs)
     assert b.ntasks == total
+
+
+def test_batched_sad_guess_same_energies(gpu_lib, batch_case):
+    b, single = batch_case
+    e, it = b.run(threshold=1e-11, guess="sad")
+    assert b.converged.all()
+    assert np.max(np.abs(e - single)) < 1e-8

@@ -132,3 +132,38 @@ def test_level_shifted_loop_reaches_the_same_energies(systems):
                                             max_iter=200, shift_after=2)
     assert done.all()
     assert np.max(np.abs(e.numpy() - np.array(single))) < 1e-9
+
+
+def test_fractional_occupations():
+    from gaussium_gb300.guess import fractional_occupations
+    eps = np.array([-11.0, -0.7, -0.3, -0.3, -0.3, 0.2])
+    occ = fractional_occupations(eps, 6)          # carbon-like: 1s2 2s2 2p(2/3 x 3)
+    assert np.allclose(occ, [2, 2, 2 / 3, 2 / 3, 2 / 3, 0])
+    assert np.isclose(fractional_occupations(eps, 1).sum(), 1.0)
+
+
+def test_starting_density_reaches_the_same_energy(systems):
+    """Block-diagonal 'atomic' starting densities (fractional-occupation SCF on each atom's
+    own functions) lead the batched loop to the same energies as the core guess."""
+    from gaussium_gb300.guess import atomic_density
+    g = golden("h2o_sto3g")
+    S, H, eri, ne = systems[0]
+    centre = g["centre"]
+    # functions of each atom (the golden lists them atom by atom)
+    atom_of = np.argmin(np.linalg.norm(centre[:, None, :] - g["coords"][None], axis=-1), axis=1)
+    P0 = np.zeros_like(S)
+    for a in range(len(g["coords"])):
+        f = np.flatnonzero(atom_of == a)
+        sub = np.ix_(f, f)
+        e4 = eri[np.ix_(f, f, f, f)]
+        nel = int(round(g["charges"][a]))
+        P0[sub] = atomic_density(S[sub], H[sub], lambda p: oracle.fock_restricted(np.zeros_like(p), e4, p), nel)
+    assert np.isclose(np.sum(P0 * S), ne, atol=1e-6)        # electrons conserved
+    Sb, Hb, X, occ, pad = padded_system([S], [H], [ne // 2], "cpu")
+    two = lambda Pb, active=None: torch.as_tensor(oracle.fock_restricted(np.zeros_like(H), eri,
+                                                                        Pb[0].numpy()))[None]
+    e_core, it_core, _, _ = batched_rhf_iterations(Sb, Hb, X, occ, pad, two, threshold=1e-12)
+    e_sad, it_sad, done, _ = batched_rhf_iterations(Sb, Hb, X, occ, pad, two, threshold=1e-12,
+                                                    P_init=torch.as_tensor(P0)[None])
+    assert done.all()
+    assert abs(float(e_sad[0]) - float(e_core[0])) < 1e-9
