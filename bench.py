@@ -554,8 +554,15 @@ def run_gradient(args, rank, world):
     sb = molecules.shell_basis(mol, "6-31G")
     from gaussium_gb300.engine import JKEngine
     eng = JKEngine(sb, schwarz_thr=1e-14)
+    fock_forms = {}
+    if not args.no_tune:
+        # the Fock build it is compared with gets its own tuned kernel forms
+        from gaussium_gb300 import autotune
+        chosen = autotune.tune_jk(eng, torch.tensor(res.density, device="cuda"), precisions=(64,),
+                                  reps=2)
+        fock_forms = {"%d%d%d%d" % c: autotune.NAMES[r["form"]] for (c, p), r in chosen.items()}
     fb = TimedFock(np.zeros((sb.nbf, sb.nbf)), eng)
-    for _ in range(3):
+    for _ in range(5):
         fb.create(res.density)
     t_fock = float(np.median(fb.builds))
     nocc = mol.electrons // 2
@@ -618,6 +625,7 @@ def run_gradient(args, rank, world):
         "energy": e, "max_abs_grad_minus_fd": err,
         "eri_gradient_ms": t_eri_grad * 1e3, "one_electron_gradient_ms": t_one_grad * 1e3,
         "eri_gradient_ms_per_class": per_cls, "gradient_kernel_forms_autotuned": forms,
+        "fock_kernel_forms_autotuned": fock_forms,
         "fock_build_ms": t_fock * 1e3, "scf_plus_gradient_s": t_total,
     }
     if rank == 0:
