@@ -156,3 +156,42 @@ class RestrictedKohnShamHamiltonianGPU(_Base):
                     xc[i, j] = xc[j, i] = self.exchange_correlation.integrate_potential(
                         density_matrix, i, j)
         return self.core_hamiltonian, J.cpu().numpy(), xc
+
+
+class _BasisOnly:
+    """Stands in for TwoElectronRepulsionMatrixOS inside HartreeFock.__init__
+    (hartreefock/hartree_fock.py:38-41): instead of the N^4 tensor it hands on the
+    basis-function list, which the drop-in Fock builders take as their source."""
+
+    def __init__(self, basis_set_array, symmetry=None, processes=1):
+        self.basis_set_array = basis_set_array
+
+    def create_repulsion_matrix(self):
+        return self.basis_set_array
+
+
+def install(gaussium, **options):
+    """Route a loaded reference package's SCF through this engine: in
+    ``gaussium.hartreefock.hartree_fock`` the tensor builder becomes ``_BasisOnly``, the
+    three Fock builders become the GPU drop-ins, and the spin-blocking of the tensor
+    (``blocked_spin_basis_set``) passes the basis list through (the blocked drop-in builds
+    the spin blocks itself); in ``gaussium.kohnsham.kohn_sham`` the Kohn-Sham Hamiltonian
+    becomes its drop-in.  ``options`` (e.g. ``mixed_cut``, ``incremental``) go to every
+    builder.  Returns the replaced originals, keyed by module attribute, for undoing."""
+    import functools
+    hf = gaussium.hartreefock.hartree_fock
+    swaps = [(hf, "TwoElectronRepulsionMatrixOS", _BasisOnly),
+             (hf, "FockMatrixRestricted", functools.partial(FockMatrixRestrictedGPU, **options)),
+             (hf, "FockMatrixUnrestricted", functools.partial(FockMatrixUnrestrictedGPU, **options)),
+             (hf, "BlockedFockMatrixUnrestricted",
+              functools.partial(BlockedFockMatrixUnrestrictedGPU, **options)),
+             (hf, "blocked_spin_basis_set", lambda basis: basis)]
+    ks = getattr(getattr(gaussium, "kohnsham", None), "kohn_sham", None)
+    if ks is not None:
+        swaps.append((ks, "RestrictedKohnShamHamiltonian",
+                      functools.partial(RestrictedKohnShamHamiltonianGPU, **options)))
+    originals = {}
+    for mod, name, new in swaps:
+        originals[(mod.__name__, name)] = getattr(mod, name)
+        setattr(mod, name, new)
+    return originals
