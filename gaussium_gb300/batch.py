@@ -118,7 +118,26 @@ class BatchedRHF:
         L = _lib.lib()
         st = _lib.stream()
         base = self.tasks.data_ptr()
-        thr = screen_thr if screen_thr > 0 else (1e-300 if mixed_cut is not None else 0.0)
+        if mixed_cut is not None or screen_thr > 0:
+            # partitioned path: screened tasks are dropped on the device before any class
+            # kernel runs, FP64/FP32 by the density-weighted bound
+            cut = mixed_cut if mixed_cut is not None else 0.0
+            thr = screen_thr if screen_thr > 0 else 1e-300
+            need = max(L.gs_fock_jk_mixed_workspace(e - s) for _, s, e in self.segments)
+            if getattr(self, "_ws", None) is None or self._ws.numel() < need:
+                self._ws = torch.empty(int(need), dtype=torch.uint8, device=self.dev)
+            for cls, s, e in self.segments:
+                if classes is not None and cls not in classes:
+                    continue
+                rc = L.gs_fock_jk_batched_mixed(
+                    *cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
+                    _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
+                    _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
+                    _lib.ptr(dmax), self.mat_stride, e - s, base + s * 8, _lib.ptr(P), _lib.ptr(J), 1,
+                    _lib.ptr(P), _lib.ptr(K), thr, cut, _lib.ptr(self._ws), self._ws.numel(), st)
+                _lib.check(rc, f"gs_fock_jk_batched_mixed{cls}")
+            return
+        thr = 0.0
         runs = [(precision, 0.0, float("inf"))]
         if mixed_cut is not None:
             runs = [(64, mixed_cut, float("inf")), (32, 0.0, mixed_cut)]

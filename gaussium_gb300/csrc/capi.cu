@@ -121,9 +121,12 @@ __global__ void k_boys(int n, const double* __restrict__ t, double* __restrict__
 // into an FP64 list (est >= cut), an FP32 list (thr <= est < cut) and dropped (est < thr).
 // Warp-aggregated atomics keep each warp's survivors contiguous, so the primitive-count
 // order of the input survives approximately.
+// dmax: per (shell, shell) block of one molecule (nshell x nshell), or, with shell_mol,
+// one value per molecule (mol_dmax[shell_mol[shell]]).
 __global__ void k_partition(int ntask, const int2* __restrict__ tasks,
                             const gs::PairRec* __restrict__ pairs,
-                            const double* __restrict__ dmax, int nshell, double thr, double cut,
+                            const double* __restrict__ dmax, int nshell,
+                            const int* __restrict__ shell_mol, double thr, double cut,
                             int2* __restrict__ out64, int2* __restrict__ out32,
                             int* __restrict__ counts) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -133,13 +136,18 @@ __global__ void k_partition(int ntask, const int2* __restrict__ tasks,
         task = tasks[t];
         const gs::PairRec B = pairs[task.x];
         const gs::PairRec K = pairs[task.y];
-        const int n = nshell;
-        double dm = dmax[B.sa * n + B.sb];
-        dm = fmax(dm, dmax[K.sa * n + K.sb]);
-        dm = fmax(dm, dmax[B.sa * n + K.sa]);
-        dm = fmax(dm, dmax[B.sa * n + K.sb]);
-        dm = fmax(dm, dmax[B.sb * n + K.sa]);
-        dm = fmax(dm, dmax[B.sb * n + K.sb]);
+        double dm;
+        if (shell_mol) {
+            dm = dmax[shell_mol[B.sa]];
+        } else {
+            const int n = nshell;
+            dm = dmax[B.sa * n + B.sb];
+            dm = fmax(dm, dmax[K.sa * n + K.sb]);
+            dm = fmax(dm, dmax[B.sa * n + K.sa]);
+            dm = fmax(dm, dmax[B.sa * n + K.sb]);
+            dm = fmax(dm, dmax[B.sb * n + K.sa]);
+            dm = fmax(dm, dmax[B.sb * n + K.sb]);
+        }
         const double est = (double)B.qmax * (double)K.qmax * dm;
         kind = est < thr ? 0 : (est >= cut ? 1 : 2);
     }
@@ -369,8 +377,8 @@ int fock_jk_mixed_impl(int la, int lb, int lc, int ld, const void* pair_rec, con
     int2* l32 = l64 + ntask;
     if (cudaMemsetAsync(counts, 0, 2 * sizeof(int), S(stream)) != cudaSuccess) return GS_ERR_CUDA;
     k_partition<<<(ntask + 255) / 256, 256, 0, S(stream)>>>(
-        ntask, (const int2*)tasks, (const gs::PairRec*)pair_rec, shell_dmax, nshell, screen_thr,
-        mixed_cut, l64, l32, counts);
+        ntask, (const int2*)tasks, (const gs::PairRec*)pair_rec, shell_dmax, nshell, nullptr,
+        screen_thr, mixed_cut, l64, l32, counts);
     if (check_launch()) return GS_ERR_CUDA;
     gs::JKArgs a;
     a.pairs = (const gs::PairRec*)pair_rec;
@@ -456,6 +464,61 @@ int gs_fock_jk_mixed_noalloc(int la, int lb, int lc, int ld, const void* pair_re
     return fock_jk_mixed_impl(la, lb, lc, ld, pair_rec, prim64, prim32, comp_scale, func_off,
                               nshell, nbf, ntask, tasks, pj, j, nk, pk, k, shell_dmax, screen_thr,
                               mixed_cut, ws, (long long)sizeof(g_noalloc_ws), stream);
+}
+
+int gs_fock_jk_batched_mixed(int la, int lb, int lc, int ld, const void* pair_rec,
+                             const void* prim64, const void* prim32, const double* comp_scale,
+                             const int* func_off, const int* shell_mol, const long long* mol_base,
+                             const int* mol_n, const double* mol_dmax, long long mat_stride,
+                             int ntask, const int* tasks, const double* pj, double* j, int nk,
+                             const double* pk, double* k, double screen_thr, double mixed_cut,
+                             void* workspace, long long ws_bytes, void* stream) {
+    launch_fn f = find_class(la, lb, lc, ld);
+    if (!f) return GS_ERR_CLASS;
+    if (ntask < 0 || nk < 0 || nk > 1 || !pair_rec || !prim64 || !prim32 || !comp_scale ||
+        !func_off || !shell_mol || !mol_base || !mol_n || !mol_dmax || (ntask > 0 && !tasks) ||
+        (!!pj != !!j) || (nk > 0 && (!pk || !k)) || mat_stride <= 0 || !workspace)
+        return GS_ERR_ARG;
+    if (ws_bytes < gs_fock_jk_mixed_workspace(ntask)) return GS_ERR_NOMEM;
+    if (ntask == 0) return GS_OK;
+    int* counts = (int*)workspace;
+    int2* l64 = (int2*)((char*)workspace + 256);
+    int2* l32 = l64 + ntask;
+    if (cudaMemsetAsync(counts, 0, 2 * sizeof(int), S(stream)) != cudaSuccess) return GS_ERR_CUDA;
+    k_partition<<<(ntask + 255) / 256, 256, 0, S(stream)>>>(
+        ntask, (const int2*)tasks, (const gs::PairRec*)pair_rec, mol_dmax, 0, shell_mol,
+        screen_thr, mixed_cut, l64, l32, counts);
+    if (check_launch()) return GS_ERR_CUDA;
+    gs::JKArgs a;
+    a.pairs = (const gs::PairRec*)pair_rec;
+    a.comp_scale = comp_scale;
+    a.func_off = func_off;
+    a.ntask = ntask;
+    a.nbf = 0;
+    a.nshell = 0;
+    a.nk = nk;
+    a.pj = pj;
+    a.pk = pk;
+    a.j = j;
+    a.k = k;
+    a.shell_dmax = nullptr;
+    a.screen_thr = 0.0;
+    a.prec_lo = 0.0;
+    a.prec_hi = 0.0;
+    a.shell_mol = shell_mol;
+    a.mol_base = mol_base;
+    a.mol_n = mol_n;
+    a.mol_dmax = mol_dmax;
+    a.mat_stride = mat_stride;
+    a.prims = prim64;
+    a.tasks = l64;
+    a.ntask_dev = counts;
+    int rc = f(GS_KIND_JK, pv(la, lb, lc, ld, 64), &a, S(stream));
+    if (rc) return rc;
+    a.prims = prim32;
+    a.tasks = l32;
+    a.ntask_dev = counts + 1;
+    return f(GS_KIND_JK, pv(la, lb, lc, ld, 32), &a, S(stream));
 }
 
 int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream) {

@@ -52,11 +52,9 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_write(const Writ
 // with v = (ab|cd) / ((1+d_ab)(1+d_cd)(1+d_ab,cd)), so that J = J' + J'^T and
 // K = K' + K'^T sum every permutation of every quartet once.
 template <int LA, int LB, int LC, int LD, typename T>
-__global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs a) {
+__device__ __forceinline__ void eri_jk_task(const JKArgs& a, int t) {
     using G = ClassGen<LA, LB, LC, LD>;
     constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (a.ntask_dev ? *a.ntask_dev : a.ntask)) return;
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
@@ -172,6 +170,18 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs 
     }
 }
 
+// One thread per task; with a task count on the device (after a partition) the grid is
+// capped and each thread strides over the tasks.
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs a) {
+    const int n = a.ntask_dev ? *a.ntask_dev : a.ntask;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        eri_jk_task<LA, LB, LC, LD, T>(a, t);
+}
+
+// Blocks launched for a task count that lives on the device (enough to fill the GPU).
+constexpr int kDeviceCountBlocks = 152 * 16;
+
 // Schwarz bound of shell pairs: q[p] = sqrt(max_ijkl |(ab|ab)|) over the scaled block.
 template <int LA, int LB, typename T>
 __global__ void __launch_bounds__(kBlock) k_schwarz(const SchwarzArgs a) {
@@ -203,7 +213,9 @@ int launch_class(int kind, const void* args, cudaStream_t st) {
     } else if (kind == GS_KIND_JK) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
-        k_eri_jk<LA, LB, LC, LD, T><<<(a.ntask + kBlock - 1) / kBlock, kBlock, 0, st>>>(a);
+        int grid = (a.ntask + kBlock - 1) / kBlock;
+        if (a.ntask_dev && grid > kDeviceCountBlocks) grid = kDeviceCountBlocks;
+        k_eri_jk<LA, LB, LC, LD, T><<<grid, kBlock, 0, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
         if constexpr (LA == LC && LB == LD && PREC == 64) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;

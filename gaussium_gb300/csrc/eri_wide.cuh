@@ -254,17 +254,11 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs 
 }
 
 template <int LA, int LB, int LC, int LD, typename T, int VG>
-__global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
+__device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restrict__ sm, int lane) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
     constexpr int NAB = NA * NB, NCD = NC * ND;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_JK;
-    const int t = blockIdx.x * kWideWarps + warp;
-    if (t >= (a.ntask_dev ? *a.ntask_dev : a.ntask)) return;
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
@@ -363,6 +357,24 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
     }
 }
 
+// One warp per task; with a task count on the device (after a partition) the grid is
+// capped and each warp strides over the tasks.
+template <int LA, int LB, int LC, int LD, typename T, int VG>
+__global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_JK;
+    const int ntask = a.ntask_dev ? *a.ntask_dev : a.ntask;
+    for (int t = blockIdx.x * kWideWarps + warp; t < ntask; t += gridDim.x * kWideWarps) {
+        wide_jk_task<LA, LB, LC, LD, T, VG>(a, t, sm, lane);
+        __syncwarp();
+    }
+}
+
+// Blocks launched for a task count that lives on the device (enough to fill the GPU).
+constexpr int kWideDeviceCountBlocks = 152 * 16;
+
 template <int LA, int LB, typename T>
 __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzArgs a) {
     using G = ClassGen<LA, LB, LA, LB>;
@@ -416,7 +428,9 @@ int launch_wide(int kind, const void* args, cudaStream_t st) {
         if (a.ntask <= 0) return 0;
         auto k = k_wide_jk<LA, LB, LC, LD, T, VG>;
         if (set_smem<k_wide_jk<LA, LB, LC, LD, T, VG>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
-        k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_JK, st>>>(a);
+        int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
+        if (a.ntask_dev && grid > kWideDeviceCountBlocks) grid = kWideDeviceCountBlocks;
+        k<<<grid, TPB, Lay::BYTES_JK, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
         if constexpr (LA == LC && LB == LD && PREC == 64 && VG == 1) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;

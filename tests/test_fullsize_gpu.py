@@ -1,0 +1,81 @@
+"""The microbench at its full size (2,000,000 seeded shell quartets, l uniform over s/p/d,
+K uniform 1-6): size-independent properties of the whole batch, and a seeded sample of
+its quartets against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def full():
+    from gaussium_gb300 import engine
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(2_000_000, seed=0)
+    ds = engine.DeviceShells(sb)
+    batch = engine.QuartetBatch(ds, q, want32=True, max_exp=engine.PRIM_SCREEN)
+    out = torch.empty(batch.total, dtype=torch.float64, device="cuda")
+    batch.run(out, 64)
+    return sb, q, batch, out
+
+
+def test_forms_agree_at_full_size(gpu_lib, full):
+    """Every class evaluated once more in another of its kernel forms: same blocks."""
+    from gaussium_gb300 import autotune
+    sb, q, batch, out = full
+    ref = out.clone()
+    changed = []
+    try:
+        for cls, _, _ in batch.segments:
+            fs = autotune.forms(cls, 64)
+            if len(fs) > 1:
+                autotune.set_form(cls, 64, fs[0] if fs[0] != autotune.WARP else fs[-1])
+                changed.append(cls)
+        batch.run(out, 64)
+    finally:
+        autotune.reset([(c, 0, 0) for c in changed], (64,))
+    scale = ref.abs().max()
+    assert changed
+    assert float((out - ref).abs().max() / scale) < 1e-12
+    batch.run(out, 64)
+
+
+def test_fp32_close_to_fp64_at_full_size(gpu_lib, full):
+    sb, q, batch, out = full
+    o32 = torch.empty_like(out)
+    batch.run(o32, 32)
+    err = (o32 - out).abs()
+    # FP32 integrals carry about 1e-6 relative error per block
+    assert float(err.max() / out.abs().max()) < 1e-5
+    assert bool(torch.isfinite(o32).all())
+
+
+def test_sampled_quartets_match_oracle(gpu_lib, full):
+    """64 seeded quartets of the 2M batch against the exact-Boys oracle."""
+    from gaussium_gb300.basis import COMPONENTS
+    sb, q, batch, out = full
+    rng = np.random.default_rng(11)
+    pick = rng.choice(len(q), size=64, replace=False)
+    off = batch.offsets
+    host = out.cpu().numpy()
+    centre, lmn, cnorm, prims = [], [], [], []
+    shells = np.unique(q[pick].ravel())
+    row = {}
+    for s in shells:
+        k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
+        row[s] = len(centre)
+        for ci, c in enumerate(COMPONENTS[int(sb.l[s])]):
+            centre.append(sb.centre[s]); lmn.append(c); cnorm.append(sb.comp_scale[s, ci])
+            prims.append(list(zip(sb.coef[k0:k1], sb.expo[k0:k1], np.ones(k1 - k0))))
+    table = oracle.FunctionTable(np.array(centre), np.array(lmn), np.array(cnorm), prims)
+    for i in pick:
+        a, b, c, d = q[i]
+        n = [len(COMPONENTS[int(sb.l[x])]) for x in (a, b, c, d)]
+        fq = np.array([(row[a] + w, row[b] + x, row[c] + y, row[d] + z) for w in range(n[0])
+                       for x in range(n[1]) for y in range(n[2]) for z in range(n[3])])
+        ref = oracle.eri_functions(table, fq, boys_mode=1)
+        got = host[off[i]:off[i + 1]]
+        assert np.max(np.abs(got - ref)) <= 1e-13 + 1e-11 * np.max(np.abs(ref)), i
