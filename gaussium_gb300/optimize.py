@@ -126,14 +126,17 @@ class NelderMead:
         return simplex, [self.energy(p) for p in simplex]
 
 
-def optimize_bfgs(mol, basis="6-31G", gtol=1e-5, max_iter=500, energy_gradient=None):
+def optimize_bfgs(mol, basis="6-31G", gtol=1e-5, max_iter=500, energy_gradient=None,
+                  method="L-BFGS-B"):
     """Gradient-driven minimisation in the Nelder-Mead driver's internal frame (first nucleus
     at the origin, second on z, third in the yz plane: 3N-6 variables, so the six zero
     modes of overall translation and rotation are not searched).  The energy is invariant
     under those motions, so the derivative with respect to each free variable is the
     Cartesian gradient component that variable sets.  Returns (energy, coordinates,
     evaluations, max |gradient| at the end).  ``energy_gradient(molecule) -> (E, dE/dR)``
-    defaults to the RHF energy and analytic gradient in ``basis``."""
+    defaults to the RHF energy and analytic gradient in ``basis``.  ``method`` is a scipy
+    quasi-Newton method: "L-BFGS-B" (default; its initial Hessian is scaled from the first
+    step, which matters for the soft intermolecular modes of clusters) or "BFGS"."""
     from scipy.optimize import minimize
     symbols = mol.symbols
     frame = NelderMead(symbols, mol.coords, None)
@@ -149,5 +152,9 @@ def optimize_bfgs(mol, basis="6-31G", gtol=1e-5, max_iter=500, energy_gradient=N
         return e, frame._vector(np.asarray(g))
 
     x0 = frame._vector(frame.frame)
-    r = minimize(fg, x0, jac=True, method="BFGS", options={"gtol": gtol, "maxiter": max_iter})
+    if method == "L-BFGS-B":
+        opts = {"gtol": gtol, "maxiter": max_iter, "maxcor": 30, "ftol": 1e-14}
+    else:
+        opts = {"gtol": gtol, "maxiter": max_iter}
+    r = minimize(fg, x0, jac=True, method=method, options=opts)
     return float(r.fun), frame.coordinates(r.x), count[0], float(np.abs(r.jac).max())
