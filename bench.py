@@ -656,7 +656,7 @@ def run_optimize(args, rank, world):
     e_n, x_n = nm.optimize()
     t_n = time.perf_counter() - t0
     line = {
-        "metric": METRIC, "value": t_b, "unit": "s (BFGS geometry optimisation)",
+        "metric": METRIC, "value": t_b, "unit": "s (gradient-driven geometry optimisation)",
         "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": t_b * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded (H2O)4, 0.1 A perturbation)",
