@@ -423,6 +423,16 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
             shifted = ~done
             sigma = level_shift * shifted.double()
             F = F + sigma[:, None, None] * (Sb - 0.5 * Sb @ Pb @ Sb)
-        _, C_new = diag(F)
-        C = torch.where(done[:, None, None], C, C_new)
+        # diagonalise only the molecules still iterating (a batched eigh of every molecule
+        # would dominate the late iterations, when few are left)
+        act = torch.nonzero(~done).flatten()
+        if act.numel() == B:
+            _, C = diag(F)
+        else:
+            Xa = X.index_select(0, act)
+            Fo = Xa.transpose(1, 2) @ F.index_select(0, act) @ Xa + \
+                torch.diag_embed(big.index_select(0, act))
+            _, ca = torch.linalg.eigh(Fo)
+            C = C.clone()
+            C.index_copy_(0, act, Xa @ ca)
     return energies, it, done.cpu().numpy(), Pb
