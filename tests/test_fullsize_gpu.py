@@ -54,8 +54,7 @@ def test_fp32_close_to_fp64_at_full_size(gpu_lib, full):
     assert bool(torch.isfinite(o32).all())
     err = (o32 - out).abs() / out.abs().max()
     assert float(err.max()) < 5e-2
-    k = max(1, err.numel() // 1000)
-    assert float(torch.topk(err, k).values[-1]) < 1e-4        # 99.9 % of the elements
+    assert int((err > 1e-4).sum()) <= err.numel() // 1000     # 99.9 % of the elements
 
 
 def test_sampled_quartets_match_oracle(gpu_lib, full):
