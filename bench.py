@@ -72,15 +72,19 @@ def parse():
 
 
 # ---------------------------------------------------------------------- distributed plumbing
-def dist_init(args):
+def dist_init(args=None):
+    """Replicas: one process per GPU (torchrun env), NCCL on GPUs; the same plumbing runs
+    over gloo on CPU for the tests.  No collective is on the data path: ranks only meet at
+    barriers and for the max-over-ranks time."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        backend = os.environ.get("GS_DIST_BACKEND") or ("nccl" if torch.cuda.is_available() else "gloo")
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
     return rank, world
 
 
@@ -95,7 +99,8 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
