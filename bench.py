@@ -463,25 +463,30 @@ def run_batch(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     build.build()
     mols = [molecules.random_chain(1000 * rank + s) for s in range(args.molecules)]
-    t0 = time.perf_counter()
-    eng = batch.BatchedRHF(mols)
-    torch.cuda.synchronize()
-    t_setup = time.perf_counter() - t0
     opts = dict(mixed_cut=args.mixed_cut, screen_thr=1e-12, incremental=True, guess=args.guess)
+    # outside the timed region: kernel loading, the per-element atomic densities of the
+    # guess, and the kernel forms, tuned on 32 other molecules of the same kind
+    other = batch.BatchedRHF([molecules.random_chain(100000 + s) for s in range(32)])
     if args.guess == "sad":
         from gaussium_gb300 import guess
         for sym in sorted(set(s for m in mols for s in m.symbols)):
-            guess.element_density(sym, "6-31G*")          # per-element atoms, once
+            guess.element_density(sym, "6-31G*")
     forms = {}
     if not args.no_tune:
         from gaussium_gb300 import autotune
-        chosen = eng.tune(reps=2)
+        chosen = other.tune(reps=2)
         forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
                  for (c, p), r in chosen.items()}
-    eng.run(max_iter=2, **opts)              # warm-up and graph capture
+    other.run(max_iter=2, **opts)
+    del other
     torch.cuda.synchronize()
+    # timed: everything per batch -- one-electron integrals, pair records, Schwarz bounds,
+    # task lists, graph capture and the SCF of all molecules
     with ClockSampler() as clk:
         t0 = time.perf_counter()
+        eng = batch.BatchedRHF(mols)
+        torch.cuda.synchronize()
+        t_setup = time.perf_counter() - t0
         e, iters = eng.run(threshold=1e-10, **opts)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
@@ -520,7 +525,11 @@ def run_batch(args, rank, world):
         "config": {"workload": f"batched RHF of {len(mols)} molecules, 6-31G*, "
                                f"{int(eng.nbf.sum())} functions in total",
                    "scf_iterations": iters, "converged": int(conv_mixed.sum()),
-                   "unique_quartets": int(eng.ntasks), "setup_s": t_setup,
+                   "unique_quartets": int(eng.ntasks),
+                   "timed": "engine set-up (one-electron integrals, pairs, Schwarz, tasks) + "
+                            "graph capture + SCF",
+                   "setup_s": t_setup, "scf_s": dt - t_setup,
+                   "kernel_forms_tuned_on": "32 other molecules of the same kind",
                    "mixed_cut": args.mixed_cut, "screen_thr": 1e-12, "incremental_reset_every": 8,
                    "guess": args.guess,
                    "final_energy": "one full FP64 build at the converged densities",

@@ -70,14 +70,20 @@ __device__ __forceinline__ double ipow(double x, int n) {
     return r;
 }
 
+// One thread per (shell pair, part): part == natom computes S and T of the pair (plain
+// stores into both (a,b) and (b,a)); part < natom adds nucleus `part`'s attraction to V
+// (V zeroed first; a diagonal pair adds only to (a,b) since its loop covers both orders).
+// Neighbouring threads share a pair, so a warp runs uniform primitive loops.
 __global__ void k_one_electron(gs::ShellView sv, const double* __restrict__ comp_scale,
                                const int* __restrict__ func_off, int npairs,
                                const int* __restrict__ pair_shells, int nbf, int natom,
                                const double* __restrict__ atom_xyz,
                                const double* __restrict__ atom_z, double* S, double* T,
                                double* V) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= npairs) return;
+    const int parts = natom + 1;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)npairs * parts) return;
+    const int t = (int)(tid / parts), part = (int)(tid % parts);
     const int sa = pair_shells[2 * t], sb = pair_shells[2 * t + 1];
     const int la = sv.l[sa], lb = sv.l[sb];
     const int na = ncart(la), nb = ncart(lb);
@@ -99,100 +105,100 @@ __global__ void k_one_electron(gs::ShellView sv, const double* __restrict__ comp
                 PA[d] = P[d] - A[d];
                 PB[d] = P[d] - B[d];
             }
-            // 1D overlaps s[d][ia][ib], ia <= la, ib <= lb + 2 (kinetic shift)
-            double s1[3][kMaxL + 1][kMaxL + 3];
-            for (int d = 0; d < 3; ++d) {
-                s1[d][0][0] = 1.0;
-                for (int b = 1; b <= lb + 2; ++b)
-                    s1[d][0][b] = PB[d] * s1[d][0][b - 1] + (b > 1 ? (b - 1) * i2p * s1[d][0][b - 2] : 0.0);
-                for (int a = 1; a <= la; ++a)
-                    for (int b = 0; b <= lb + 2; ++b) {
-                        double v = PA[d] * s1[d][a - 1][b];
-                        if (a > 1) v += (a - 1) * i2p * s1[d][a - 2][b];
-                        if (b > 0) v += b * i2p * s1[d][a - 1][b - 1];
-                        s1[d][a][b] = v;
-                    }
-            }
-            const double pref = Kab * ip * sqrt(ip) * 5.568327996831708;  // pi^{3/2}
-            for (int ia = 0; ia < na; ++ia) {
-                int ax, ay, az;
-                cart_of(la, ia, ax, ay, az);
-                const int a3[3] = {ax, ay, az};
-                for (int ib = 0; ib < nb; ++ib) {
-                    int bx, by, bz;
-                    cart_of(lb, ib, bx, by, bz);
-                    const int b3[3] = {bx, by, bz};
-                    double sx[3], tx[3];
-                    for (int d = 0; d < 3; ++d) {
-                        const int a = a3[d], b = b3[d];
-                        sx[d] = s1[d][a][b];
-                        // -1/2 d^2/dx^2 on x^b exp(-be x^2)
-                        tx[d] = be * (2 * b + 1) * s1[d][a][b] - 2.0 * be * be * s1[d][a][b + 2] -
-                                (b >= 2 ? 0.5 * b * (b - 1) * s1[d][a][b - 2] : 0.0);
-                    }
-                    s_acc[ia * nb + ib] += pref * sx[0] * sx[1] * sx[2];
-                    t_acc[ia * nb + ib] += pref * (tx[0] * sx[1] * sx[2] + sx[0] * tx[1] * sx[2] +
-                                                   sx[0] * sx[1] * tx[2]);
-                }
-            }
-            // nuclear attraction: (e|A|0)^(m), e up to L, then HRR
-            const double vpref = Kab * ip * 6.283185307179586;   // 2 pi / p
-            for (int c = 0; c < natom; ++c) {
-                const double* C = atom_xyz + 3 * c;
-                const double PC[3] = {P[0] - C[0], P[1] - C[1], P[2] - C[2]};
-                const double u = p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]);
-                double F[2 * kMaxL + 1];
-                switch (L) {
-                    case 0: gs::boys<0, double>(u, 1.0, F); break;
-                    case 1: gs::boys<1, double>(u, 1.0, F); break;
-                    case 2: gs::boys<2, double>(u, 1.0, F); break;
-                    case 3: gs::boys<3, double>(u, 1.0, F); break;
-                    default: gs::boys<4, double>(u, 1.0, F); break;
-                }
-                // th[m][lbase(Le)+k]
-                double th[2 * kMaxL + 1][35];
-                for (int m = 0; m <= L; ++m) th[m][0] = F[m];
-                for (int Le = 1; Le <= L; ++Le)
-                    for (int k = 0; k < ncart(Le); ++k) {
-                        int e[3];
-                        cart_of(Le, k, e[0], e[1], e[2]);
-                        int d = e[0] ? 0 : (e[1] ? 1 : 2);
-                        int e1[3] = {e[0], e[1], e[2]};
-                        e1[d] -= 1;
-                        const int i1 = lbase(Le - 1) + cart_index(e1[0], e1[1], e1[2]);
-                        int i2 = -1;
-                        if (e1[d] > 0) {
-                            int e2[3] = {e1[0], e1[1], e1[2]};
-                            e2[d] -= 1;
-                            i2 = lbase(Le - 2) + cart_index(e2[0], e2[1], e2[2]);
+            if (part == natom) {
+                // 1D overlaps s[d][ia][ib], ia <= la, ib <= lb + 2 (kinetic shift)
+                double s1[3][kMaxL + 1][kMaxL + 3];
+                for (int d = 0; d < 3; ++d) {
+                    s1[d][0][0] = 1.0;
+                    for (int b = 1; b <= lb + 2; ++b)
+                        s1[d][0][b] = PB[d] * s1[d][0][b - 1] + (b > 1 ? (b - 1) * i2p * s1[d][0][b - 2] : 0.0);
+                    for (int a = 1; a <= la; ++a)
+                        for (int b = 0; b <= lb + 2; ++b) {
+                            double v = PA[d] * s1[d][a - 1][b];
+                            if (a > 1) v += (a - 1) * i2p * s1[d][a - 2][b];
+                            if (b > 0) v += b * i2p * s1[d][a - 1][b - 1];
+                            s1[d][a][b] = v;
                         }
-                        for (int m = 0; m <= L - Le; ++m) {
-                            double v = PA[d] * th[m][i1] - PC[d] * th[m + 1][i1];
-                            if (i2 >= 0) v += e1[d] * i2p * (th[m][i2] - th[m + 1][i2]);
-                            th[m][lbase(Le) + k] = v;
-                        }
-                    }
-                // transfer to the ket centre: (x - B)^b = sum_k C(b,k) (x - A)^k AB^(b-k)
-                const double zc = atom_z[c];
+                }
+                const double pref = Kab * ip * sqrt(ip) * 5.568327996831708;  // pi^{3/2}
                 for (int ia = 0; ia < na; ++ia) {
                     int ax, ay, az;
                     cart_of(la, ia, ax, ay, az);
+                    const int a3[3] = {ax, ay, az};
                     for (int ib = 0; ib < nb; ++ib) {
                         int bx, by, bz;
                         cart_of(lb, ib, bx, by, bz);
-                        // expand (a|b) = sum over binomial transfer: prod_d sum_k C(b_d,k) AB_d^(b_d-k) (a+k e_d|
-                        double val = 0.0;
-                        for (int kx = 0; kx <= bx; ++kx)
-                            for (int ky = 0; ky <= by; ++ky)
-                                for (int kz = 0; kz <= bz; ++kz) {
-                                    const double cx = (bx == 2 && kx == 1 ? 2.0 : 1.0) * pow(AB[0], bx - kx);
-                                    const double cy = (by == 2 && ky == 1 ? 2.0 : 1.0) * pow(AB[1], by - ky);
-                                    const double cz = (bz == 2 && kz == 1 ? 2.0 : 1.0) * pow(AB[2], bz - kz);
-                                    const int ex = ax + kx, ey = ay + ky, ez = az + kz;
-                                    val += cx * cy * cz * th[0][lbase(ex + ey + ez) + cart_index(ex, ey, ez)];
-                                }
-                        v_acc[ia * nb + ib] -= zc * vpref * val;
+                        const int b3[3] = {bx, by, bz};
+                        double sx[3], tx[3];
+                        for (int d = 0; d < 3; ++d) {
+                            const int a = a3[d], b = b3[d];
+                            sx[d] = s1[d][a][b];
+                            // -1/2 d^2/dx^2 on x^b exp(-be x^2)
+                            tx[d] = be * (2 * b + 1) * s1[d][a][b] - 2.0 * be * be * s1[d][a][b + 2] -
+                                    (b >= 2 ? 0.5 * b * (b - 1) * s1[d][a][b - 2] : 0.0);
+                        }
+                        s_acc[ia * nb + ib] += pref * sx[0] * sx[1] * sx[2];
+                        t_acc[ia * nb + ib] += pref * (tx[0] * sx[1] * sx[2] + sx[0] * tx[1] * sx[2] +
+                                                       sx[0] * sx[1] * tx[2]);
                     }
+                }
+                continue;
+            }
+            // nuclear attraction of nucleus `part`: (e|A|0)^(m), e up to L, then transfer
+            const double vpref = Kab * ip * 6.283185307179586;   // 2 pi / p
+            const double* C = atom_xyz + 3 * part;
+            const double PC[3] = {P[0] - C[0], P[1] - C[1], P[2] - C[2]};
+            const double u = p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]);
+            double F[2 * kMaxL + 1];
+            switch (L) {
+                case 0: gs::boys<0, double>(u, 1.0, F); break;
+                case 1: gs::boys<1, double>(u, 1.0, F); break;
+                case 2: gs::boys<2, double>(u, 1.0, F); break;
+                case 3: gs::boys<3, double>(u, 1.0, F); break;
+                default: gs::boys<4, double>(u, 1.0, F); break;
+            }
+            // th[m][lbase(Le)+k]
+            double th[2 * kMaxL + 1][35];
+            for (int m = 0; m <= L; ++m) th[m][0] = F[m];
+            for (int Le = 1; Le <= L; ++Le)
+                for (int k = 0; k < ncart(Le); ++k) {
+                    int e[3];
+                    cart_of(Le, k, e[0], e[1], e[2]);
+                    int d = e[0] ? 0 : (e[1] ? 1 : 2);
+                    int e1[3] = {e[0], e[1], e[2]};
+                    e1[d] -= 1;
+                    const int i1 = lbase(Le - 1) + cart_index(e1[0], e1[1], e1[2]);
+                    int i2 = -1;
+                    if (e1[d] > 0) {
+                        int e2[3] = {e1[0], e1[1], e1[2]};
+                        e2[d] -= 1;
+                        i2 = lbase(Le - 2) + cart_index(e2[0], e2[1], e2[2]);
+                    }
+                    for (int m = 0; m <= L - Le; ++m) {
+                        double v = PA[d] * th[m][i1] - PC[d] * th[m + 1][i1];
+                        if (i2 >= 0) v += e1[d] * i2p * (th[m][i2] - th[m + 1][i2]);
+                        th[m][lbase(Le) + k] = v;
+                    }
+                }
+            const double zc = atom_z[part];
+            for (int ia = 0; ia < na; ++ia) {
+                int ax, ay, az;
+                cart_of(la, ia, ax, ay, az);
+                for (int ib = 0; ib < nb; ++ib) {
+                    int bx, by, bz;
+                    cart_of(lb, ib, bx, by, bz);
+                    // (x - B)^b = sum_k C(b,k) (x - A)^k AB^(b-k) per dimension
+                    double val = 0.0;
+                    for (int kx = 0; kx <= bx; ++kx)
+                        for (int ky = 0; ky <= by; ++ky)
+                            for (int kz = 0; kz <= bz; ++kz) {
+                                const double cx = (bx == 2 && kx == 1 ? 2.0 : 1.0) * pow(AB[0], bx - kx);
+                                const double cy = (by == 2 && ky == 1 ? 2.0 : 1.0) * pow(AB[1], by - ky);
+                                const double cz = (bz == 2 && kz == 1 ? 2.0 : 1.0) * pow(AB[2], bz - kz);
+                                const int ex = ax + kx, ey = ay + ky, ez = az + kz;
+                                val += cx * cy * cz * th[0][lbase(ex + ey + ez) + cart_index(ex, ey, ez)];
+                            }
+                    v_acc[ia * nb + ib] -= zc * vpref * val;
                 }
             }
         }
@@ -202,9 +208,13 @@ __global__ void k_one_electron(gs::ShellView sv, const double* __restrict__ comp
         for (int ib = 0; ib < nb; ++ib) {
             const double sc = comp_scale[6 * sa + ia] * comp_scale[6 * sb + ib];
             const int r = fa + ia, q = fb + ib;
-            S[r * nbf + q] = S[q * nbf + r] = sc * s_acc[ia * nb + ib];
-            T[r * nbf + q] = T[q * nbf + r] = sc * t_acc[ia * nb + ib];
-            V[r * nbf + q] = V[q * nbf + r] = sc * v_acc[ia * nb + ib];
+            if (part == natom) {
+                S[r * nbf + q] = S[q * nbf + r] = sc * s_acc[ia * nb + ib];
+                T[r * nbf + q] = T[q * nbf + r] = sc * t_acc[ia * nb + ib];
+            } else {
+                atomicAdd(V + r * nbf + q, sc * v_acc[ia * nb + ib]);
+                if (sa != sb) atomicAdd(V + q * nbf + r, sc * v_acc[ia * nb + ib]);
+            }
         }
 }
 
@@ -404,7 +414,11 @@ extern "C" int gs_one_electron(const double* centre, const int* l, const int* pr
         return GS_ERR_ARG;
     if (npairs == 0) return GS_OK;
     gs::ShellView sv{centre, l, prim_off, expo, coef};
-    k_one_electron<<<(npairs + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
+    const long long nthr = (long long)npairs * (natom + 1);
+    if (nthr > (long long)INT_MAX * 64) return GS_ERR_ARG;
+    if (cudaMemsetAsync(V, 0, sizeof(double) * (size_t)nbf * nbf, (cudaStream_t)stream) != cudaSuccess)
+        return GS_ERR_CUDA;
+    k_one_electron<<<(unsigned)((nthr + 63) / 64), 64, 0, (cudaStream_t)stream>>>(
         sv, comp_scale, func_off, npairs, pair_shells, nbf, natom, atom_xyz, atom_z, S, T, V);
     return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA;
 }

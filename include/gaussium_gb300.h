@@ -189,10 +189,11 @@ int gs_fock_jk_batched_mixed(int la, int lb, int lc, int ld, const void* pair_re
  * (integrals/boys_function.py:4-76). */
 int gs_boys_eval(int m, int precision, int n, const double* t, double* F, void* stream);
 
-/* K7 one-electron integrals over npairs shell pairs pair_shells[2*p] (any order of l):
- * overlap S, kinetic T (-1/2 nabla^2 on the ket) and nuclear attraction V of natom point
- * charges atom_z[] at atom_xyz[3*natom], written to both (a,b) and (b,a) blocks of the
- * nbf x nbf matrices.  Replaces OrbitalOverlapMatrix / KineticEnergyMatrix /
+/* K7 one-electron integrals over npairs shell pairs pair_shells[2*p] (any order of l; each
+ * unordered pair once): overlap S, kinetic T (-1/2 nabla^2 on the ket) and nuclear
+ * attraction V of natom point charges atom_z[] at atom_xyz[3*natom], written to both (a,b)
+ * and (b,a) blocks of the nbf x nbf matrices (V is zeroed first and summed over the nuclei,
+ * one thread per pair and nucleus).  Replaces OrbitalOverlapMatrix / KineticEnergyMatrix /
  * NuclearAttractionMatrix .create (matrixelements/orbital_overlap_matrix.py:15-27,
  * kinetic_energy_matrix.py:16-33, nuclear_attraction_matrix.py:16-29) and the integrals
  * they call (integrals/orbital_overlap_integral.py:16-36,
