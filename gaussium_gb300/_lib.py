@@ -25,8 +25,9 @@ _SIGS = {
     "gs_fock_jk": (I, [I, I, I, I, I, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, D, P]),
     "gs_fock_jk_batched": (I, [I, I, I, I, I, P, P, P, P, P, P, P, P, ctypes.c_longlong, I, P,
                                P, P, I, P, P, D, D, D, P]),
-    "gs_fock_jk_batched_mixed": (I, [I, I, I, I, P, P, P, P, P, P, P, P, P, ctypes.c_longlong, I, P,
-                                     P, P, I, P, P, D, D, P, ctypes.c_longlong, P]),
+    "gs_fock_jk_batched_mixed": (I, [I, I, I, I, P, P, P, P, P, P, P, P, P, P, P, P,
+                                     ctypes.c_longlong, I, P, P, P, I, P, P, D, D, P,
+                                     ctypes.c_longlong, P]),
     "gs_fock_jk_mixed_workspace": (ctypes.c_longlong, [I]),
     "gs_fock_jk_mixed": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, P,
                              ctypes.c_longlong, P]),

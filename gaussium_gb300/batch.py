@@ -72,6 +72,19 @@ class BatchedRHF:
                                         _lib.ptr(self.ds.comp_scale), len(idx), _lib.ptr(it),
                                         _lib.ptr(q), len(pairs), _lib.stream()), "gs_schwarz")
         self._tasks(q, pc, pair_mol, schwarz_thr)
+        # per-molecule shell-block tables of max |P| (density-weighted bounds): molecule m's
+        # ns_m x ns_m table starts at sbase[m]; every packed density element maps to its block
+        ns = np.array([sb.nshell for sb in sbs], dtype=np.int64)
+        sbase = np.concatenate([[0], np.cumsum(ns * ns)])
+        self.nblocks = int(sbase[-1])
+        self.mol_shell0 = t(np.array(shell0[:-1]), np.int32)
+        self.mol_nshell = t(ns, np.int32)
+        self.mol_sbase = t(sbase[:-1], np.int64)
+        blk = np.empty(self.mat_stride, dtype=np.int64)
+        for m, sb in enumerate(sbs):
+            fs = np.repeat(np.arange(sb.nshell), sb.nfunc)
+            blk[self.base[m]:self.base[m + 1]] = sbase[m] + (fs[:, None] * ns[m] + fs[None, :]).ravel()
+        self.block_of = torch.as_tensor(blk).to(self.dev)
         # one-electron matrices, orthogonalisers, padded index maps
         self.S, self.H = [], []
         for m, (mol, sb) in enumerate(zip(molecules, sbs)):
@@ -133,7 +146,9 @@ class BatchedRHF:
                     *cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
                     _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
                     _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
-                    _lib.ptr(dmax), self.mat_stride, e - s, base + s * 8, _lib.ptr(P), _lib.ptr(J), 1,
+                    _lib.ptr(dmax), _lib.ptr(self.mol_shell0), _lib.ptr(self.mol_nshell),
+                    _lib.ptr(self.mol_sbase), self.mat_stride, e - s, base + s * 8, _lib.ptr(P),
+                    _lib.ptr(J), 1,
                     _lib.ptr(P), _lib.ptr(K), thr, cut, _lib.ptr(self._ws), self._ws.numel(), st)
                 _lib.check(rc, f"gs_fock_jk_batched_mixed{cls}")
             return
@@ -171,13 +186,14 @@ class BatchedRHF:
     def fock_packed(self, P, precision=64, mixed_cut=None, screen_thr=0.0):
         """G = J - K/2 (padded [B, N, N], symmetric) for packed densities P, all molecules.
         With ``screen_thr`` a quartet is skipped when its Schwarz bound times the largest
-        |P| element of its molecule is below it; with ``mixed_cut`` the quartets whose such
-        bound is below the cut run in FP32 (FP64 accumulation)."""
+        |P| element of the six shell blocks it touches is below it; with ``mixed_cut`` the
+        quartets whose such bound is below the cut run in FP32 (FP64 accumulation)."""
         J = torch.zeros_like(P)
         K = torch.zeros_like(P)
         dmax = None
         if mixed_cut is not None or screen_thr > 0:
-            dmax = self.to_padded(P).abs().amax(dim=(1, 2)).contiguous()
+            dmax = torch.zeros(self.nblocks, dtype=torch.float64, device=self.dev)
+            dmax.scatter_reduce_(0, self.block_of, P.abs(), "amax", include_self=True)
         self._jk_launch(P, J, K, precision, mixed_cut, dmax, screen_thr)
         Jb, Kb = self.to_padded(J), self.to_padded(K)
         G = (Jb + Jb.transpose(1, 2)) - 0.5 * (Kb + Kb.transpose(1, 2))

@@ -121,12 +121,27 @@ __global__ void k_boys(int n, const double* __restrict__ t, double* __restrict__
 // into an FP64 list (est >= cut), an FP32 list (thr <= est < cut) and dropped (est < thr).
 // Warp-aggregated atomics keep each warp's survivors contiguous, so the primitive-count
 // order of the input survives approximately.
-// dmax: per (shell, shell) block of one molecule (nshell x nshell), or, with shell_mol,
-// one value per molecule (mol_dmax[shell_mol[shell]]).
+// Largest |P| over the six shell blocks a quartet (ab|cd) touches, from an ns x ns table.
+__device__ __forceinline__ double block_dmax(const double* __restrict__ d, int ns, int a, int b,
+                                             int c, int e) {
+    double dm = d[a * ns + b];
+    dm = fmax(dm, d[c * ns + e]);
+    dm = fmax(dm, d[a * ns + c]);
+    dm = fmax(dm, d[a * ns + e]);
+    dm = fmax(dm, d[b * ns + c]);
+    dm = fmax(dm, d[b * ns + e]);
+    return dm;
+}
+
+// dmax: per (shell, shell) block of one molecule (nshell x nshell); with shell_mol, per
+// molecule: either one value per molecule (mol_sbase null) or molecule m's own block table
+// at dmax + mol_sbase[m] over its mol_nshell[m] shells, numbered from mol_shell0[m].
 __global__ void k_partition(int ntask, const int2* __restrict__ tasks,
                             const gs::PairRec* __restrict__ pairs,
                             const double* __restrict__ dmax, int nshell,
-                            const int* __restrict__ shell_mol, double thr, double cut,
+                            const int* __restrict__ shell_mol,
+                            const int* __restrict__ mol_shell0, const int* __restrict__ mol_nshell,
+                            const long long* __restrict__ mol_sbase, double thr, double cut,
                             int2* __restrict__ out64, int2* __restrict__ out32,
                             int* __restrict__ counts) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,16 +152,14 @@ __global__ void k_partition(int ntask, const int2* __restrict__ tasks,
         const gs::PairRec B = pairs[task.x];
         const gs::PairRec K = pairs[task.y];
         double dm;
-        if (shell_mol) {
+        if (shell_mol && mol_sbase) {
+            const int m = shell_mol[B.sa], s0 = mol_shell0[m];
+            dm = block_dmax(dmax + mol_sbase[m], mol_nshell[m], B.sa - s0, B.sb - s0, K.sa - s0,
+                            K.sb - s0);
+        } else if (shell_mol) {
             dm = dmax[shell_mol[B.sa]];
         } else {
-            const int n = nshell;
-            dm = dmax[B.sa * n + B.sb];
-            dm = fmax(dm, dmax[K.sa * n + K.sb]);
-            dm = fmax(dm, dmax[B.sa * n + K.sa]);
-            dm = fmax(dm, dmax[B.sa * n + K.sb]);
-            dm = fmax(dm, dmax[B.sb * n + K.sa]);
-            dm = fmax(dm, dmax[B.sb * n + K.sb]);
+            dm = block_dmax(dmax, nshell, B.sa, B.sb, K.sa, K.sb);
         }
         const double est = (double)B.qmax * (double)K.qmax * dm;
         kind = est < thr ? 0 : (est >= cut ? 1 : 2);
@@ -378,7 +391,7 @@ int fock_jk_mixed_impl(int la, int lb, int lc, int ld, const void* pair_rec, con
     if (cudaMemsetAsync(counts, 0, 2 * sizeof(int), S(stream)) != cudaSuccess) return GS_ERR_CUDA;
     k_partition<<<(ntask + 255) / 256, 256, 0, S(stream)>>>(
         ntask, (const int2*)tasks, (const gs::PairRec*)pair_rec, shell_dmax, nshell, nullptr,
-        screen_thr, mixed_cut, l64, l32, counts);
+        nullptr, nullptr, nullptr, screen_thr, mixed_cut, l64, l32, counts);
     if (check_launch()) return GS_ERR_CUDA;
     gs::JKArgs a;
     a.pairs = (const gs::PairRec*)pair_rec;
@@ -469,15 +482,17 @@ int gs_fock_jk_mixed_noalloc(int la, int lb, int lc, int ld, const void* pair_re
 int gs_fock_jk_batched_mixed(int la, int lb, int lc, int ld, const void* pair_rec,
                              const void* prim64, const void* prim32, const double* comp_scale,
                              const int* func_off, const int* shell_mol, const long long* mol_base,
-                             const int* mol_n, const double* mol_dmax, long long mat_stride,
-                             int ntask, const int* tasks, const double* pj, double* j, int nk,
-                             const double* pk, double* k, double screen_thr, double mixed_cut,
-                             void* workspace, long long ws_bytes, void* stream) {
+                             const int* mol_n, const double* mol_dmax, const int* mol_shell0,
+                             const int* mol_nshell, const long long* mol_sbase,
+                             long long mat_stride, int ntask, const int* tasks, const double* pj,
+                             double* j, int nk, const double* pk, double* k, double screen_thr,
+                             double mixed_cut, void* workspace, long long ws_bytes, void* stream) {
     launch_fn f = find_class(la, lb, lc, ld);
     if (!f) return GS_ERR_CLASS;
     if (ntask < 0 || nk < 0 || nk > 1 || !pair_rec || !prim64 || !prim32 || !comp_scale ||
         !func_off || !shell_mol || !mol_base || !mol_n || !mol_dmax || (ntask > 0 && !tasks) ||
-        (!!pj != !!j) || (nk > 0 && (!pk || !k)) || mat_stride <= 0 || !workspace)
+        (!!pj != !!j) || (nk > 0 && (!pk || !k)) || mat_stride <= 0 || !workspace ||
+        (!!mol_sbase != !!mol_shell0) || (!!mol_sbase != !!mol_nshell))
         return GS_ERR_ARG;
     if (ws_bytes < gs_fock_jk_mixed_workspace(ntask)) return GS_ERR_NOMEM;
     if (ntask == 0) return GS_OK;
@@ -487,7 +502,7 @@ int gs_fock_jk_batched_mixed(int la, int lb, int lc, int ld, const void* pair_re
     if (cudaMemsetAsync(counts, 0, 2 * sizeof(int), S(stream)) != cudaSuccess) return GS_ERR_CUDA;
     k_partition<<<(ntask + 255) / 256, 256, 0, S(stream)>>>(
         ntask, (const int2*)tasks, (const gs::PairRec*)pair_rec, mol_dmax, 0, shell_mol,
-        screen_thr, mixed_cut, l64, l32, counts);
+        mol_shell0, mol_nshell, mol_sbase, screen_thr, mixed_cut, l64, l32, counts);
     if (check_launch()) return GS_ERR_CUDA;
     gs::JKArgs a;
     a.pairs = (const gs::PairRec*)pair_rec;

@@ -170,19 +170,23 @@ int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void
                        double screen_thr, double prec_lo, double prec_hi, void* stream);
 
 /* Mixed-precision, density-screened form of gs_fock_jk_batched: a partition kernel splits
- * the tasks by est = qmax_bra qmax_ket mol_dmax[molecule] into an FP64 list (est >=
- * mixed_cut), an FP32 list (screen_thr <= est < mixed_cut) and dropped tasks, in the
- * caller's workspace (ws_bytes >= gs_fock_jk_mixed_workspace(ntask)); the class launches
- * read the list lengths on the device and stride over them, so a batch whose densities
- * barely change (incremental builds near convergence) costs little more than the
- * partition.  Same replaced reference functions as gs_fock_jk. */
+ * the tasks by est = qmax_bra qmax_ket dmax into an FP64 list (est >= mixed_cut), an FP32
+ * list (screen_thr <= est < mixed_cut) and dropped tasks, in the caller's workspace
+ * (ws_bytes >= gs_fock_jk_mixed_workspace(ntask)); the class launches read the list lengths
+ * on the device and stride over them, so a batch whose densities barely change
+ * (incremental builds near convergence) costs little more than the partition.  dmax is the
+ * largest |P| over the six shell blocks of the quartet, from molecule m's own block table
+ * at mol_dmax + mol_sbase[m] (mol_nshell[m] x mol_nshell[m], shells numbered from
+ * mol_shell0[m]); with those three arrays null, mol_dmax[m] is one value per molecule.
+ * Same replaced reference functions as gs_fock_jk. */
 int gs_fock_jk_batched_mixed(int la, int lb, int lc, int ld, const void* pair_rec,
                              const void* prim64, const void* prim32, const double* comp_scale,
                              const int* func_off, const int* shell_mol, const long long* mol_base,
-                             const int* mol_n, const double* mol_dmax, long long mat_stride,
-                             int ntask, const int* tasks, const double* pj, double* j, int nk,
-                             const double* pk, double* k, double screen_thr, double mixed_cut,
-                             void* workspace, long long ws_bytes, void* stream);
+                             const int* mol_n, const double* mol_dmax, const int* mol_shell0,
+                             const int* mol_nshell, const long long* mol_sbase,
+                             long long mat_stride, int ntask, const int* tasks, const double* pj,
+                             double* j, int nk, const double* pk, double* k, double screen_thr,
+                             double mixed_cut, void* workspace, long long ws_bytes, void* stream);
 
 /* K2 Boys function F_0..F_m(t) (m <= 10) of n arguments t[] into F[n*(m+1)], in FP64 or
  * FP32 (results widened to FP64).  Replaces boys_function / boys_function_recursion
