@@ -65,7 +65,8 @@ def parse():
                     help="starting density of the batch workload's SCF")
     ap.add_argument("--batch-check", type=int, default=16,
                     help="molecules of the batch workload checked against single FP64 RHF")
-    ap.add_argument("--mixed-cut", type=float, default=1e-4)
+    ap.add_argument("--mixed-cut", type=float, default=1e-2,
+                    help="density-weighted bound below which a quartet runs in FP32 (water, batch)")
     ap.add_argument("--prim-screen", type=float, default=55.262,
                     help="drop primitive pairs with alpha*beta/p |AB|^2 above this (0: keep all)")
     return ap.parse_args()

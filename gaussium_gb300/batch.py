@@ -334,6 +334,22 @@ def batched_task_list(q, pair_class, pair_mol, nprim, thr, nclass, nmol):
     return segs, tasks.contiguous()
 
 
+_POOL = None
+
+
+def _host_eigh(Fo):
+    """Eigenvectors of a batch of symmetric matrices, one LAPACK call per matrix on a pool
+    of host threads (the calls release the interpreter lock)."""
+    global _POOL
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    if _POOL is None:
+        _POOL = ThreadPoolExecutor(max(1, os.cpu_count() or 1))
+    host = Fo.cpu().numpy()
+    vecs = list(_POOL.map(lambda a: np.linalg.eigh(a)[1], list(host)))
+    return torch.as_tensor(np.stack(vecs)).to(Fo.device)
+
+
 def padded_system(S_list, H_list, nocc, device):
     """Zero-padded [B, N, N] overlap and core Hamiltonian (identity overlap on the padding),
     the canonical orthogonaliser of each molecule (eigenvalues ascending, as the reference
@@ -360,7 +376,7 @@ def padded_system(S_list, H_list, nocc, device):
 
 def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold=1e-10,
                            max_iter=60, diis_subspace=8, level_shift=0.3, shift_after=30,
-                           shifted_error=1e-5, on_iteration=None, P_init=None):
+                           shifted_error=1e-5, on_iteration=None, P_init=None, eigh_on="host"):
     """Restricted SCF of B molecules at once over zero-padded [B, N, N] FP64 matrices.
 
     ``two_electron(P, active)`` returns G = J - K/2 for the padded densities; ``active``
@@ -384,10 +400,14 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
     B = Hb.shape[0]
     big = 1e6 * pad_orb
 
+    def eigh(Fo):
+        if eigh_on == "device":
+            return torch.linalg.eigh(Fo)[1]
+        return _host_eigh(Fo)
+
     def diag(F):
         Fo = X.transpose(1, 2) @ F @ X + torch.diag_embed(big)
-        e, c = torch.linalg.eigh(Fo)
-        return e, X @ c
+        return None, X @ eigh(Fo)
 
     _, C = diag(Hb)
     prev = torch.zeros(B, dtype=torch.float64, device=dev)
@@ -448,7 +468,7 @@ def batched_rhf_iterations(Sb, Hb, X, occ_mask, pad_orb, two_electron, threshold
             Xa = X.index_select(0, act)
             Fo = Xa.transpose(1, 2) @ F.index_select(0, act) @ Xa + \
                 torch.diag_embed(big.index_select(0, act))
-            _, ca = torch.linalg.eigh(Fo)
+            ca = eigh(Fo)
             C = C.clone()
             C.index_copy_(0, act, Xa @ ca)
     return energies, it, done.cpu().numpy(), Pb
