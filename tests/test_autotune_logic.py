@@ -1,0 +1,41 @@
+"""The autotuner's choice logic with the library calls replaced by fakes (no GPU): every
+class with several forms is timed in each and left on its fastest; single-form classes
+and empty segments are skipped."""
+import pytest
+
+from gaussium_gb300 import autotune
+
+
+def test_tune_picks_fastest_form(monkeypatch):
+    built = {(2, 1, 0, 0): [1, 2, 3], (1, 0, 0, 0): [1], (2, 2, 2, 2): [2, 3]}
+    cost = {((2, 1, 0, 0), 1): 3.0, ((2, 1, 0, 0), 2): 2.0, ((2, 1, 0, 0), 3): 1.0,
+            ((2, 2, 2, 2), 2): 1.0, ((2, 2, 2, 2), 3): 5.0}
+    state = {}
+    monkeypatch.setattr(autotune, "forms", lambda cls, prec: built[cls])
+    monkeypatch.setattr(autotune, "set_form", lambda cls, prec, v: state.__setitem__((cls, prec), v))
+    current = {}
+
+    def run_class(cls, prec):
+        current["c"] = (cls, state[(cls, prec)])
+
+    monkeypatch.setattr(autotune, "_time", lambda fn, reps: (fn(), cost[current["c"]])[1])
+    segs = [((2, 1, 0, 0), 0, 10), ((1, 0, 0, 0), 10, 20), ((2, 2, 2, 2), 20, 20)]
+    chosen = autotune.tune(segs, run_class, precisions=(64,), reps=1)
+    assert chosen[((2, 1, 0, 0), 64)]["form"] == 3
+    assert state[((2, 1, 0, 0), 64)] == 3
+    assert ((1, 0, 0, 0), 64) not in chosen          # one form only
+    assert ((2, 2, 2, 2), 64) not in chosen          # empty segment (min_tasks)
+
+
+def test_vrr_group_choice():
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                    "gaussium_gb300", "csrc"))
+    import gen_eri
+    # segments [noff, unused, cnt, nt, level, sync]: narrow levels want a group
+    narrow = [[0, 0, 4, 2, 1, 1], [1, 0, 6, 3, 2, 1]]
+    wide = [[0, 0, 64, 2, 1, 1], [2, 0, 96, 3, 2, 1]]
+    assert gen_eri.vrr_group(narrow, 20) > 1
+    assert gen_eri.vrr_group(wide, 20) == 1
+    assert gen_eri.vrr_group(narrow, 2000) == 1           # buffer budget
