@@ -323,13 +323,36 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
         const int at[4] = {a.shell_atom[B.sa], a.shell_atom[B.sb], a.shell_atom[K.sa],
                            a.shell_atom[K.sb]};
         double* dst = shared_sum ? sg : a.grad;
+        // per-centre contributions (D by translational invariance); when the whole warp is
+        // active and every lane has the same atom at a centre (neighbouring tasks usually
+        // share their bra pair), the warp sums first and one lane adds
+        double gc[4][3];
 #pragma unroll
-        for (int cen = 0; cen < 3; ++cen)
+        for (int x = 0; x < 3; ++x) {
+            gc[0][x] = g[x];
+            gc[1][x] = g[3 + x];
+            gc[2][x] = g[6 + x];
+            gc[3][x] = -(g[x] + g[3 + x] + g[6 + x]);
+        }
+        const unsigned act = __activemask();
+        const int lane = threadIdx.x & 31;
 #pragma unroll
-            for (int x = 0; x < 3; ++x) {
-                atomicAdd(dst + 3 * at[cen] + x, g[3 * cen + x]);
-                atomicAdd(dst + 3 * at[3] + x, -g[3 * cen + x]);
+        for (int cen = 0; cen < 4; ++cen) {
+            const bool uniform =
+                act == 0xffffffffu && __all_sync(act, at[cen] == __shfl_sync(act, at[cen], 0));
+            if (uniform) {
+#pragma unroll
+                for (int x = 0; x < 3; ++x) {
+                    double v = gc[cen][x];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(act, v, o);
+                    if (lane == 0) atomicAdd(dst + 3 * at[cen] + x, v);
+                }
+            } else {
+#pragma unroll
+                for (int x = 0; x < 3; ++x) atomicAdd(dst + 3 * at[cen] + x, gc[cen][x]);
             }
+        }
     }
     if (shared_sum) {
         __syncthreads();
