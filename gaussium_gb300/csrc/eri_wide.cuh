@@ -209,8 +209,18 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     const T dv3 = T(K.ABx), dv4 = T(K.ABy), dv5 = T(K.ABz);
     for (int lv = 0; lv < W::NHLEV; ++lv) {
         const int e1 = __ldg(hlev + lv + 1);
-        for (int e = __ldg(hlev + lv) + lane; e < e1; e += 32) {
-            const unsigned int a = __ldg(hop + 2 * e), b = __ldg(hop + 2 * e + 1);
+        int e = __ldg(hlev + lv) + lane;
+        unsigned int ra = 0, rb = 0;
+        if (e < e1) {
+            ra = __ldg(hop + 2 * e);
+            rb = __ldg(hop + 2 * e + 1);
+        }
+        for (; e < e1; e += 32) {
+            const unsigned int a = ra, b = rb;
+            if (e + 32 < e1) {                            // prefetch the next element
+                ra = __ldg(hop + 2 * (e + 32));
+                rb = __ldg(hop + 2 * (e + 32) + 1);
+            }
             const int d = b >> 16;
             const T dv = d == 0 ? dv0 : d == 1 ? dv1 : d == 2 ? dv2 : d == 3 ? dv3 : d == 4 ? dv4 : dv5;
             H[a & 0xffff] = fma(dv, H[b & 0xffff], H[a >> 16]);
