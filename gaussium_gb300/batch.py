@@ -338,16 +338,18 @@ _POOL = None
 
 
 def _host_eigh(Fo):
-    """Eigenvectors of a batch of symmetric matrices, one LAPACK call per matrix on a pool
-    of host threads (the calls release the interpreter lock)."""
+    """Eigenvectors of a batch of symmetric matrices on the host: torch's LAPACK path over
+    chunks of the batch on a pool of threads (the calls release the interpreter lock)."""
     global _POOL
     import os
     from concurrent.futures import ThreadPoolExecutor
+    nthr = max(1, os.cpu_count() or 1)
     if _POOL is None:
-        _POOL = ThreadPoolExecutor(max(1, os.cpu_count() or 1))
-    host = Fo.cpu().numpy()
-    vecs = list(_POOL.map(lambda a: np.linalg.eigh(a)[1], list(host)))
-    return torch.as_tensor(np.stack(vecs)).to(Fo.device)
+        _POOL = ThreadPoolExecutor(nthr)
+    host = Fo.cpu()
+    chunks = host.split(max(1, -(-host.shape[0] // nthr)))
+    vecs = list(_POOL.map(lambda c: torch.linalg.eigh(c)[1], chunks))
+    return torch.cat(vecs).to(Fo.device)
 
 
 def padded_system(S_list, H_list, nocc, device):
