@@ -259,16 +259,16 @@ int gs_one_electron_grad(const double* centre, const int* l, const int* prim_off
                          const double* atom_z, const double* density,
                          const double* energy_weighted, double* grad, void* stream);
 
-/* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks;
+/* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
+ * blocks*threads elements of the chosen type.  No reference counterpart. */
+int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);
 
 /* The same probe with only the first `lanes` (1..32) lanes of each warp running the FMA
  * chains: on GB300 the FP64 time does not shrink with fewer active lanes, which is why the
  * warp kernels fill narrow recursion levels with several primitive quartets.  No
  * reference counterpart. */
 int gs_fma_probe_lanes(int precision, int blocks, int threads, int iters, int lanes, void* sink,
-                       void* stream); sink must hold
- * blocks*threads elements of the chosen type.  No reference counterpart. */
-int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);
+                       void* stream);
 
 #ifdef __cplusplus
 }

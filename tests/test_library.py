@@ -11,13 +11,26 @@ from conftest import ROOT
 
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "gaussium_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gs_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|long long|const char\*)\s+(gs_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_entry_points():
     names = declared_symbols()
     for n in ("gs_pairs_build", "gs_eri_blocks", "gs_fock_jk", "gs_schwarz", "gs_boys_eval"):
         assert n in names
+
+
+@pytest.mark.parametrize("lang,cc", [("c", "gcc"), ("c++", "g++")])
+def test_header_compiles_as_c_and_cxx(lang, cc, tmp_path):
+    """A foreign-function binding (cgo, cffi, a C host) includes the header as plain C."""
+    if shutil.which(cc) is None:
+        pytest.skip(f"{cc} not available")
+    import subprocess
+    src = tmp_path / ("use." + ("c" if lang == "c" else "cpp"))
+    src.write_text('#include "gaussium_gb300.h"\nint main(void) { return gs_version() == 1 ? 0 : 1; }\n')
+    r = subprocess.run([cc, "-fsyntax-only", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
 
 
 @pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc not available")
