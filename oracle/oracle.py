@@ -226,3 +226,66 @@ def fock_blocked(hcore2, eri2, p2):
 def coulomb(eri, p):
     """RestrictedKohnShamHamiltonian.create, calculate_elst: J_ij = sum_ab P_ab (ij|ab)."""
     return np.einsum("ab,ijab->ij", p, eri)
+
+
+# ---------------------------------------------------------------------- AO -> MO transforms
+# Restatements of matrixelements/transformations.py (test infrastructure, like the rest of
+# this file): the reference's loops, in numpy.
+
+def molecular_orbitals(repulsion, coefficients):
+    """transformations.py:5-26: C^T X C over the last index pair for every (r, s), then over
+    the first pair for every (t, u)."""
+    x = np.array(repulsion, dtype=np.float64, copy=True)
+    c = np.asarray(coefficients)
+    n = c.shape[0]
+    for r in range(n):
+        for s in range(n):
+            x[r, s, :, :] = c.T @ x[r, s, :, :] @ c
+    for t in range(n):
+        for u in range(n):
+            x[:, :, t, u] = c.T @ x[:, :, t, u] @ c
+    return x
+
+
+def blocked_spin_basis_set(repulsion):
+    """transformations.py:29-70: alpha block first, beta second; (r s| only within a spin."""
+    h = repulsion.shape[0]
+    out = np.zeros((2 * h,) * 4)
+    for r in range(2 * h):
+        for s in range(2 * h):
+            if (r < h) == (s < h):
+                blk = repulsion[r % h, s % h]
+                out[r, s, :h, :h] = blk
+                out[r, s, h:, h:] = blk
+    return out
+
+
+def spin_basis_set(repulsion):
+    """transformations.py:73-92: interleaved spins, (rs|tu) = (r/2 s/2|t/2 u/2) when r, s share
+    a spin and t, u share a spin."""
+    n = 2 * repulsion.shape[0]
+    out = np.zeros((n,) * 4)
+    for r in range(n):
+        for s in range(n):
+            if r % 2 != s % 2:
+                continue
+            for t in range(n):
+                for u in range(n):
+                    if t % 2 == u % 2:
+                        out[r, s, t, u] = repulsion[r // 2, s // 2, t // 2, u // 2]
+    return out
+
+
+def spin_basis_anti_physicist(repulsion):
+    """transformations.py:114-136: <rs||tu> = [rt|su] d(r,t) d(s,u) - [ru|st] d(r,u) d(s,t)
+    over interleaved spins."""
+    n = 2 * repulsion.shape[0]
+    out = np.zeros((n,) * 4)
+    for r in range(n):
+        for s in range(n):
+            for t in range(n):
+                for u in range(n):
+                    a = (r % 2 == t % 2) * (s % 2 == u % 2) * repulsion[r // 2, t // 2, s // 2, u // 2]
+                    b = (r % 2 == u % 2) * (s % 2 == t % 2) * repulsion[r // 2, u // 2, s // 2, t // 2]
+                    out[r, s, t, u] = a - b
+    return out

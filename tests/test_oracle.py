@@ -87,3 +87,14 @@ def test_synthetic_quartets_and_normalisation():
     assert np.max(np.abs(g["hgp"][m] - g["os"][m])) < 1e-15
     m = ~np.isnan(g["cook"])
     assert np.max(np.abs(g["cook"][m] - g["os"][m])) < 5e-9
+
+
+def test_ao_to_mo_restatements_match_reference():
+    """The oracle's restatements of matrixelements/transformations.py against the
+    reference's own outputs (tests/golden/make_mo_golden.py)."""
+    g = golden("mo_transform")
+    mo = oracle.molecular_orbitals(g["ao"], g["coefficients"])
+    assert np.max(np.abs(mo - g["mo"])) < 1e-14
+    assert np.max(np.abs(oracle.spin_basis_set(g["mo"]) - g["spin"])) == 0.0
+    assert np.max(np.abs(oracle.blocked_spin_basis_set(g["mo"]) - g["blocked"])) == 0.0
+    assert np.max(np.abs(oracle.spin_basis_anti_physicist(g["mo"]) - g["anti"])) == 0.0
