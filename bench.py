@@ -53,12 +53,14 @@ def parse():
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the built-in kernel form of every class (no autotuning)")
     ap.add_argument("--cpu-sample", type=int, default=1024)
-    ap.add_argument("--workload", default="microbench", choices=["microbench", "water", "batch", "gradient", "optimize"])
+    ap.add_argument("--workload", default="microbench", choices=["microbench", "water", "batch", "gradient", "optimize", "mo"])
     ap.add_argument("--nm-evals", type=int, default=4000,
                     help="energy evaluations the Nelder-Mead comparison may spend")
     ap.add_argument("--fd-coords", type=int, default=72)
     ap.add_argument("--molecules", type=int, default=256)
     ap.add_argument("--waters", type=int, default=16)
+    ap.add_argument("--mo-waters", type=int, default=6,
+                    help="water molecules of the AO->MO workload (13 6-31G functions each)")
     ap.add_argument("--optimizer", default="L-BFGS-B", choices=["L-BFGS-B", "BFGS"],
                     help="quasi-Newton method of the geometry-optimisation workload")
     ap.add_argument("--guess", default="sad", choices=["core", "sad"],
@@ -689,6 +691,154 @@ def run_optimize(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------- AO -> MO transform
+def hbm_peak():
+    """Measured HBM copy bandwidth of this GPU type (GB/s) and where it came from."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def run_mo(args, rank, world):
+    """AO -> MO four-index transform and spin-orbital expansion of (H2O)n / 6-31G with a
+    seeded orthogonal coefficient matrix (the operation count does not depend on its
+    values).  One step = molecular_orbitals (four FP64 GEMM quarter transforms) followed by
+    spin_basis_anti_physicist (the gs_spin_expand kernel), on device-resident tensors.
+    The tensor has the pair symmetries of real integrals, so the transform takes its
+    pair-packed form (about 4 n^5 GEMM flops).  ``roofline`` is the spin-orbital kernel's:
+    17 n^4 doubles per launch (16 n^4 written, n^4 read) over its CUDA-event time."""
+    import torch
+    from gaussium_gb300 import _lib, build, molecules, transform
+    from gaussium_gb300.dropin import dense_eri
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    build.build()
+    L = _lib.lib()
+    mol = molecules.water_cluster(args.mo_waters, seed=args.mo_waters)
+    sb = molecules.shell_basis(mol, "6-31G")
+    n = sb.nbf
+    ao = dense_eri(sb)
+    rng = np.random.default_rng(args.seed)
+    c_host, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    c = torch.tensor(c_host, device="cuda")
+    spin = torch.empty((2 * n,) * 4, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def expand(mo, mode):
+        _lib.check(L.gs_spin_expand(_lib.ptr(mo), n, mode, _lib.ptr(spin), _lib.stream()),
+                   "gs_spin_expand")
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    for _ in range(max(3, args.warmup)):
+        expand(transform.transform_device(ao, c), transform.SPIN_ANTI_PHYSICIST)
+    torch.cuda.synchronize()
+    t_tr, t_sp = [], []
+    with ClockSampler() as clk:
+        e_start = ev()
+        e_start.record(st)
+        for _ in range(args.steps):
+            a, b, d = ev(), ev(), ev()
+            a.record(st)
+            mo = transform.transform_device(ao, c)
+            b.record(st)
+            expand(mo, transform.SPIN_ANTI_PHYSICIST)
+            d.record(st)
+            t_tr.append((a, b))
+            t_sp.append((b, d))
+            del mo
+        e_end = ev()
+        e_end.record(st)
+        torch.cuda.synchronize()
+    ms_total = e_start.elapsed_time(e_end)
+    ms_tr = float(np.mean([x.elapsed_time(y) for x, y in t_tr]))
+    ms_sp = float(np.mean([x.elapsed_time(y) for x, y in t_sp]))
+    # each spin mode alone (inputs 16x smaller than the output, which is > L2)
+    mo = transform.transform_device(ao, c)
+    per_mode = {}
+    for mode, name in ((0, "spin_basis_set"), (1, "blocked_spin_basis_set"),
+                       (2, "spin_basis_anti_physicist")):
+        expand(mo, mode)
+        a, b = ev(), ev()
+        a.record(st)
+        for _ in range(args.steps):
+            expand(mo, mode)
+        b.record(st)
+        b.synchronize()
+        per_mode[name] = a.elapsed_time(b) / args.steps
+    spin_bytes = 17 * n ** 4 * 8           # (2n)^4 written + n^4 read
+    peak, peak_kind = hbm_peak()
+    achieved = spin_bytes / (ms_sp * 1e-3) / 1e9
+    # GEMM flops of the pair-packed transform the symmetric tensor takes: C^T X C over
+    # P = n(n+1)/2 pairs in each half, 2 GEMMs of 2 n^3 flops per pair and half
+    npair = n * (n + 1) // 2
+    flops = 8.0 * npair * n ** 3
+    fp64 = fma_peak(64)
+    # end to end through the host-array API: AO tensor in, MO tensor back (molecular_orbitals),
+    # then the MO tensor in and the spin-orbital tensor back (spin_basis_anti_physicist)
+    ao_host = ao.cpu().numpy()
+    e2e = []
+    for k in range(args.warmup + args.steps):
+        inp = ao_host.copy()            # molecular_orbitals overwrites its argument
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mo_h = transform.molecular_orbitals(inp, c_host)
+        sp_h = transform.spin_basis_anti_physicist(mo_h)
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e.append(t1 - t0)
+        del sp_h
+    h2d = (n ** 4 + n * n) * 8 + n ** 4 * 8
+    d2h = n ** 4 * 8 + 16 * n ** 4 * 8
+    # CPU baseline: the oracle's restatement of transformations.py:5-26 on the same
+    # tensor (numpy matrix products over index pairs), and its spin-orbital expansion
+    # (pure Python element loops) on a 6-orbital sample, scaled per output element
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        t0 = time.perf_counter()
+        oracle.molecular_orbitals(ao_host, c_host)
+        t_cpu_tr = time.perf_counter() - t0
+        small = np.asarray(mo.cpu().numpy()[:6, :6, :6, :6])
+        t0 = time.perf_counter()
+        oracle.spin_basis_anti_physicist(small)
+        t_cpu_sp = (time.perf_counter() - t0) * (n / 6) ** 4
+        cpu = {"value": (t_cpu_tr + t_cpu_sp) * 1e3, "unit": "ms per step", "cores": 1,
+               "kind": "port",
+               "sample": f"transform: the full {n}-function tensor; spin expansion: 6 orbitals "
+                         f"(1296 spin-orbital elements per orbital^4), scaled by (n/6)^4",
+               "transform_ms": t_cpu_tr * 1e3, "spin_ms_scaled": t_cpu_sp * 1e3}
+    line = {
+        "metric": "AO->MO transform + spin-orbital expansion time", "value": ms_tr + ms_sp,
+        "unit": "ms per step", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_total / args.steps, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded water cluster, seeded C)",
+        "config": {"workload": f"AO->MO (H2O){args.mo_waters}/6-31G, {n} functions, "
+                               f"spin-orbital tensor (2*{n})^4",
+                   "l2": "output (2n)^4 doubles far larger than L2"},
+        "transform_ms": ms_tr, "transform_form": "pair-packed (tensor symmetric in a<->b, c<->d)",
+        "transform_gemm_gflop": flops / 1e9, "transform_tflops": flops / (ms_tr * 1e-3) / 1e12,
+        "transform_frac_of_fp64_fma_peak": flops / (ms_tr * 1e-3) / 1e12 / fp64,
+        "fp64_fma_peak_tflops": fp64,
+        "spin_expand_ms": ms_sp, "spin_expand_ms_per_mode": per_mode,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_spin_expand (spin_basis_anti_physicist)",
+                     "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": float(np.mean(e2e)) * 1e3, "unit": "ms per step",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps,
+        "library_launches_per_step": "4 cuBLAS DGEMM calls (the quarter transforms)",
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------- reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -730,6 +880,8 @@ def main():
         run_gradient(args, rank, world)
     elif args.workload == "optimize":
         run_optimize(args, rank, world)
+    elif args.workload == "mo":
+        run_mo(args, rank, world)
     else:
         run_gpu(args, rank, world)
     if world > 1:

@@ -45,6 +45,8 @@ _SIGS = {
     "gs_eri_grad_variants": (I, [I, I, I, I]),
     "gs_set_eri_grad_variant": (I, [I, I, I, I, I]),
     "gs_one_electron_grad": (I, [P, P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),
+    "gs_spin_expand": (I, [P, I, I, P, P]),
+    "gs_spin_expand_max_orbitals": (I, []),
 }
 
 

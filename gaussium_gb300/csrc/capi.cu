@@ -213,7 +213,8 @@ const char* gs_status_string(int status) {
         case GS_ERR_NOMEM: return "workspace too small";
         case GS_ERR_LIMIT:
             return "task count exceeds the fixed workspace of the no-allocation entry point "
-                   "(gs_fock_jk_mixed_noalloc_max_tasks)";
+                   "(gs_fock_jk_mixed_noalloc_max_tasks), or orbital count exceeds "
+                   "gs_spin_expand_max_orbitals";
         default: return "unknown status";
     }
 }

@@ -170,15 +170,38 @@ class _BasisOnly:
         return self.basis_set_array
 
 
+def _mo_from_source(repulsion, coefficients):
+    """``molecular_orbitals`` for callers of an installed package, whose
+    ``hartree_fock.repulsion`` is the basis-function list (``_BasisOnly``): the MO tensor
+    is built from the shells on the device; a dense tensor goes through the drop-in."""
+    from . import transform
+    from .basis import ShellBasis
+    if isinstance(repulsion, (list, tuple)):
+        sb = ShellBasis.from_functions(repulsion)
+        return transform.mo_integrals(sb, coefficients).cpu().numpy()
+    return transform.molecular_orbitals(repulsion, coefficients)
+
+
+# post-SCF modules of the reference and the transform names each imports
+# (moellerplesset/moeller_plesset.py:2, coupledcluster/coupled_cluster.py:5-6,
+# tdhartreefock/td_hartree_fock.py:3-4)
+_POST_SCF = (("moellerplesset", "moeller_plesset"), ("coupledcluster", "coupled_cluster"),
+             ("tdhartreefock", "td_hartree_fock"))
+
+
 def install(gaussium, **options):
     """Route a loaded reference package's SCF through this engine: in
     ``gaussium.hartreefock.hartree_fock`` the tensor builder becomes ``_BasisOnly``, the
     three Fock builders become the GPU drop-ins, and the spin-blocking of the tensor
     (``blocked_spin_basis_set``) passes the basis list through (the blocked drop-in builds
     the spin blocks itself); in ``gaussium.kohnsham.kohn_sham`` the Kohn-Sham Hamiltonian
-    becomes its drop-in.  ``options`` (e.g. ``mixed_cut``, ``incremental``) go to every
-    builder.  Returns the replaced originals, keyed by module attribute, for undoing."""
+    becomes its drop-in.  In the post-SCF modules (MP2, CCSD, TDHF) that are loaded,
+    ``molecular_orbitals`` builds the MO tensor from the basis list on the device and
+    ``spin_basis_set`` / ``spin_basis_anti_physicist`` become the GPU drop-ins.
+    ``options`` (e.g. ``mixed_cut``, ``incremental``) go to every builder.  Returns the
+    replaced originals, keyed by module attribute, for undoing."""
     import functools
+    from . import transform
     hf = gaussium.hartreefock.hartree_fock
     swaps = [(hf, "TwoElectronRepulsionMatrixOS", _BasisOnly),
              (hf, "FockMatrixRestricted", functools.partial(FockMatrixRestrictedGPU, **options)),
@@ -190,6 +213,15 @@ def install(gaussium, **options):
     if ks is not None:
         swaps.append((ks, "RestrictedKohnShamHamiltonian",
                       functools.partial(RestrictedKohnShamHamiltonianGPU, **options)))
+    for pkg, modname in _POST_SCF:
+        mod = getattr(getattr(gaussium, pkg, None), modname, None)
+        if mod is None:
+            continue
+        for name, new in (("molecular_orbitals", _mo_from_source),
+                          ("spin_basis_set", transform.spin_basis_set),
+                          ("spin_basis_anti_physicist", transform.spin_basis_anti_physicist)):
+            if hasattr(mod, name):
+                swaps.append((mod, name, new))
     originals = {}
     for mod, name, new in swaps:
         originals[(mod.__name__, name)] = getattr(mod, name)

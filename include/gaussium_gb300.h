@@ -259,6 +259,19 @@ int gs_one_electron_grad(const double* centre, const int* l, const int* prim_off
                          const double* atom_z, const double* density,
                          const double* energy_weighted, double* grad, void* stream);
 
+/* Spin-orbital expansion of an MO-basis two-electron tensor on the device: mo is h^4
+ * doubles (chemists' order (pq|rs), row-major), out is (2h)^4 doubles, every element of
+ * which is written.  mode 0 replaces spin_basis_set (matrixelements/transformations.py:
+ * 73-92, spins interleaved), mode 1 blocked_spin_basis_set (29-70, alpha block first),
+ * mode 2 spin_basis_anti_physicist (114-136, <rs||tu> with interleaved spins).  Results
+ * are exact copies (mode 2: one subtraction) of the input elements.  Both arrays must be
+ * 8-byte aligned (else GS_ERR_ARG); a 16-byte-aligned out takes the faster paired form for
+ * modes 0 and 2.  h above
+ * gs_spin_expand_max_orbitals() (the h x h slab one CTA stages must fit in shared memory;
+ * 169 with the 227 KiB of GB300) returns GS_ERR_LIMIT; h = 0 is a no-op. */
+int gs_spin_expand(const double* mo, int h, int mode, double* out, void* stream);
+int gs_spin_expand_max_orbitals(void);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);

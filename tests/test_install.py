@@ -12,8 +12,17 @@ def _fake_gaussium():
         setattr(hf, name, object())
     ks = types.ModuleType("gaussium.kohnsham.kohn_sham")
     ks.RestrictedKohnShamHamiltonian = object()
+    mp = types.ModuleType("gaussium.moellerplesset.moeller_plesset")
+    mp.molecular_orbitals = object()
+    cc = types.ModuleType("gaussium.coupledcluster.coupled_cluster")
+    cc.molecular_orbitals, cc.spin_basis_anti_physicist = object(), object()
+    td = types.ModuleType("gaussium.tdhartreefock.td_hartree_fock")
+    td.molecular_orbitals, td.spin_basis_set = object(), object()
     g = types.SimpleNamespace(hartreefock=types.SimpleNamespace(hartree_fock=hf),
-                              kohnsham=types.SimpleNamespace(kohn_sham=ks))
+                              kohnsham=types.SimpleNamespace(kohn_sham=ks),
+                              moellerplesset=types.SimpleNamespace(moeller_plesset=mp),
+                              coupledcluster=types.SimpleNamespace(coupled_cluster=cc),
+                              tdhartreefock=types.SimpleNamespace(td_hartree_fock=td))
     return g
 
 
@@ -32,3 +41,16 @@ def test_install_rebinds_and_returns_originals():
     assert hf.TwoElectronRepulsionMatrixOS(basis, None, 4).create_repulsion_matrix() is basis
     assert hf.blocked_spin_basis_set(basis) is basis
     assert orig[("gaussium.hartreefock.hartree_fock", "FockMatrixRestricted")] is before["FockMatrixRestricted"]
+
+
+def test_install_reroutes_post_scf_transforms():
+    from gaussium_gb300 import transform
+    g = _fake_gaussium()
+    before = g.coupledcluster.coupled_cluster.spin_basis_anti_physicist
+    orig = fock.install(g)
+    assert g.moellerplesset.moeller_plesset.molecular_orbitals is fock._mo_from_source
+    assert g.coupledcluster.coupled_cluster.molecular_orbitals is fock._mo_from_source
+    assert g.coupledcluster.coupled_cluster.spin_basis_anti_physicist is transform.spin_basis_anti_physicist
+    assert g.tdhartreefock.td_hartree_fock.spin_basis_set is transform.spin_basis_set
+    assert not hasattr(g.tdhartreefock.td_hartree_fock, "spin_basis_anti_physicist")
+    assert orig[("gaussium.coupledcluster.coupled_cluster", "spin_basis_anti_physicist")] is before

@@ -42,6 +42,8 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, name), name
     assert L.gs_version() == 1
     assert L.gs_status_string(0) == b"ok"
+    limit = L.gs_status_string(6)
+    assert b"no-allocation" in limit and b"gs_spin_expand_max_orbitals" in limit
 
 
 def test_product_path_fails_loudly_without_gpu(monkeypatch):
@@ -51,3 +53,18 @@ def test_product_path_fails_loudly_without_gpu(monkeypatch):
     monkeypatch.setattr(_lib, "_LIB", None)
     with pytest.raises(_lib.GsError):
         _lib.lib()
+
+
+def test_transform_fails_loudly_without_gpu(monkeypatch):
+    """The AO -> MO drop-ins have no CPU path: no device (or a CPU device) is an error."""
+    import numpy as np
+    import torch
+    from gaussium_gb300 import _lib, transform
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
+    monkeypatch.setattr(_lib, "_LIB", None)
+    x = np.zeros((2, 2, 2, 2))
+    for call in (lambda: transform.spin_basis_set(x),
+                 lambda: transform.molecular_orbitals(x, np.eye(2)),
+                 lambda: transform.spin_basis_anti_physicist(x, device="cpu")):
+        with pytest.raises(_lib.GsError):
+            call()
