@@ -53,12 +53,14 @@ def parse():
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the built-in kernel form of every class (no autotuning)")
     ap.add_argument("--cpu-sample", type=int, default=1024)
-    ap.add_argument("--workload", default="microbench", choices=["microbench", "water", "batch", "gradient", "optimize", "mo"])
+    ap.add_argument("--workload", default="microbench", choices=["microbench", "water", "batch", "gradient", "optimize", "mo", "xc"])
     ap.add_argument("--nm-evals", type=int, default=4000,
                     help="energy evaluations the Nelder-Mead comparison may spend")
     ap.add_argument("--fd-coords", type=int, default=72)
     ap.add_argument("--molecules", type=int, default=256)
     ap.add_argument("--waters", type=int, default=16)
+    ap.add_argument("--xc-waters", type=int, default=8,
+                    help="water molecules of the XC workload (19 6-31G* functions each)")
     ap.add_argument("--mo-waters", type=int, default=6,
                     help="water molecules of the AO->MO workload (13 6-31G functions each)")
     ap.add_argument("--optimizer", default="L-BFGS-B", choices=["L-BFGS-B", "BFGS"],
@@ -839,6 +841,107 @@ def run_mo(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------- LDA XC quadrature
+def run_xc(args, rank, world):
+    """LDA exchange-correlation matrix and energy (Slater + VWN3) of (H2O)n / 6-31G* on the
+    reference's grid placement (one spherical grid about the origin; 200 radial x 648
+    angular points).  One step = one XC build for a new density matrix with the basis
+    values on the grid kept from the first build, as an SCF iteration does: rho (GEMM),
+    the functionals (k_lda), V = Phi^T diag(w v) Phi (GEMM), E = sum w rho eps."""
+    import torch
+    from gaussium_gb300 import build, guess, kohnsham, molecules
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    build.build()
+    mol = molecules.water_cluster(args.xc_waters, seed=args.xc_waters)
+    sb = molecules.shell_basis(mol, "6-31G*")
+    n = sb.nbf
+    P = guess.sad_density(mol, "6-31G*")
+    xc = kohnsham.ExchangeCorrelationGPU(sb, params=(2 / 3, kohnsham.VWN3))
+    st = torch.cuda.current_stream()
+    g = xc.points.shape[0]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    xc.phi()
+    e1.record(st)
+    e1.synchronize()
+    ms_phi = e0.elapsed_time(e1)
+    Pd = torch.as_tensor(P).to(xc.device)
+    for _ in range(max(3, args.warmup)):
+        xc.evaluate_device(Pd)
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        e0.record(st)
+        for k in range(args.steps):
+            v, e = xc.evaluate_device(Pd * (1.0 + 1e-9 * k))
+        e1.record(st)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = 2.0 * 2.0 * g * n * n          # Phi P and Phi^T (w v Phi)
+    fp64 = fma_peak(64)
+    # end to end through the reference surface: host P in, XC matrix and energy back
+    e2e = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        V = xc.potential_matrix(P * (1.0 + 1e-9 * (k + 100)))
+        E = xc.integrate_energy(P * (1.0 + 1e-9 * (k + 100)))
+        if k >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        # the oracle's restatement of integrate_potential (kohnsham/integration.py:26-40) on
+        # a sample of matrix elements, scaled to the n(n+1)/2 the reference evaluates
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        from gaussium_gb300.basis import COMPONENTS
+        centre, lmn, cnorm, prims = [], [], [], []
+        for s in range(sb.nshell):
+            k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
+            for ci, c in enumerate(COMPONENTS[int(sb.l[s])]):
+                centre.append(sb.centre[s]); lmn.append(c); cnorm.append(sb.comp_scale[s, ci])
+                prims.append(list(zip(sb.coef[k0:k1], sb.expo[k0:k1], np.ones(k1 - k0))))
+        table = oracle.FunctionTable(np.array(centre), np.array(lmn), np.array(cnorm), prims)
+        sample = 2
+        t0 = time.perf_counter()
+        for i in range(sample):
+            def f(pts, i=i):
+                phi = oracle.basis_values(table, pts)
+                rho = np.einsum("ga,ab,gb->g", phi, P, phi)
+                m = rho > 1e-300
+                vv = np.zeros_like(rho)
+                vv[m] = oracle._xc_parts(rho[m], 2 / 3, oracle.VWN3)[1]
+                return phi[:, i] * vv * phi[:, i]
+            oracle.xc_integrate(f)
+        per = (time.perf_counter() - t0) / sample
+        cpu = {"value": per * n * (n + 1) / 2 * 1e3, "unit": "ms per XC build", "cores": 1,
+               "kind": "port",
+               "sample": f"{sample} of the {n * (n + 1) // 2} matrix elements (adaptive radial "
+                         "quad x degree-35 angular rule, numpy), scaled by the element count"}
+    line = {
+        "metric": "LDA XC matrix build time", "value": ms, "unit": "ms per XC build",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded water cluster, SAD density)",
+        "config": {"workload": f"LDA (Slater + VWN3) XC, (H2O){args.xc_waters}/6-31G*, {n} "
+                               f"functions, {g} grid points about the origin",
+                   "l2": f"basis values on the grid {g * n * 8 / 1e6:.0f} MB"},
+        "basis_on_grid_ms": ms_phi,
+        "basis_on_grid_gbs_written": g * n * 8 / (ms_phi * 1e-3) / 1e9,
+        "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12, "peak": fp64,
+                     "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / fp64,
+                     "traffic": None, "kernel": "cuBLAS DGEMM (rho and V contractions)",
+                     "peak_source": "FP64 FMA probe (gs_fma_probe) in this process"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": float(np.mean(e2e)) * 1e3, "unit": "ms per XC build",
+                "h2d_bytes_per_step": n * n * 8, "d2h_bytes_per_step": n * n * 8 + 8},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps,
+        "energy": float(e.item()),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------- reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -882,6 +985,8 @@ def main():
         run_optimize(args, rank, world)
     elif args.workload == "mo":
         run_mo(args, rank, world)
+    elif args.workload == "xc":
+        run_xc(args, rank, world)
     else:
         run_gpu(args, rank, world)
     if world > 1:

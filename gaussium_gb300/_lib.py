@@ -47,6 +47,8 @@ _SIGS = {
     "gs_one_electron_grad": (I, [P, P, P, P, P, P, P, P, I, P, I, I, P, P, P, P, P, P]),
     "gs_spin_expand": (I, [P, I, I, P, P]),
     "gs_spin_expand_max_orbitals": (I, []),
+    "gs_basis_on_grid": (I, [P, P, P, P, P, P, P, I, I, ctypes.c_longlong, P, P, P]),
+    "gs_lda_xc": (I, [ctypes.c_longlong, P, P, D, I, D, D, D, D, P, P, P]),
 }
 
 

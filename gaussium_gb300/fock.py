@@ -131,8 +131,9 @@ class BlockedFockMatrixUnrestrictedGPU(_Base):
 
 class RestrictedKohnShamHamiltonianGPU(_Base):
     """Returns (core_hamiltonian, J, XC) like the reference's create; J comes from the
-    engine, XC from the caller's exchange-correlation object exactly as the reference
-    evaluates it (outside this engine's scope)."""
+    engine, XC from the caller's exchange-correlation object: the whole matrix at once from
+    ``kohnsham.ExchangeCorrelationGPU``, element by element (as the reference evaluates it)
+    from any other object."""
 
     def __init__(self, core_hamiltonian, source, exchange_correlation=None, **kw):
         super().__init__(core_hamiltonian, source, **kw)
@@ -148,7 +149,10 @@ class RestrictedKohnShamHamiltonianGPU(_Base):
 
         (J,) = self._two_electron([p], g)
         xc = None
-        if self.exchange_correlation is not None:
+        if hasattr(self.exchange_correlation, "potential_matrix"):
+            # the GPU exchange-correlation object builds the whole matrix in one pass
+            xc = self.exchange_correlation.potential_matrix(density_matrix)
+        elif self.exchange_correlation is not None:
             n = self.matrix_size
             xc = np.zeros((n, n))
             for i in range(n):
@@ -195,7 +199,7 @@ def install(gaussium, **options):
     three Fock builders become the GPU drop-ins, and the spin-blocking of the tensor
     (``blocked_spin_basis_set``) passes the basis list through (the blocked drop-in builds
     the spin blocks itself); in ``gaussium.kohnsham.kohn_sham`` the Kohn-Sham Hamiltonian
-    becomes its drop-in.  In the post-SCF modules (MP2, CCSD, TDHF) that are loaded,
+    and the exchange-correlation quadrature become their drop-ins.  In the post-SCF modules (MP2, CCSD, TDHF) that are loaded,
     ``molecular_orbitals`` builds the MO tensor from the basis list on the device and
     ``spin_basis_set`` / ``spin_basis_anti_physicist`` become the GPU drop-ins.
     ``options`` (e.g. ``mixed_cut``, ``incremental``) go to every builder.  Returns the
@@ -211,8 +215,11 @@ def install(gaussium, **options):
              (hf, "blocked_spin_basis_set", lambda basis: basis)]
     ks = getattr(getattr(gaussium, "kohnsham", None), "kohn_sham", None)
     if ks is not None:
+        from .kohnsham import ExchangeCorrelationGPU
         swaps.append((ks, "RestrictedKohnShamHamiltonian",
                       functools.partial(RestrictedKohnShamHamiltonianGPU, **options)))
+        if hasattr(ks, "ExchangeCorrelation"):
+            swaps.append((ks, "ExchangeCorrelation", ExchangeCorrelationGPU))
     for pkg, modname in _POST_SCF:
         mod = getattr(getattr(gaussium, pkg, None), modname, None)
         if mod is None:

@@ -141,6 +141,36 @@ def restricted_scf(overlap, hcore, electrons, fock_builder, threshold=1e-12, max
                      converged=False, energies=energies, density=p, fock=f)
 
 
+def ks_restricted_scf(overlap, hcore, electrons, coulomb, exchange_correlation, threshold=1e-12,
+                      max_iter=100):
+    """KSRestrictedSCF.begin_iterations (kohnsham/kohn_sham_scf.py:14-38) with
+    KSEnergy.restricted (kohnsham/kohn_sham_energy.py:10-18): core-Hamiltonian guess; per
+    iteration P, J = coulomb(P), (V_xc, E_xc) = exchange_correlation.evaluate(P), the
+    energy 2 sum(eps_occ) - sum P (J/2 + V_xc) + E_xc from the previous orbital energies,
+    DIIS on H + J + V_xc, diagonalise; stop when |dE| < threshold."""
+    la = LinearAlgebra(overlap)
+    diis = DIIS(overlap, la)
+    e_orb, c = la.diagonalize(hcore)
+    previous = 0.0
+    energies = []
+    nocc = electrons // 2
+    for it in range(1, max_iter + 1):
+        p = density_matrix_restricted(c, electrons)
+        j = coulomb(p)
+        v, exc = exchange_correlation.evaluate(p)
+        ks = hcore + j + v
+        e = 2 * float(np.sum(e_orb[:nocc])) - float(np.sum(p * (0.5 * j + v))) + exc
+        energies.append(e)
+        if abs(previous - e) < threshold:
+            return SCFResult(energy=e, orbital_energies=e_orb, coefficients=c, iterations=it,
+                             converged=True, energies=energies, density=p, fock=ks)
+        previous = e
+        ks = diis.fock_matrix(ks, p)
+        e_orb, c = la.diagonalize(ks)
+    return SCFResult(energy=e, orbital_energies=e_orb, coefficients=c, iterations=max_iter,
+                     converged=False, energies=energies, density=p, fock=ks)
+
+
 def unrestricted_scf(overlap, hcore, electrons, multiplicity, fock_builder, threshold=1e-12,
                      max_iter=200):
     """PopleNesbetBerthier.begin_iterations (first density from all alpha orbitals as the

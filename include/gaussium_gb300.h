@@ -272,6 +272,29 @@ int gs_one_electron_grad(const double* centre, const int* l, const int* prim_off
 int gs_spin_expand(const double* mo, int h, int mode, double* out, void* stream);
 int gs_spin_expand_max_orbitals(void);
 
+/* Values of every basis function at npts grid points: phi[g*nbf + f] (row-major, npts x
+ * nbf), points[3*g..] in bohr; shells as in gs_pairs_build plus comp_scale[nshell*6] and
+ * func_off[nshell].  Replaces Basis.value / PrimitiveBasis.value
+ * (objects/basis_function.py, objects/primitive_basis_function.py:44-60) as the
+ * reference's exchange-correlation quadrature calls them (kohnsham/integration.py:14-51). */
+int gs_basis_on_grid(const double* centre, const int* l, const int* prim_off, const double* expo,
+                     const double* coef, const double* comp_scale, const int* func_off,
+                     int nshell, int nbf, long long npts, const double* points, double* phi,
+                     void* stream);
+
+/* LDA functionals at npts densities rho[g] with quadrature weights w[g]:
+ *   weighted_potential[g] = w[g] * (v_x + v_c)(rho[g]),
+ *   weighted_energy[g]    = w[g] * rho[g] * (eps_x + eps_c)(rho[g]),
+ * Slater exchange with slater_alpha (0 = none; kohnsham/exchange/slater_exchange.py) and,
+ * if vwn != 0, Vosko-Wilk-Nusair correlation with fit (a, x0, b, c), a in Rydberg as the
+ * reference passes it (kohnsham/correlation/local_density.py, kohnsham/kohn_sham.py:21-28).
+ * rho <= 1e-300 contributes 0 (the reference's zero-density rule, extended to subnormal
+ * densities whose Wigner-Seitz radius overflows).  4c - b^2 <= 0 with vwn set is
+ * GS_ERR_ARG. */
+int gs_lda_xc(long long npts, const double* rho, const double* weights, double slater_alpha,
+              int vwn, double vwn_a, double vwn_x0, double vwn_b, double vwn_c,
+              double* weighted_potential, double* weighted_energy, void* stream);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);

@@ -289,3 +289,182 @@ def spin_basis_anti_physicist(repulsion):
                     b = (r % 2 == u % 2) * (s % 2 == t % 2) * repulsion[r // 2, u // 2, s // 2, t // 2]
                     out[r, s, t, u] = a - b
     return out
+
+
+# ---------------------------------------------------------------------- LDA exchange-correlation
+# Restatements of kohnsham/ (test infrastructure, like the rest of this file).  The
+# reference's angular rule is quadpy's Lebedev rule of degree 35 (kohnsham/integration.py:
+# 53-61; quadpy is not installed here).  The oracle uses a product rule of the same degree
+# instead: 18 Gauss-Legendre nodes in cos(theta) times 36 equally spaced phi (exact for
+# spherical harmonics up to degree 35, weights summing to 4 pi).  On the reference's own
+# use, atoms at the origin, every integrand is a radial function times a polynomial of
+# degree <= 4 in the direction, which both rules integrate exactly.  Radial: scipy's
+# adaptive quad on [0, inf) with its default tolerances, as the reference.
+
+def slater_energy(rho, alpha):
+    """SlaterExchange.energy, kohnsham/exchange/slater_exchange.py (per electron)."""
+    return -(9 / 8) * alpha * (3 / np.pi) ** (1 / 3) * np.cbrt(rho)
+
+
+def slater_potential(rho, alpha):
+    """SlaterExchange.potential."""
+    return -(3 / 2) * alpha * (3 / np.pi) ** (1 / 3) * np.cbrt(rho)
+
+
+def _vwn_terms(rho, a, x0, b, c):
+    rs = (3 / (4 * np.pi * rho)) ** (1 / 3)
+    x = np.sqrt(rs)
+    xx = x * x + b * x + c
+    xx0 = x0 * x0 + b * x0 + c
+    q = np.sqrt(4 * c - b * b)
+    at = np.arctan(q / (2 * x + b))
+    e = (a / 2) * (np.log(x * x / xx) + (2 * b / q) * at
+                   - (b * x0 / xx0) * (np.log((x - x0) ** 2 / xx) + (2 * (b + 2 * x0) / q) * at))
+    return x, xx, e
+
+
+def vwn_energy(rho, a, x0, b, c):
+    """VoskoWilkNusair._energy, kohnsham/correlation/local_density.py (a in Rydberg, halved
+    to Hartree; 0 at zero density)."""
+    rho = np.asarray(rho, dtype=np.float64)
+    out = np.zeros_like(rho)
+    m = rho != 0
+    out[m] = _vwn_terms(rho[m], a, x0, b, c)[2]
+    return out
+
+
+def vwn_potential(rho, a, x0, b, c):
+    """VoskoWilkNusair._potential."""
+    rho = np.asarray(rho, dtype=np.float64)
+    out = np.zeros_like(rho)
+    m = rho != 0
+    x, xx, e = _vwn_terms(rho[m], a, x0, b, c)
+    out[m] = e - (a / 2 / 3) * ((c * (x - x0) - b * x0 * x) / ((x - x0) * xx))
+    return out
+
+
+VWN3 = (0.0621814, -0.409286, 13.0720, 42.7198)     # kohnsham/kohn_sham.py:21-28
+VWN5 = (0.0621814, -0.10498, 3.72744, 12.9352)
+
+
+def basis_values(table, pts):
+    """Basis.value / PrimitiveBasis.value (objects/basis_function.py, objects/
+    primitive_basis_function.py:44-60) of every function at points (n, 3)."""
+    pts = np.asarray(pts, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((len(pts), len(table)))
+    for f in range(len(table)):
+        d = pts - table.centre[f]
+        r2 = np.sum(d * d, axis=1)
+        poly = np.prod(d ** table.lmn[f], axis=1)
+        s = np.zeros(len(pts))
+        for k in range(table.pstart[f], table.pstart[f + 1]):
+            s += table.pnorm[k] * table.coef[k] * np.exp(-table.expo[k] * r2)
+        out[:, f] = table.cnorm[f] * poly * s
+    return out
+
+
+def electron_density(table, p, pts):
+    """ExchangeCorrelation.electron_density, kohnsham/integration.py:14-24."""
+    phi = basis_values(table, pts)
+    return np.einsum("ga,ab,gb->g", phi, p, phi)
+
+
+def angular_rule():
+    """Product rule of degree 35 on the unit sphere: unit vectors (648, 3), weights."""
+    ct, wt = np.polynomial.legendre.leggauss(18)
+    phi = 2 * np.pi * np.arange(36) / 36
+    st = np.sqrt(1 - ct * ct)
+    dirs = np.stack([np.outer(st, np.cos(phi)), np.outer(st, np.sin(phi)),
+                     np.outer(ct, np.ones_like(phi))], axis=-1).reshape(-1, 3)
+    w = np.outer(wt, np.full(36, 2 * np.pi / 36)).reshape(-1)
+    return dirs, w
+
+
+def _xc_parts(rho, alpha, vwn):
+    e = np.zeros_like(rho)
+    v = np.zeros_like(rho)
+    if alpha:
+        e += slater_energy(rho, alpha)
+        v += slater_potential(rho, alpha)
+    if vwn is not None:
+        e += vwn_energy(rho, *vwn)
+        v += vwn_potential(rho, *vwn)
+    return e, v
+
+
+def xc_integrate(fn):
+    """ExchangeCorrelation.integrate, kohnsham/integration.py:53-61: radial quad of the
+    spherical integral of fn(points (n, 3)) r^2 about the origin."""
+    from scipy import integrate
+    dirs, w = angular_rule()
+    return integrate.quad(lambda r: float(np.dot(w, fn(r * dirs))) * r * r, 0.0, np.inf)[0]
+
+
+def xc_potential_matrix(table, p, alpha, vwn):
+    """ExchangeCorrelation.integrate_potential (kohnsham/integration.py:26-40) for every
+    (i, j), i <= j mirrored, as RestrictedKohnShamHamiltonian.create builds it
+    (kohnsham/kohn_sham_hamiltonian.py:21-24)."""
+    n = len(table)
+    out = np.zeros((n, n))
+    for i in range(n):
+        for j in range(i, n):
+            def f(pts, i=i, j=j):
+                phi = basis_values(table, pts)
+                rho = np.einsum("ga,ab,gb->g", phi, p, phi)
+                return phi[:, i] * _xc_parts(rho, alpha, vwn)[1] * phi[:, j]
+            out[i, j] = out[j, i] = xc_integrate(f)
+    return out
+
+
+def xc_energy(table, p, alpha, vwn):
+    """ExchangeCorrelation.integrate_energy, kohnsham/integration.py:42-51."""
+    def f(pts):
+        rho = electron_density(table, p, pts)
+        return rho * _xc_parts(rho, alpha, vwn)[0]
+    return xc_integrate(f)
+
+
+def ks_restricted_scf(overlap, hcore, eri, electrons, table, alpha, vwn, threshold=1e-12,
+                      max_iter=60):
+    """KSRestrictedSCF.begin_iterations (kohnsham/kohn_sham_scf.py:14-38) with
+    KSEnergy.restricted (kohnsham/kohn_sham_energy.py:10-18): core guess, then
+    P -> (H, J, XC), E = 2 sum(eps_occ) - sum P (J/2 + XC) + Exc, until |dE| < threshold.
+    Plain Roothaan steps (the reference's DIIS changes the path, not the fixed point)."""
+    s_eval, s_vec = np.linalg.eigh(overlap)
+    x = s_vec / np.sqrt(s_eval)
+    eps, c = np.linalg.eigh(x.T @ hcore @ x)
+    c = x @ c
+    previous = 0.0
+    for _ in range(max_iter):
+        occ = c[:, :electrons // 2]
+        p = 2 * occ @ occ.T
+        j = coulomb(eri, p)
+        v = xc_potential_matrix(table, p, alpha, vwn)
+        e = 2 * np.sum(eps[:electrons // 2]) - np.sum(p * (0.5 * j + v)) + xc_energy(table, p, alpha, vwn)
+        if abs(previous - e) < threshold:
+            return e
+        previous = e
+        eps, c = np.linalg.eigh(x.T @ (hcore + j + v) @ x)
+        c = x @ c
+    return e
+
+
+def one_centre_s(table, charge):
+    """S, T, V of s functions that all sit on one nucleus of the given charge (closed forms
+    of integrals/orbital_overlap_integral.py, matrixelements/kinetic_energy_matrix.py and
+    integrals/nuclear_attraction_integral.py for l = 0, |AB| = |AC| = 0)."""
+    n = len(table)
+    S, T, V = (np.zeros((n, n)) for _ in range(3))
+    for i in range(n):
+        for j in range(n):
+            for a in range(table.pstart[i], table.pstart[i + 1]):
+                for b in range(table.pstart[j], table.pstart[j + 1]):
+                    pa, pb = table.expo[a], table.expo[b]
+                    k = (table.cnorm[i] * table.cnorm[j] * table.coef[a] * table.coef[b]
+                         * table.pnorm[a] * table.pnorm[b])
+                    p = pa + pb
+                    s = (np.pi / p) ** 1.5
+                    S[i, j] += k * s
+                    T[i, j] += k * 3 * pa * pb / p * s
+                    V[i, j] += -k * charge * 2 * np.pi / p
+    return S, T, V

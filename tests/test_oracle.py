@@ -98,3 +98,38 @@ def test_ao_to_mo_restatements_match_reference():
     assert np.max(np.abs(oracle.spin_basis_set(g["mo"]) - g["spin"])) == 0.0
     assert np.max(np.abs(oracle.blocked_spin_basis_set(g["mo"]) - g["blocked"])) == 0.0
     assert np.max(np.abs(oracle.spin_basis_anti_physicist(g["mo"]) - g["anti"])) == 0.0
+
+
+def test_lda_functionals_and_density_match_reference():
+    """The oracle's Slater / VWN restatements and electron density against the reference's
+    own outputs (tests/golden/make_xc_golden.py)."""
+    from molecules import load
+    g = golden("xc")
+    d = g["density"]
+    for tag, alpha in (("s", 2 / 3), ("xa", 0.7)):
+        assert np.allclose(oracle.slater_energy(d, alpha), g[f"slater_{tag}_energy"], rtol=1e-14, atol=0)
+        assert np.allclose(oracle.slater_potential(d, alpha), g[f"slater_{tag}_potential"], rtol=1e-14, atol=0)
+    for tag, prm in (("vwn3", oracle.VWN3), ("vwn5", oracle.VWN5)):
+        assert np.allclose(oracle.vwn_energy(d, *prm), g[f"{tag}_energy"], rtol=1e-13, atol=0)
+        assert np.allclose(oracle.vwn_potential(d, *prm), g[f"{tag}_potential"], rtol=1e-13, atol=0)
+    _, _, table = load("h2o_sto3g")
+    rho = oracle.electron_density(table, g["pmat"], g["points"])
+    assert np.max(np.abs(rho - g["rho"])) < 1e-15
+
+
+def he_sto3g():
+    return oracle.FunctionTable.from_shells([dict(
+        l=0, centre=np.zeros(3), expo=np.array([6.36242139, 1.15892300, 0.31364979]),
+        coef=np.array([0.15432897, 0.53532814, 0.44463454]))])
+
+
+def test_ks_oracle_reproduces_reference_he_dft_energies():
+    """The oracle's Kohn-Sham restatement (quad radially, degree-35 product rule in angle)
+    against the reference's own He/STO-3G DFT energies (test_start.py, 6 s.f.)."""
+    g = golden("xc")
+    he = he_sto3g()
+    S, T, V = oracle.one_centre_s(he, 2.0)
+    eri = oracle.dense_tensor(he)
+    for alpha, vwn, key in ((2 / 3, None, "he_energy_s"), (2 / 3, oracle.VWN3, "he_energy_svwn3")):
+        e = oracle.ks_restricted_scf(S, T + V, eri, 2, he, alpha, vwn)
+        assert abs(e - float(g[key])) < 1e-8, key
