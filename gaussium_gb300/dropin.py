@@ -24,7 +24,7 @@ not C1 is honoured by zeroing the keys its ``none_zero_integral`` rejects, as
 import numpy as np
 import torch
 
-from . import engine
+from . import _lib, engine
 from .basis import COMPONENTS, ShellBasis, component_index
 
 
@@ -109,6 +109,48 @@ def dense_eri(sb: ShellBasis, device="cuda", precision=64):
     return t
 
 
+_PARITIES = [(p & 1, (p >> 1) & 1, (p >> 2) & 1) for p in range(8)]
+
+
+def symmetry_tables(symmetry, basis_set_array):
+    """Device-kernel tables of the reference's Symmetry object (common/symmetry.py:10-16):
+    (table, flip, centre_id, parity) as numpy arrays, or None when the object does not
+    carry the reference's ``symmetry_matrix`` / ``int_operate_dict``."""
+    sm = getattr(symmetry, "symmetry_matrix", None)
+    ops = getattr(symmetry, "int_operate_dict", None)
+    n = len(basis_set_array)
+    if not isinstance(sm, np.ndarray) or not isinstance(ops, dict) or sm.ndim != 2 \
+            or sm.shape[0] != n + 1:
+        return None
+    nops = sm.shape[1] - 1
+    table = np.array([[int(sm[f + 1, m + 1]) for m in range(nops)] for f in range(n)],
+                     dtype=np.int32).reshape(n, nops)
+    flip = np.array([[_PARITIES[p] != tuple(ops[(m + 1, _PARITIES[p])]) for p in range(8)]
+                     for m in range(nops)], dtype=np.uint8).reshape(nops, 8)
+    ids = {}
+    centre = np.array([ids.setdefault(tuple(float(v) for v in b.coordinates), len(ids))
+                       for b in basis_set_array], dtype=np.int32)
+    lmn = np.array([b.integral_exponents for b in basis_set_array], dtype=np.int64).reshape(n, 3)
+    parity = ((lmn[:, 0] % 2) | ((lmn[:, 1] % 2) << 1) | ((lmn[:, 2] % 2) << 2)).astype(np.int32)
+    return table, flip, centre, parity
+
+
+def symmetry_zero(tensor, table, flip, centre_id, parity):
+    """Zero in place the elements of a dense device tensor that the point group makes
+    vanish (``gs_symmetry_zero``)."""
+    n = tensor.shape[0]
+    dev = tensor.device
+    tb = torch.as_tensor(np.ascontiguousarray(table, dtype=np.int32)).to(dev)
+    fl = torch.as_tensor(np.ascontiguousarray(flip, dtype=np.uint8)).to(dev)
+    ci = torch.as_tensor(np.ascontiguousarray(centre_id, dtype=np.int32)).to(dev)
+    pa = torch.as_tensor(np.ascontiguousarray(parity, dtype=np.int32)).to(dev)
+    L = _lib.lib()
+    _lib.check(L.gs_symmetry_zero(n, tb.shape[1] if tb.dim() == 2 else 0, _lib.ptr(tb), _lib.ptr(fl),
+                                  _lib.ptr(ci), _lib.ptr(pa), _lib.ptr(tensor), _lib.stream()),
+               "gs_symmetry_zero")
+    return tensor
+
+
 class TwoElectronRepulsionGPU:
     def __init__(self, basis_set_array, integral=None, symmetry=None, processes=1, device="cuda"):
         self.basis_set_array = basis_set_array
@@ -140,6 +182,12 @@ class TwoElectronRepulsionGPU:
         s = self.symmetry
         pg = getattr(s, "point_group", None) if s is not None else None
         if s is not None and not (pg is not None and getattr(pg, "label", None) == "C_{1}"):
+            tables = symmetry_tables(s, self.basis_set_array)
+            if tables is not None:
+                symmetry_zero(t, *tables)
+                return t if as_tensor else t.cpu().numpy()
+            # a symmetry object without the reference's tables (e.g. a test double):
+            # ask it key by key, as the reference does
             n = self.matrix_size
             mask = torch.ones((n, n, n, n), dtype=torch.bool)
             for a in range(n):

@@ -295,6 +295,17 @@ int gs_lda_xc(long long npts, const double* rho, const double* weights, double s
               int vwn, double vwn_a, double vwn_x0, double vwn_b, double vwn_c,
               double* weighted_potential, double* weighted_energy, void* stream);
 
+/* Point-group zero screening of a dense n^4 tensor (row-major, device), in place: every
+ * element Symmetry.none_zero_integral (common/symmetry.py:18-47) declares zero is set to
+ * 0.  Tables of a non-C1 group with nops operations besides the identity:
+ * table[f*nops + m] = signed 1-based image of function f under operation m+1, 0 for none
+ * (the reference's basis_set_symmetry_matrix without its label row and identity column);
+ * flip[m*8 + p] = 1 if operation m+1 changes parity vector p (bit 0 x, bit 1 y, bit 2 z;
+ * from symmetry_exponent_dict); centre_id[f] (equal for functions on one centre);
+ * parity[f] = parity bits of f's integral exponents. */
+int gs_symmetry_zero(int n, int nops, const int* table, const unsigned char* flip,
+                     const int* centre_id, const int* parity, double* tensor, void* stream);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);

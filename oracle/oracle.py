@@ -468,3 +468,38 @@ def one_centre_s(table, charge):
                     T[i, j] += k * 3 * pa * pb / p * s
                     V[i, j] += -k * charge * 2 * np.pi / p
     return S, T, V
+
+
+# ---------------------------------------------------------------------- point-group screening
+def symmetry_nonzero(table, flip, centre_id, parity, key):
+    """Symmetry.none_zero_integral (common/symmetry.py:18-47) for a non-C1 group, from its
+    tables: table[f, m-1] = signed 1-based image of function f under operation m (0: none,
+    basis_set_symmetry_matrix), flip[m-1, p] = whether operation m changes the parity vector
+    p (symmetry_exponent_dict), centre_id[f] (functions on one centre share it),
+    parity[f] = bits (l mod 2, m mod 2, n mod 2) of the integral exponents."""
+    i, j, k, l = (int(x) for x in key)
+    p = parity[i] ^ parity[j] ^ parity[k] ^ parity[l]
+    if centre_id[i] == centre_id[j] == centre_id[k] == centre_id[l]:
+        return p == 0
+    for m in range(table.shape[1]):
+        a, b, c, d = table[i, m], table[j, m], table[k, m], table[l, m]
+        if a == 0 or b == 0 or c == 0 or d == 0:
+            continue
+        w, x, y, z = abs(a) - 1, abs(b) - 1, abs(c) - 1, abs(d) - 1
+        if ((i == w and j == x) or (i == x and j == w)) and \
+                ((k == y and l == z) or (k == z and l == y)) and flip[m, p]:
+            return False
+    return True
+
+
+def centre_ids(centres):
+    """Functions whose coordinates are exactly equal share an id (the reference compares
+    coordinate tuples with ==, common/symmetry.py:28)."""
+    ids = {}
+    return np.array([ids.setdefault(tuple(float(v) for v in c), len(ids)) for c in centres],
+                    dtype=np.int32)
+
+
+def parity_bits(lmn):
+    lmn = np.asarray(lmn)
+    return ((lmn[:, 0] % 2) | ((lmn[:, 1] % 2) << 1) | ((lmn[:, 2] % 2) << 2)).astype(np.int32)

@@ -133,3 +133,22 @@ def test_ks_oracle_reproduces_reference_he_dft_energies():
     for alpha, vwn, key in ((2 / 3, None, "he_energy_s"), (2 / 3, oracle.VWN3, "he_energy_svwn3")):
         e = oracle.ks_restricted_scf(S, T + V, eri, 2, he, alpha, vwn)
         assert abs(e - float(g[key])) < 1e-8, key
+
+
+def test_symmetry_screen_restatement_matches_reference():
+    """The oracle's point-group screen against the reference's none_zero_integral on every
+    canonical key of three systems (tests/golden/make_symmetry_golden.py), and invariance
+    under the 8 index permutations the dense tensor expands each key to."""
+    g = golden("symmetry")
+    rng = np.random.default_rng(0)
+    for name in ("ethene", "water", "o2"):
+        table, flip = g[f"{name}_table"], g[f"{name}_flip"]
+        cid = oracle.centre_ids(g[f"{name}_centre"])
+        par = oracle.parity_bits(g[f"{name}_lmn"])
+        keys, ref = g[f"{name}_keys"], g[f"{name}_nonzero"]
+        got = np.array([oracle.symmetry_nonzero(table, flip, cid, par, k) for k in keys])
+        assert np.array_equal(got, ref), name
+        for t in rng.choice(len(keys), 300, replace=False):
+            a, b, c, d = keys[t]
+            for perm in ((b, a, c, d), (a, b, d, c), (c, d, a, b), (d, c, b, a)):
+                assert oracle.symmetry_nonzero(table, flip, cid, par, perm) == ref[t]
