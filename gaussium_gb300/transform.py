@@ -108,9 +108,24 @@ def max_spatial_orbitals():
     return _lib.lib().gs_spin_expand_max_orbitals()
 
 
+def _to_host(t):
+    """A device tensor as a new numpy array, copied into page-locked memory (torch's
+    pinned-host cache reuses the block once the array is freed), which the copy engine
+    fills at full link speed instead of staging through pageable pages."""
+    out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    out.copy_(t)
+    return out.numpy()
+
+
 def molecular_orbitals(repulsion, coefficients, device="cuda"):
     c = _dev(coefficients, device)
-    out = transform_device(_dev(repulsion, device), c).cpu().numpy()
+    mo = transform_device(_dev(repulsion, device), c)
+    if isinstance(repulsion, np.ndarray) and repulsion.shape == tuple(mo.shape) \
+            and repulsion.dtype == np.float64 and repulsion.flags.writeable \
+            and repulsion.flags.c_contiguous:
+        torch.from_numpy(repulsion).copy_(mo)       # straight into the caller's array
+        return repulsion
+    out = _to_host(mo)
     if isinstance(repulsion, np.ndarray) and repulsion.shape == out.shape \
             and repulsion.dtype == np.float64 and repulsion.flags.writeable:
         repulsion[...] = out
@@ -119,15 +134,15 @@ def molecular_orbitals(repulsion, coefficients, device="cuda"):
 
 
 def spin_basis_set(repulsion, device="cuda"):
-    return spin_expand_device(_dev(repulsion, device), SPIN_INTERLEAVED).cpu().numpy()
+    return _to_host(spin_expand_device(_dev(repulsion, device), SPIN_INTERLEAVED))
 
 
 def blocked_spin_basis_set(repulsion, device="cuda"):
-    return spin_expand_device(_dev(repulsion, device), SPIN_BLOCKED).cpu().numpy()
+    return _to_host(spin_expand_device(_dev(repulsion, device), SPIN_BLOCKED))
 
 
 def spin_basis_anti_physicist(repulsion, device="cuda"):
-    return spin_expand_device(_dev(repulsion, device), SPIN_ANTI_PHYSICIST).cpu().numpy()
+    return _to_host(spin_expand_device(_dev(repulsion, device), SPIN_ANTI_PHYSICIST))
 
 
 def mo_integrals(sb, coefficients, device="cuda"):

@@ -31,6 +31,23 @@ def test_golden_molecular_orbitals_mutates_and_returns_its_argument(gpu_lib):
     assert np.max(np.abs(out - g["mo"])) < 1e-13
 
 
+def test_molecular_orbitals_other_input_layouts(gpu_lib):
+    """Fortran-ordered input is still overwritten and returned; a read-only input is left
+    alone and a new array returned; a nested list gives an array."""
+    from gaussium_gb300 import transform
+    g = golden("mo_transform")
+    f = np.asfortranarray(g["ao"])
+    assert transform.molecular_orbitals(f, g["coefficients"]) is f
+    assert np.max(np.abs(f - g["mo"])) < 1e-13
+    ro = g["ao"].copy()
+    ro.flags.writeable = False
+    out = transform.molecular_orbitals(ro, g["coefficients"])
+    assert out is not ro and np.array_equal(ro, g["ao"])
+    assert np.max(np.abs(out - g["mo"])) < 1e-13
+    out = transform.molecular_orbitals(g["ao"].tolist(), g["coefficients"])
+    assert isinstance(out, np.ndarray) and np.max(np.abs(out - g["mo"])) < 1e-13
+
+
 def test_golden_spin_expansions_exact(gpu_lib):
     from gaussium_gb300 import transform
     g = golden("mo_transform")
