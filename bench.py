@@ -391,6 +391,11 @@ def run_gpu(args, rank, world):
                      "peak_source": "gs_fma_probe FP64 FMA rate measured in this run "
                                     "(no FP64 figure among the pool's measured peaks)"},
         "fp64": {"value": n_all / (ms64 * 1e-3), "ms_per_step": ms64,
+                 # the same step counted in the reference's unit (function quartets) and
+                 # in primitive quartets (all, and those left after the pair screen)
+                 "function_quartets_per_s": batch.total * world / (ms64 * 1e-3),
+                 "primitive_quartets_per_s": batch.full_prim_quartets * world / (ms64 * 1e-3),
+                 "primitive_quartets_evaluated_per_s": batch.prim_quartets * world / (ms64 * 1e-3),
                  "tflops": total_flops / (ms64 * 1e-3) / 1e12,
                  "frac_of_fp64_peak": total_flops / (ms64 * 1e-3) / 1e12 / peak64},
         "fp64_rate_with_8_of_32_lanes_active_tflops": peak64_8lanes,
