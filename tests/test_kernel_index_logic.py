@@ -1,0 +1,143 @@
+"""Index arithmetic of the data-movement kernels, walked on the CPU exactly as the device
+code does it (no GPU): the spin-orbital expansion kernels of csrc/transform.cu and the
+element decomposition of csrc/symmetry.cu, against the oracle.  Every address the walk
+forms is checked against its buffer, so a change to the kernels' indexing is caught here
+before it runs on a GPU."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden
+
+THREADS = 256
+
+
+def slab_of(mo, h, mode, r, s):
+    """stage_slab: (live, slab with odd row pitch, pitch); asserts the reads stay in mo."""
+    pitch = h | 1
+    flat = mo.ravel()
+    h2, h3 = h * h, h * h * h
+    if mode == 0:
+        live, src, si = (r & 1) == (s & 1), (r >> 1) * h3 + (s >> 1) * h2, h
+    elif mode == 1:
+        live, src, si = (r < h) == (s < h), (r % h) * h3 + (s % h) * h2, h
+    else:
+        live, src, si = True, (r >> 1) * h3 + (s >> 1) * h, h2
+    slab = np.full(h * pitch, np.nan)
+    if live:
+        for i in range(h):
+            idx = src + i * si + np.arange(h)
+            assert idx.min() >= 0 and idx.max() < h ** 4
+            slab[i * pitch:i * pitch + h] = flat[idx]
+    return live, slab, pitch
+
+
+def pairs_kernel(mo, h, mode):
+    """k_spin_expand_pairs, modes 0 and 2, with its (t, k) carry instead of a division."""
+    n = 2 * h
+    out = np.full(n ** 4, np.nan)
+    sign = lambda x: -x if x != 0 else np.copysign(0.0, -np.copysign(1.0, x))  # noqa: E731
+    for blk in range(n * n):
+        r, s = blk // n, blk % n
+        live, slab, pitch = slab_of(mo, h, mode, r, s)
+        sp, rp = s & 1, r & 1
+        npairs = 2 * h * h
+        dt, dk = THREADS // h, THREADS - (THREADS // h) * h
+        for tid in range(min(THREADS, npairs)):
+            t, k, e = tid // h, tid - (tid // h) * h, tid
+            while e < npairs:
+                assert t * h + k == e and 0 <= k < h and 0 <= t < n
+                tp = t & 1
+                if mode == 0:
+                    a = slab[(t >> 1) * pitch + k] if live else 0.0
+                    x, y = (0.0, a) if tp else (a, 0.0)
+                elif sp == rp:
+                    d = slab[(t >> 1) * pitch + k] - slab[(t >> 1) + k * pitch] if tp == sp else 0.0
+                    x, y = (0.0, d) if sp else (d, 0.0)
+                else:
+                    a = slab[(t >> 1) * pitch + k] if tp == rp else 0.0
+                    b = sign(slab[(t >> 1) + k * pitch]) if tp == sp else 0.0
+                    x, y = (b, a) if sp else (a, b)
+                o = blk * n * n + 2 * e
+                assert o + 1 < n ** 4
+                out[o], out[o + 1] = x, y
+                k += dk
+                t += dt
+                if k >= h:
+                    k -= h
+                    t += 1
+                e += THREADS
+    return out.reshape((n,) * 4)
+
+
+def scalar_kernel(mo, h, mode):
+    """k_spin_expand (any mode): one warp per output row."""
+    n = 2 * h
+    out = np.full(n ** 4, np.nan)
+    for blk in range(n * n):
+        r, s = blk // n, blk % n
+        live, slab, pitch = slab_of(mo, h, mode, r, s)
+        for t in range(n):
+            row = blk * n * n + t * n
+            for u in range(n):
+                if mode == 0:
+                    v = slab[(t >> 1) * pitch + (u >> 1)] if live and (u & 1) == (t & 1) else 0.0
+                elif mode == 1:
+                    tlo = t < h
+                    v = slab[(t if tlo else t - h) * pitch + (u if u < h else u - h)] \
+                        if live and (u < h) == tlo else 0.0
+                else:
+                    a = slab[(t >> 1) * pitch + (u >> 1)] if (r & 1) == (t & 1) and (u & 1) == (s & 1) else 0.0
+                    b = slab[(t >> 1) + (u >> 1) * pitch] if (u & 1) == (r & 1) and (s & 1) == (t & 1) else 0.0
+                    v = a - b
+                out[row + u] = v
+    return out.reshape((n,) * 4)
+
+
+REF = {0: oracle.spin_basis_set, 1: oracle.blocked_spin_basis_set, 2: oracle.spin_basis_anti_physicist}
+
+
+@pytest.mark.parametrize("h", [1, 2, 3, 5, 17])
+def test_spin_pair_kernel_walk(h):
+    mo = np.random.default_rng(h).standard_normal((h,) * 4)
+    for mode in (0, 2):
+        assert np.array_equal(pairs_kernel(mo, h, mode), REF[mode](mo)), mode
+
+
+@pytest.mark.parametrize("h", [1, 2, 3, 4])
+def test_spin_scalar_kernel_walk(h):
+    mo = np.random.default_rng(10 + h).standard_normal((h,) * 4)
+    for mode in (0, 1, 2):
+        assert np.array_equal(scalar_kernel(mo, h, mode), REF[mode](mo)), mode
+
+
+def test_symmetry_kernel_element_decomposition():
+    """k_symmetry_zero's e -> (i, j, k, l) split and test, over every element of O2/STO-3G
+    (10 functions), against the oracle on the canonical keys."""
+    g = golden("symmetry")
+    table, flip = g["o2_table"], g["o2_flip"]
+    cid = oracle.centre_ids(g["o2_centre"])
+    par = oracle.parity_bits(g["o2_lmn"])
+    n, nops = table.shape
+    n2 = n * n
+    zero = np.zeros(n ** 4, dtype=bool)
+    for e in range(n ** 4):
+        ij, kl = divmod(e, n2)
+        i, j = divmod(ij, n)
+        k, l = divmod(kl, n)
+        p = par[i] ^ par[j] ^ par[k] ^ par[l]
+        if cid[i] == cid[j] == cid[k] == cid[l]:
+            zero[e] = p != 0
+            continue
+        for m in range(nops):
+            a, b, c, d = table[i, m], table[j, m], table[k, m], table[l, m]
+            if a == 0 or b == 0 or c == 0 or d == 0:
+                continue
+            w, x, y, z = abs(a) - 1, abs(b) - 1, abs(c) - 1, abs(d) - 1
+            if ((i == w and j == x) or (i == x and j == w)) and \
+                    ((k == y and l == z) or (k == z and l == y)) and flip[m, p]:
+                zero[e] = True
+                break
+    zero = zero.reshape((n,) * 4)
+    keys = g["o2_keys"]
+    assert np.array_equal(~zero[keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3]], g["o2_nonzero"])
