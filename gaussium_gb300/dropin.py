@@ -139,6 +139,9 @@ def symmetry_zero(tensor, table, flip, centre_id, parity):
     """Zero in place the elements of a dense device tensor that the point group makes
     vanish (``gs_symmetry_zero``)."""
     n = tensor.shape[0]
+    if not tensor.is_cuda or tensor.dtype != torch.float64 or not tensor.is_contiguous() \
+            or tuple(tensor.shape) != (n, n, n, n):
+        raise _lib.GsError("gs_symmetry_zero takes a contiguous float64 CUDA tensor of n^4 elements")
     dev = tensor.device
     tb = torch.as_tensor(np.ascontiguousarray(table, dtype=np.int32)).to(dev)
     fl = torch.as_tensor(np.ascontiguousarray(flip, dtype=np.uint8)).to(dev)

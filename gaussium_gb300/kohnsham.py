@@ -83,6 +83,8 @@ class ExchangeCorrelationGPU:
         self.correlation = correlation
         self.alpha, self.vwn = params if params is not None else functional_params(exchange,
                                                                                     correlation)
+        if torch.device(device).type != "cuda":
+            raise _lib.GsError("the exchange-correlation quadrature runs on a CUDA device only")
         self.sb = basis_set if isinstance(basis_set, ShellBasis) else ShellBasis.from_functions(basis_set)
         self.ds = DeviceShells(self.sb, device)
         self.device = self.ds.device

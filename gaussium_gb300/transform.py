@@ -85,6 +85,8 @@ def transform_device(ao, c):
     n, m = c.shape
     if ao.shape != (n, n, n, n):
         raise ValueError(f"repulsion tensor {tuple(ao.shape)} does not match {n} basis functions")
+    if not (ao.is_cuda and c.is_cuda):
+        raise _lib.GsError("the AO -> MO transform runs on CUDA tensors only")
     ao = ao.contiguous()
     if torch.equal(ao, ao.transpose(0, 1)) and torch.equal(ao, ao.transpose(2, 3)):
         return transform_pair_symmetric(ao, c)
@@ -95,6 +97,8 @@ def spin_expand_device(mo, mode):
     """(2h)^4 spin-orbital tensor from an h^4 MO tensor on the device (``gs_spin_expand``)."""
     if mo.dim() != 4 or len(set(mo.shape)) != 1:
         raise ValueError(f"expected an h^4 tensor, got {tuple(mo.shape)}")
+    if not mo.is_cuda:
+        raise _lib.GsError("gs_spin_expand takes a CUDA tensor")
     mo = mo.to(torch.float64).contiguous()
     h = mo.shape[0]
     out = torch.empty((2 * h,) * 4, dtype=torch.float64, device=mo.device)

@@ -68,3 +68,22 @@ def test_transform_fails_loudly_without_gpu(monkeypatch):
                  lambda: transform.spin_basis_anti_physicist(x, device="cpu")):
         with pytest.raises(_lib.GsError):
             call()
+
+
+def test_new_drop_ins_refuse_cpu_tensors():
+    """CPU tensors never reach a kernel: the transform, the spin expansion, the symmetry
+    screen and the XC quadrature raise instead of passing host pointers or computing on
+    the host."""
+    import numpy as np
+    import torch
+    from gaussium_gb300 import _lib, dropin, kohnsham, transform
+    x = torch.zeros((2, 2, 2, 2), dtype=torch.float64)
+    with pytest.raises(_lib.GsError):
+        transform.transform_device(x, torch.eye(2, dtype=torch.float64))
+    with pytest.raises(_lib.GsError):
+        transform.spin_expand_device(x, 0)
+    with pytest.raises(_lib.GsError):
+        dropin.symmetry_zero(x, np.zeros((2, 1), np.int32), np.zeros((1, 8), np.uint8),
+                             np.zeros(2, np.int32), np.zeros(2, np.int32))
+    with pytest.raises(_lib.GsError):
+        kohnsham.ExchangeCorrelationGPU([], params=(2 / 3, None), device="cpu")
