@@ -39,6 +39,19 @@ def _check_sizes():
         raise _lib.GsError(f"record sizes mismatch: library {tuple(sizes)}")
 
 
+def _check_device_tensor(t, device, what, shape=None):
+    """Tensors handed to a kernel must be float64 on the engine's CUDA device (a host
+    pointer or a float32 buffer would be read as the wrong memory)."""
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
+        raise _lib.GsError(f"{what} must be a float64 CUDA tensor")
+    if t.device != torch.device(device) and torch.device(device).index is not None:
+        raise _lib.GsError(f"{what} is on {t.device}, the engine on {device}")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{what} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    if shape is None and not t.is_contiguous():
+        raise ValueError(f"{what} must be contiguous")
+
+
 class DeviceShells:
     """A ShellBasis copied to the device."""
 
@@ -180,6 +193,9 @@ class QuartetBatch:
         return {cls: e - s for cls, s, e in self.segments}
 
     def run(self, out, precision=64, stream=None, classes=None):
+        _check_device_tensor(out, self.ds.device, "output buffer")
+        if out.numel() < self.total:
+            raise ValueError(f"output buffer holds {out.numel()} doubles, the blocks need {self.total}")
         L = _lib.lib()
         st = _lib.stream(stream)
         base = self.tasks.data_ptr()
@@ -309,6 +325,8 @@ class JKEngine:
         dev = self.dev
         pk = list(pk)
         nk = len(pk)
+        for d in ([pj] if pj is not None else []) + pk:
+            _check_device_tensor(d, dev, "density matrix", (n, n))
         jbuf = torch.zeros((n, n), dtype=torch.float64, device=dev) if pj is not None else None
         kbuf = torch.zeros((max(nk, 1), n, n), dtype=torch.float64, device=dev) if nk else None
         pj_c = pj.contiguous() if pj is not None else None
