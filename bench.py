@@ -896,16 +896,7 @@ def run_xc(args, rank, world):
     if not args.no_cpu_baseline and rank == 0:
         # the oracle's restatement of integrate_potential (kohnsham/integration.py:26-40) on
         # a sample of matrix elements, scaled to the n(n+1)/2 the reference evaluates
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
-        from gaussium_gb300.basis import COMPONENTS
-        centre, lmn, cnorm, prims = [], [], [], []
-        for s in range(sb.nshell):
-            k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
-            for ci, c in enumerate(COMPONENTS[int(sb.l[s])]):
-                centre.append(sb.centre[s]); lmn.append(c); cnorm.append(sb.comp_scale[s, ci])
-                prims.append(list(zip(sb.coef[k0:k1], sb.expo[k0:k1], np.ones(k1 - k0))))
-        table = oracle.FunctionTable(np.array(centre), np.array(lmn), np.array(cnorm), prims)
+        oracle, table = oracle_table(sb)
         sample = 2
         t0 = time.perf_counter()
         for i in range(sample):
