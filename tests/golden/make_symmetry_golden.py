@@ -12,7 +12,8 @@ the basis arrays (as make_golden.py's ``basis_arrays``), the function-image tabl
 ``flip[m - 1, p] = (p != int_operate_dict[(m, p)])`` for the 8 parity vectors p (bit 0 x,
 bit 1 y, bit 2 z), the point-group label, and the reference's
 ``none_zero_integral`` (``common/symmetry.py:18-47``) for every canonical key
-a <= b, c <= d, (a, b) <= (c, d).
+a <= b, c <= d, (a, b) <= (c, d), in the order create_repulsion_matrix enumerates them
+(lexicographic; ``oracle.canonical_keys`` regenerates the list, so it is not stored).
 
 Systems: ethene/3-21G (the reference's own symmetry test, test_start.py:27-31), water/
 6-311+G** (d functions) and O2/STO-3G (test_start.py:33-43), all from the reference's
@@ -57,7 +58,7 @@ def system(mol_path, gbs):
     keys = np.array(keys, dtype=np.int32)
     mask = np.array([bool(sym.none_zero_integral(tuple(int(x) for x in k))) for k in keys])
     out = {"table": table, "flip": flip, "label": np.array(point_group.label),
-           "keys": keys, "nonzero": mask}
+           "nonzero": mask}
     out.update(make_golden.basis_arrays(basis))
     return out
 

@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 import torch
 
+import oracle
 from conftest import golden
 from molecules import functions
 from test_symmetry_logic import fake_reference_symmetry
@@ -25,7 +26,7 @@ def test_kernel_zeroes_exactly_the_reference_zeros(gpu_lib, name):
     n = len(funcs)
     t = torch.ones((n, n, n, n), dtype=torch.float64, device="cuda")
     dropin.symmetry_zero(t, *dropin.symmetry_tables(sym, funcs))
-    keys = torch.as_tensor(g[f"{name}_keys"].astype(np.int64)).cuda()
+    keys = torch.as_tensor(oracle.canonical_keys(g[f"{name}_table"].shape[0]).astype(np.int64)).cuda()
     got = t[keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3]].cpu().numpy()
     assert np.array_equal(got == 1.0, g[f"{name}_nonzero"])
     # every permutation of a key agrees with the key (the reference's 8-fold expansion)
@@ -43,7 +44,7 @@ def test_drop_in_tensor_with_symmetry(gpu_lib):
     funcs = system_functions(g, "ethene")
     full = TwoElectronRepulsionGPU(funcs, None, None, 1).create_repulsion_matrix()
     screened = TwoElectronRepulsionGPU(funcs, None, sym, 1).create_repulsion_matrix()
-    k = g["ethene_keys"]
+    k = oracle.canonical_keys(g["ethene_table"].shape[0])
     nz = g["ethene_nonzero"]
     vals = screened[k[:, 0], k[:, 1], k[:, 2], k[:, 3]]
     assert np.all(vals[~nz] == 0.0)

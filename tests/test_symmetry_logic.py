@@ -48,7 +48,7 @@ def test_tables_from_reference_object_give_reference_screen():
         table, flip, cid, par = dropin.symmetry_tables(sym, funcs)
         assert np.array_equal(table, g[f"{name}_table"])
         assert np.array_equal(flip.astype(bool), g[f"{name}_flip"])
-        keys, ref = g[f"{name}_keys"], g[f"{name}_nonzero"]
+        keys, ref = oracle.canonical_keys(g[f"{name}_table"].shape[0]), g[f"{name}_nonzero"]
         pick = np.random.default_rng(1).choice(len(keys), min(2000, len(keys)), replace=False)
         got = [oracle.symmetry_nonzero(table, flip.astype(bool), cid, par, keys[t]) for t in pick]
         assert np.array_equal(got, ref[pick]), name
