@@ -67,3 +67,26 @@ def test_xc_drop_in_fails_loudly_without_gpu(monkeypatch):
     with pytest.raises((_lib.GsError, RuntimeError, AssertionError)):
         kohnsham.ExchangeCorrelationGPU.__new__(kohnsham.ExchangeCorrelationGPU).functionals(
             torch.zeros(3, dtype=torch.float64), torch.zeros(3, dtype=torch.float64))
+
+
+def test_ks_scf_loop_reproduces_reference_he_energies():
+    """scf.ks_restricted_scf (the product's restatement of KSRestrictedSCF with DIIS) driven
+    by the oracle's J and XC on the host reaches the reference's He/STO-3G DFT energies."""
+    import oracle
+    from conftest import golden
+    from gaussium_gb300 import scf
+    he = oracle.FunctionTable.from_shells([dict(
+        l=0, centre=np.zeros(3), expo=np.array([6.36242139, 1.15892300, 0.31364979]),
+        coef=np.array([0.15432897, 0.53532814, 0.44463454]))])
+    S, T, V = oracle.one_centre_s(he, 2.0)
+    eri = oracle.dense_tensor(he)
+    g = golden("xc")
+    for vwn, key in ((None, "he_energy_s"), (oracle.VWN3, "he_energy_svwn3")):
+        class XC:
+            @staticmethod
+            def evaluate(p, vwn=vwn):
+                return (oracle.xc_potential_matrix(he, p, 2 / 3, vwn),
+                        oracle.xc_energy(he, p, 2 / 3, vwn))
+        res = scf.ks_restricted_scf(S, T + V, 2, lambda p: oracle.coulomb(eri, p), XC())
+        assert res["converged"]
+        assert abs(res["energy"] - float(g[key])) < 1e-8, key
