@@ -145,8 +145,9 @@ class ExchangeCorrelationGPU:
 
     # ------------------------------------------------------------------ reference surface
     def potential_matrix(self, density_matrix):
-        """All of integrate_potential(P, i, j) at once."""
-        return self.evaluate(density_matrix)[0]
+        """All of integrate_potential(P, i, j) at once (a copy: the cached matrix stays
+        intact if the caller updates the returned one in place)."""
+        return self.evaluate(density_matrix)[0].copy()
 
     def integrate_potential(self, density_matrix, i, j):
         return float(self.evaluate(density_matrix)[0][i, j])
