@@ -87,3 +87,9 @@ def test_new_drop_ins_refuse_cpu_tensors():
                              np.zeros(2, np.int32), np.zeros(2, np.int32))
     with pytest.raises(_lib.GsError):
         kohnsham.ExchangeCorrelationGPU([], params=(2 / 3, None), device="cpu")
+
+
+def test_every_entry_point_is_documented_for_integrators():
+    """Each C-ABI symbol the header declares has its row in INTEGRATION.md."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    assert [n for n in declared_symbols() if n not in doc] == []
