@@ -93,9 +93,13 @@ def generate():
             # no warp program: the warp kernels are never selected below WIDE_PROG_MIN
             inc = ('#include "eri_class_%s.h"\nnamespace gs { template <> struct WideProg<%d, %d, %d, %d> '
                    '{ static constexpr int NVSLOT = 1, NVSEG = 0, VGROUP = 1, HSIZE = 1, NHLEV = 0; '
+                   'static constexpr int NVSLOT_G = 1, NVSEG_G = 0; '
                    'static __device__ const uint4* vrec() { return nullptr; } '
                    'static __device__ const int* vseg() { return nullptr; } '
                    'static __device__ const unsigned short* vtgt() { return nullptr; } '
+                   'static __device__ const uint4* vrec_g() { return nullptr; } '
+                   'static __device__ const int* vseg_g() { return nullptr; } '
+                   'static __device__ const unsigned short* vtgt_g() { return nullptr; } '
                    'static __device__ const unsigned int* hop() { return nullptr; } '
                    'static __device__ const int* hlev() { return nullptr; } '
                    'static __device__ const unsigned short* outslot() { return nullptr; } }; }\n'

@@ -83,26 +83,18 @@ GS_HD GS_INLINE float gs_exp(float x) {
 }
 
 // ------------------------------------------------------------------ Boys function
+// F_m(T_k) and e^{-T_k} on the grid T_k = k / BOYS_INV_H (FP64; FP32 quartets evaluate
+// the small-T branch in FP64 too)
 #if defined(__CUDACC__)
 __device__ const double g_boys_d[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
-__device__ const float g_boys_f[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
 #endif
 static const double h_boys_d[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
-static const float h_boys_f[BOYS_ROWS * BOYS_NCOL] = {GS_BOYS_TABLE_VALUES};
 
-template <typename T> GS_HD GS_INLINE const T* boys_table();
-template <> GS_HD GS_INLINE const double* boys_table<double>() {
+GS_HD GS_INLINE const double* boys_table() {
 #if defined(__CUDA_ARCH__)
     return g_boys_d;
 #else
     return h_boys_d;
-#endif
-}
-template <> GS_HD GS_INLINE const float* boys_table<float>() {
-#if defined(__CUDA_ARCH__)
-    return g_boys_f;
-#else
-    return h_boys_f;
 #endif
 }
 
@@ -114,52 +106,53 @@ template <typename T> GS_HD GS_INLINE T ldg(const T* p) {
 #endif
 }
 
-// F[m] = pref * F_m(t), m = 0..M.  Below BOYS_TMAX: Taylor expansion of F_M about the
-// nearest grid point (7 terms in double, 4 in float) and downward recursion.  Above it:
-// F_0 = sqrt(pi/t)/2 (erf(sqrt t) = 1 to 2e-17) and upward recursion, stable for t > M.
+// Boys function below BOYS_TMAX, always in FP64: 7-term Taylor expansion of F_M about the
+// nearest grid point (grid step 1/BOYS_INV_H), then downward recursion
+//   F_{m-1}(t) = (2t F_m(t) + e^{-t}) / (2m - 1),
+// stable downwards; e^{-t} comes from the tabulated e^{-t_k} times the Taylor series of
+// e^{-(t - t_k)}.  F[m] = pref * F_m(t).
+template <int M>
+GS_HD GS_INLINE void boys_small(double t, double pref, double* __restrict__ F) {
+    const int k = (int)(t * BOYS_INV_H + 0.5);
+    const double d = k * (1.0 / BOYS_INV_H) - t;
+    const double* row = boys_table() + k * BOYS_NCOL;
+    const double d2 = d * (1.0 / 2), d3 = d * (1.0 / 3), d4 = d * (1.0 / 4);
+    const double d5 = d * (1.0 / 5), d6 = d * (1.0 / 6);
+    double f = ldg(row + M + 6);
+    f = f * d6 + ldg(row + M + 5);
+    f = f * d5 + ldg(row + M + 4);
+    f = f * d4 + ldg(row + M + 3);
+    f = f * d3 + ldg(row + M + 2);
+    f = f * d2 + ldg(row + M + 1);
+    f = f * d + ldg(row + M);
+    F[M] = f * pref;
+    if (M > 0) {
+        double e = d6 + 1.0;
+        e = e * d5 + 1.0;
+        e = e * d4 + 1.0;
+        e = e * d3 + 1.0;
+        e = e * d2 + 1.0;
+        e = e * d + 1.0;
+        const double et = e * ldg(row + BOYS_NCOL - 1) * pref;
+        const double t2 = t + t;
+        GS_UNROLL for (int m = M; m >= 1; --m) F[m - 1] = (t2 * F[m] + et) * (1.0 / (2 * m - 1));
+    }
+}
+
+// F[m] = pref * F_m(t), m = 0..M.  Below BOYS_TMAX: boys_small in FP64 for either T (in
+// FP32 quartets the FP64 values are rounded to float once, so neither the series nor the
+// downward recursion accumulates FP32 rounding).  Above it: F_0 = sqrt(pi/t)/2
+// (erf(sqrt t) = 1 to 2e-17) and upward recursion in T, stable for t > M.
 template <int M, typename T>
 GS_HD GS_INLINE void boys(T t, T pref, T* __restrict__ F) {
     constexpr bool dbl = sizeof(T) == 8;
     if (t < T(BOYS_TMAX)) {
-        const int k = (int)(t * T(BOYS_INV_H) + T(0.5));
-        const T d = T(k) * T(1.0 / BOYS_INV_H) - t;
-        const T* row = boys_table<T>() + k * BOYS_NCOL;
-        T f, e;
-        if (dbl) {
-            const T d2 = d * T(1.0 / 2), d3 = d * T(1.0 / 3), d4 = d * T(1.0 / 4);
-            const T d5 = d * T(1.0 / 5), d6 = d * T(1.0 / 6);
-            f = ldg(row + M + 6);
-            f = f * d6 + ldg(row + M + 5);
-            f = f * d5 + ldg(row + M + 4);
-            f = f * d4 + ldg(row + M + 3);
-            f = f * d3 + ldg(row + M + 2);
-            f = f * d2 + ldg(row + M + 1);
-            f = f * d + ldg(row + M);
-            if (M > 0) {
-                e = d6 + T(1);
-                e = e * d5 + T(1);
-                e = e * d4 + T(1);
-                e = e * d3 + T(1);
-                e = e * d2 + T(1);
-                e = e * d + T(1);
-            }
+        if constexpr (dbl) {
+            boys_small<M>(t, pref, F);
         } else {
-            const T d2 = d * T(1.0 / 2), d3 = d * T(1.0 / 3);
-            f = ldg(row + M + 3);
-            f = f * d3 + ldg(row + M + 2);
-            f = f * d2 + ldg(row + M + 1);
-            f = f * d + ldg(row + M);
-            if (M > 0) {
-                e = d3 + T(1);
-                e = e * d2 + T(1);
-                e = e * d + T(1);
-            }
-        }
-        F[M] = f * pref;
-        if (M > 0) {
-            const T et = e * ldg(row + BOYS_NCOL - 1) * pref;
-            const T t2 = t + t;
-            GS_UNROLL for (int m = M; m >= 1; --m) F[m - 1] = (t2 * F[m] + et) * T(1.0 / (2 * m - 1));
+            double Fd[M + 1];
+            boys_small<M>((double)t, (double)pref, Fd);
+            GS_UNROLL for (int m = 0; m <= M; ++m) F[m] = (T)Fd[m];
         }
     } else {
         const T rs = gs_rsqrt(t);

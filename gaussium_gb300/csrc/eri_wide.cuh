@@ -27,6 +27,9 @@ template <int LA, int LB, int LC, int LD> struct WideProg;
 #endif
 constexpr int kWideWarps = GS_WIDE_WARPS;     // warps per block
 constexpr int kNCoef = 32;                    // coefficient slots per primitive quartet
+// coefficient slot set to zero after the set-up: the padding term of nodes whose wave holds
+// nodes with more terms (gen_eri.py ZERO_COEF; the i2p_4 slot, unused up to (dd|dd))
+constexpr int kZeroCoef = 15;
 constexpr int kSetupBatch = GS_SETUP_BATCH;   // primitive quartets prepared per setup round
 static_assert(kSetupBatch >= 1 && kSetupBatch <= 32, "one primitive quartet per lane at most");
 static_assert(kWideWarps >= 1 && kWideWarps <= 32, "warps per block");
@@ -37,10 +40,12 @@ template <int LA, int LB, int LC, int LD, typename T, int VG = 1> struct WideLay
     using W = WideProg<LA, LB, LC, LD>;
     // primitive quartets set up per round: a grouped form with large node buffers prepares
     // half as many, so that its shared memory stays near the ungrouped form's
-    static constexpr int SB = (VG > 1 && VG * W::NVSLOT > 1024 && kSetupBatch > 16) ? 16 : kSetupBatch;
+    // node slots of the program this form runs (the grouped form has its own schedule)
+    static constexpr int NVS = VG == 1 ? W::NVSLOT : W::NVSLOT_G;
+    static constexpr int SB = (VG > 1 && VG * NVS > 1024 && kSetupBatch > 16) ? 16 : kSetupBatch;
     static constexpr int SC = SB * kNCoef;                       // coefficients
     static constexpr int SF = SB * (G::L + 1);                   // Boys values
-    static constexpr int VRR = SC + SF + VG * W::NVSLOT;
+    static constexpr int VRR = SC + SF + VG * NVS;
     // write/Schwarz epilogues need the HRR buffer and the scale vectors; the J/K epilogue
     // also a scaled copy of the block
     static constexpr int HR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
@@ -103,15 +108,20 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     T* node = sm + Lay::SC + Lay::SF;
     const int nK = K.nprim;
     const int ntot = B.nprim * nK;
-    const uint4* __restrict__ vrec = W::vrec();
-    const int* __restrict__ vseg = W::vseg();
-    const unsigned short* __restrict__ vtgt = W::vtgt();
+    // the node program: waves of at most 32 nodes (one per lane), or of 32/VG nodes for the
+    // grouped form (one per lane group of VG primitive quartets)
+    constexpr int NVS = Lay::NVS;
+    constexpr int NVSEG = VG == 1 ? W::NVSEG : W::NVSEG_G;
+    const uint4* __restrict__ vrec = VG == 1 ? W::vrec() : W::vrec_g();
+    const int* __restrict__ vseg = VG == 1 ? W::vseg() : W::vseg_g();
+    const unsigned short* __restrict__ vtgt = VG == 1 ? W::vtgt() : W::vtgt_g();
     for (int base = 0; base < ntot; base += Lay::SB) {
         const int i = base + lane;
         if (lane < Lay::SB && i < ntot) {
             const PrimRec<T> P = prims[B.prim_off + i / nK];
             const PrimRec<T> Q = prims[K.prim_off + i % nK];
             wide_setup_m<L, T>(P, Q, sC + lane * kNCoef, sF + lane * (L + 1));
+            sC[lane * kNCoef + kZeroCoef] = T(0);
         }
         __syncwarp();
         const int nb = min(Lay::SB, ntot - base);
@@ -120,7 +130,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
             const T* __restrict__ c = sC + j * kNCoef;
             if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
             __syncwarp();
-            for (int s = 0; s < W::NVSEG; ++s) {
+            for (int s = 0; s < NVSEG; ++s) {
                 const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
                 const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
                 if (sync && s > 0) __syncwarp();
@@ -160,10 +170,10 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
             const int ng = min(VG, nb - j0);
             for (int x = lane; x < ng * (L + 1); x += 32) {
                 const int g = x / (L + 1), m = x - g * (L + 1);
-                node[g * W::NVSLOT + m] = sF[(j0 + g) * (L + 1) + m];
+                node[g * NVS + m] = sF[(j0 + g) * (L + 1) + m];
             }
             __syncwarp();
-            for (int s = 0; s < W::NVSEG; ++s) {
+            for (int s = 0; s < NVSEG; ++s) {
                 const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
                 const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
                 if (sync && s > 0) __syncwarp();
@@ -173,7 +183,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                     const uint4 a = __ldg(vrec + 2 * (noff + n));
                     const uint4 b = __ldg(vrec + 2 * (noff + n) + 1);
                     const T* __restrict__ c = sC + (j0 + g) * kNCoef;
-                    T* nd = node + g * W::NVSLOT;
+                    T* nd = node + g * NVS;
                     T r = c[a.y >> 16] * nd[a.y & 0xffff];
                     r = fma(c[a.z >> 16], nd[a.z & 0xffff], r);
                     if (nt > 2) r = fma(c[a.w >> 16], nd[a.w & 0xffff], r);
@@ -188,7 +198,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                 const int t = lane + 32 * k;
                 if (t < NACC) {
                     const int v = __ldg(vtgt + t);
-                    for (int g = 0; g < ng; ++g) acc[k] += node[g * W::NVSLOT + v];
+                    for (int g = 0; g < ng; ++g) acc[k] += node[g * NVS + v];
                 }
             }
             __syncwarp();

@@ -393,10 +393,100 @@ def _release(free, start, size):
     free[:] = merged
 
 
-def wide_program(cls):
-    """Tables for the warp-cooperative kernel of one class: VRR node descriptors grouped
-    by dependency level and term count, the targets' slots, and the HRR element
-    operations on a liveness-planned shared buffer."""
+# Coefficient slot that the warp kernels set to zero: the term a node is padded with when
+# its wave holds nodes with more terms.  It is the i2p_4 slot, which no class up to
+# (dd|dd) reads (the bra step uses (e-1_i)_i <= la+lb-1 <= 3).
+ZERO_COEF = 15
+
+
+def vrr_waves(nodes, L, target_slots, wave=32):
+    """Schedule the VRR nodes of one primitive quartet for a warp.
+
+    ``nodes``: (virtual slot, [(coefficient id, operand slot), ...]) in dependency order;
+    slots 0..L are the scaled Boys values.  Returns (vrec, vseg, phys, nvslot).
+
+    The warp evaluates the nodes in waves of at most ``wave`` nodes, one node per lane (or
+    per lane group of the grouped form, which runs 32/wave primitive quartets at once).
+    Each wave costs as many FP64 instructions as its largest term count whatever its
+    active lanes, so the scheduler fills waves completely: at each step it takes the nodes
+    whose operands are all done, most critical (longest path to a target) first, and
+    emits as many full waves as it can, a partial one only when nothing else is ready.
+    Nodes of a wave with fewer terms are padded with (ZERO_COEF x node 0).  Waves of one
+    step read only values of earlier steps, so the kernel synchronises the warp at the
+    first wave of each step only.  Slots are assigned by liveness over steps: a slot last
+    read in step s is reused from step s+1 on; targets and Boys values live to the end."""
+    import collections
+    byout = {o: ts for o, ts in nodes}
+    users = collections.defaultdict(list)
+    for o, ts in nodes:
+        for _, s in ts:
+            users[s].append(o)
+    height = {}
+    for o, ts in reversed(nodes):
+        height[o] = 1 + max((height[u] for u in users[o]), default=0)
+    done = set(range(L + 1))
+    pending = set(byout)
+    steps = []
+    while pending:
+        ready = [o for o in pending if all(s in done for _, s in byout[o])]
+        ready.sort(key=lambda o: (-height[o], -len(byout[o]), o))
+        nfull = len(ready) // wave
+        take = ready[:nfull * wave] if nfull else ready
+        take.sort(key=lambda o: (-len(byout[o]), o))
+        steps.append([take[i:i + wave] for i in range(0, len(take), wave)])
+        done |= set(take)
+        pending -= set(take)
+    step_of = {o: k for k, st in enumerate(steps) for w in st for o in w}
+    last = {}
+    for o, ts in nodes:
+        for _, s in ts:
+            last[s] = max(last.get(s, 0), step_of[o])
+    for s in target_slots:
+        last[s] = len(steps)
+    phys = {m: m for m in range(L + 1)}
+    free, top = [], L + 1
+    for k, st in enumerate(steps):
+        for w in st:
+            for o in w:
+                if free:
+                    phys[o] = free.pop()
+                else:
+                    phys[o] = top
+                    top += 1
+        for s, lu in last.items():
+            if lu == k and s > L:
+                free.append(phys[s])
+        free.sort(reverse=True)
+    vrec, vseg = [], []
+    for k, st in enumerate(steps):
+        for i, w in enumerate(st):
+            nt = max(len(byout[o]) for o in w)
+            vseg.append([len(vrec) // 8, 0, len(w), nt, k, 1 if (i == 0 and k > 0) else 0])
+            for o in w:
+                ts = byout[o]
+                assert all(cid != ZERO_COEF for cid, _ in ts), "zero slot in use"
+                words = [phys[o] | (nt << 16)] + [(cid << 16) | phys[s] for cid, s in ts]
+                words += [(ZERO_COEF << 16)] * (nt - len(ts))
+                words += [0] * (8 - len(words))
+                vrec.extend(words)
+    return vrec, vseg, phys, top
+
+
+def wave_efficiency(vrec, vseg, lanes_per_node=1):
+    """Useful FMA lane-slots over issued lane-slots of a scheduled VRR program."""
+    useful = issued = 0
+    for noff, _, cnt, nt, _, _ in vseg:
+        for n in range(cnt):
+            useful += sum(1 for w in vrec[8 * (noff + n) + 1: 8 * (noff + n) + 1 + nt]
+                          if (w >> 16) != ZERO_COEF)
+        issued += 32 * nt
+    return useful * lanes_per_node / issued
+
+
+def wide_program(cls, wave=32):
+    """Tables for the warp-cooperative kernel of one class: VRR node descriptors packed
+    into waves of ``wave`` independent nodes (vrr_waves), the targets' slots, and the HRR
+    element operations on a liveness-planned shared buffer."""
     la, lb, lc, ld = cls
     v = VrrGen(cls).build()
     h = HrrGen(cls, v.e_targets, v.f_targets).build()
@@ -412,61 +502,12 @@ def wide_program(cls):
             return int(opnd[2:-1])
         return L + 1 + int(opnd[1:])
 
-    level = {}
-    for m in range(L + 1):
-        level[m] = 0
-    nodes = []
-    for idx, terms in enumerate(v.struct):
-        ts = [(COEF_ID[c], slot(x)) for c, x in terms]
-        lv = 1 + max(level[s] for _, s in ts)
-        level[L + 1 + idx] = lv
-        nodes.append((lv, len(ts), L + 1 + idx, ts))
-    nodes.sort(key=lambda n: (n[0], n[1], n[2]))
+    nodes = [(L + 1 + idx, [(COEF_ID[c], slot(x)) for c, x in terms])
+             for idx, terms in enumerate(v.struct)]
     tgt = [v.names[(e, f, 0)] if not (e == (0, 0, 0) and f == (0, 0, 0)) else "F[0]"
            for e in v.e_targets for f in v.f_targets]
-    tslots = set(slot(t) for t in tgt)
-    # liveness: a node's slot is free after the last level that reads it; targets and
-    # the Boys values live to the end of the primitive quartet
-    maxlv = max((n[0] for n in nodes), default=0)
-    last = {}
-    for lv, nt, out, ts in nodes:
-        for _, sl in ts:
-            last[sl] = max(last.get(sl, 0), lv)
-    for sl in tslots:
-        last[sl] = maxlv + 1
-    phys = {m: m for m in range(L + 1)}
-    free = []
-    top = L + 1
-    by_level = {}
-    for n in nodes:
-        by_level.setdefault(n[0], []).append(n)
-    for lv in sorted(by_level):
-        for n in by_level[lv]:
-            if free:
-                phys[n[2]] = free.pop()
-            else:
-                phys[n[2]] = top
-                top += 1
-        for sl, lu in last.items():
-            if lu == lv and sl > L:
-                free.append(phys[sl])
-        free.sort(reverse=True)
-    vrec, vseg = [], []
-    i = 0
-    while i < len(nodes):
-        j = i
-        while j < len(nodes) and nodes[j][:2] == nodes[i][:2]:
-            j += 1
-        lv, nt = nodes[i][:2]
-        sync = 1 if (not vseg or vseg[-1][4] != lv) else 0
-        vseg.append([len(vrec) // 8, 0, j - i, nt, lv, sync])
-        for n in nodes[i:j]:
-            words = [phys[n[2]] | (nt << 16)] + [(cid << 16) | phys[sl] for cid, sl in n[3]]
-            words += [0] * (8 - len(words))
-            vrec.extend(words)
-        i = j
+    vrec, vseg, phys, nvslot = vrr_waves(nodes, L, [slot(t) for t in tgt], wave)
     vtgt = [phys[slot(t)] for t in tgt]
-    nvslot = top
     vout, vdesc = [], []
     # ---- HRR: arrays, levels, liveness
     arrays = {}          # name -> (size, producer level)
@@ -566,53 +607,62 @@ def wide_program(cls):
 VGROUP_SLOT_BUDGET = 2600     # node slots (doubles) the grouped VRR buffers may take per warp
 
 
-def vrr_group(vseg, nvslot):
-    """Primitive quartets a warp runs through the VRR node program at once: the smallest
-    of 1, 2, 4, 8 that fills at least 85 % of the lanes of the program's segments (or the
-    best within the buffer budget)."""
-    def eff(g):
-        useful = slots = 0
-        for s in vseg:
-            cnt, nt = s[2], s[3]
-            useful += g * cnt * nt
-            slots += -(-g * cnt // 32) * 32 * nt
-        return useful / max(1, slots)
-    best = 1
-    for g in (1, 2, 4, 8):
-        if g * nvslot > VGROUP_SLOT_BUDGET and g > 1:
+def vrr_group(cls):
+    """Primitive quartets the grouped warp form runs through the VRR at once, with its
+    program (waves of 32/VG nodes, so a wave of VG quartets fills the warp): the smallest
+    of 2, 4, 8 whose program fills at least 95 % of the lanes, or the best within the
+    buffer budget.  Returns (VG, program), VG = 1 when no grouped form pays."""
+    base = wide_program(cls, 32)
+    best, best_eff, best_p = 1, wave_efficiency(base["vrec"], base["vseg"]), base
+    if best_eff >= 0.95:
+        return 1, base
+    for g in (2, 4, 8):
+        p = wide_program(cls, 32 // g)
+        if g * p["nvslot"] > VGROUP_SLOT_BUDGET:
             break
-        if eff(g) > eff(best) + 0.02:
-            best = g
-        if eff(g) >= 0.85:
+        e = wave_efficiency(p["vrec"], p["vseg"], g)
+        if e > best_eff + 0.02:
+            best, best_eff, best_p = g, e, p
+        if e >= 0.95:
             break
-    return best
+    return best, best_p
 
 
 def emit_wide(cls):
     p = wide_program(cls)
+    vg, pg = vrr_group(cls)
     tag = "".join(map(str, cls))
     la, lb, lc, ld = cls
 
     def arr(ctype, name, vals):
         body = ",".join(str(x) for x in vals) if vals else "0"
         return f"__device__ const {ctype} {name}[{max(1, len(vals))}] = {{{body}}};"
-    segs = [x for s in p["vseg"] for x in (s[0], s[2], s[3], s[5])]
+
+    def segs(q):
+        return [x for s in q["vseg"] for x in (s[0], s[2], s[3], s[5])]
     hop = [x for o in p["hops"] for x in (o[0] | (o[1] << 16), o[2] | (o[3] << 16))]
     out = [f"// generated by gen_eri.py -- warp program of class ({la}{lb}|{lc}{ld})",
            "#pragma once", "namespace gs {",
            arr("unsigned int __align__(16)", f"w{tag}_vrec", p["vrec"]),
-           arr("int", f"w{tag}_vseg", segs),
+           arr("int", f"w{tag}_vseg", segs(p)),
            arr("unsigned short", f"w{tag}_vtgt", p["vtgt"]),
+           arr("unsigned int __align__(16)", f"w{tag}_vrecg", pg["vrec"]),
+           arr("int", f"w{tag}_vsegg", segs(pg)),
+           arr("unsigned short", f"w{tag}_vtgtg", pg["vtgt"]),
            arr("unsigned int", f"w{tag}_hop", hop),
            arr("int", f"w{tag}_hlev", p["hlev"]),
            arr("unsigned short", f"w{tag}_out", p["outslot"]),
            f"template <> struct WideProg<{la}, {lb}, {lc}, {ld}> {{",
            f"  static constexpr int NVSLOT = {p['nvslot']}, NVSEG = {len(p['vseg'])}, "
-           f"VGROUP = {vrr_group(p['vseg'], p['nvslot'])};",
+           f"VGROUP = {vg};",
+           f"  static constexpr int NVSLOT_G = {pg['nvslot']}, NVSEG_G = {len(pg['vseg'])};",
            f"  static constexpr int HSIZE = {p['hsize']}, NHLEV = {len(p['hlev']) - 1};",
            f"  static __device__ const uint4* vrec() {{ return reinterpret_cast<const uint4*>(w{tag}_vrec); }}",
            f"  static __device__ const int* vseg() {{ return w{tag}_vseg; }}",
            f"  static __device__ const unsigned short* vtgt() {{ return w{tag}_vtgt; }}",
+           f"  static __device__ const uint4* vrec_g() {{ return reinterpret_cast<const uint4*>(w{tag}_vrecg); }}",
+           f"  static __device__ const int* vseg_g() {{ return w{tag}_vsegg; }}",
+           f"  static __device__ const unsigned short* vtgt_g() {{ return w{tag}_vtgtg; }}",
            f"  static __device__ const unsigned int* hop() {{ return w{tag}_hop; }}",
            f"  static __device__ const int* hlev() {{ return w{tag}_hlev; }}",
            f"  static __device__ const unsigned short* outslot() {{ return w{tag}_out; }}",

@@ -1,8 +1,9 @@
 /*
  * gaussium_gb300 -- C ABI of the GB300 (sm_103a) two-electron-integral and Fock-build
  * engine.  The reference Gaussium is pure Python and has no FFI; these entry points are
- * what its ERI path binds through ctypes.  Each one cites the
- * reference function it replaces (file:line within the reference project).
+ * what its ERI path binds through ctypes (the Python package gaussium_gb300 is that
+ * binding).  Each one cites the reference function it replaces (file:line within the
+ * reference project).
  *
  * Conventions
  *   - All array arguments are DEVICE pointers owned by the caller (torch tensors in the

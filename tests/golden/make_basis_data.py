@@ -3,12 +3,12 @@ the reference's example GAMESS-UK files into gaussium_gb300/data/basis_sets.json
 
 Basis-set exponents and contraction coefficients are published data (Hehre, Stewart &
 Pople 1969; Hehre, Ditchfield & Pople 1972; Hariharan & Pople 1973); 6-31G is 6-31G*
-without its d shells.  Run here once:  python make_basis_data.py
+without its d shells.  Run once, with GAUSSIUM_REFERENCE set to the reference source tree:
+    GAUSSIUM_REFERENCE=<tree> python make_basis_data.py
 """
 import json
 import os
 
-REF = "/root/reference/examples/basissets"
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "..", "..", "gaussium_gb300", "data", "basis_sets.json")
 ELEMENTS = {"HYDROGEN": "H", "CARBON": "C", "NITROGEN": "N", "OXYGEN": "O", "HELIUM": "He"}
@@ -37,6 +37,10 @@ def parse(path):
 
 
 def main():
+    root = os.environ.get("GAUSSIUM_REFERENCE")
+    if not root:
+        raise SystemExit("set GAUSSIUM_REFERENCE to the reference source tree")
+    REF = os.path.join(root, "examples", "basissets")
     sto = parse(os.path.join(REF, "STO-3G.gbs"))
     p631s = parse(os.path.join(REF, "6-31GP.gbs"))
     p631 = {el: [s for s in shells if s["type"] != "D"] for el, shells in p631s.items()}

@@ -1,7 +1,8 @@
 """Generate the golden vectors in ``tests/golden/`` by running the reference Gaussium here.
 
 Run from this directory:  ``python make_golden.py [--quick]``.  It needs the reference
-source tree (``ref_harness.REFERENCE_SRC``) and writes only ``*.npz`` files beside itself.
+source tree (the GAUSSIUM_REFERENCE environment variable, read by ``ref_harness``) and
+writes only ``*.npz`` files beside itself.
 The fixtures it writes are committed; the GPU tests read them and never the reference.
 
 Each file records what produced it:
@@ -40,7 +41,6 @@ sys.path.insert(0, HERE)
 import ref_harness  # noqa: E402
 
 BOHR_PER_ANGSTROM = 1.0 / 0.529177210903
-REF = "/root/reference"
 COMPONENTS = {0: [(0, 0, 0)],
               1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)],
               2: [(2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)]}
@@ -195,7 +195,7 @@ def make_h2o_sto3g(procs):
     from gaussium.kohnsham.kohn_sham_hamiltonian import RestrictedKohnShamHamiltonian
     from gaussium.matrixelements import blocked_spin_basis_set
     mol = write_tmp("h2o.mol", water_mol_text())
-    nuclei, electrons, mult, basis = load_molecule(mol, f"{REF}/examples/basissets/STO-3G.gbs")
+    nuclei, electrons, mult, basis = load_molecule(mol, f"{ref_harness.reference_root()}/examples/basissets/STO-3G.gbs")
     keys, vals = eri_all(basis, procs)
     dense = quiet(TwoElectronRepulsionMatrixOS(basis, ref_harness.c1_symmetry(basis), 1).create_repulsion_matrix)
     dense = np.asarray(dense)
@@ -233,8 +233,8 @@ def one_electron(nuclei, basis):
 
 
 def make_h2o_631gs(procs):
-    nuclei, electrons, mult, basis = load_molecule(f"{REF}/examples/molfiles/H2O.mol",
-                                                   f"{REF}/examples/basissets/6-31GP.gbs")
+    nuclei, electrons, mult, basis = load_molecule(f"{ref_harness.reference_root()}/examples/molfiles/H2O.mol",
+                                                   f"{ref_harness.reference_root()}/examples/basissets/6-31GP.gbs")
     keys, vals = eri_all(basis, procs)
     energy, iters = run_rhf(nuclei, electrons, basis, procs)
     np.savez_compressed(os.path.join(HERE, "h2o_631gs.npz"), keys=keys, eri=vals, energy=energy,
@@ -353,7 +353,7 @@ def make_energies(procs):
     from gaussium.energy import Energy
     from gaussium.hartreefock import RestrictedHF
     out = {}
-    d = f"{REF}/tests/testslow/start"
+    d = f"{ref_harness.reference_root()}/tests/testslow/start"
     nuclei, electrons, mult, basis = load_molecule(f"{d}/HeH+.mol", f"{d}/STO-3G.gbs")
     out["heh_sto3g_rhf"], out["heh_sto3g_rhf_iterations"] = run_rhf(nuclei, electrons, basis, procs)
     np.savez_compressed(os.path.join(HERE, "heh_sto3g.npz"), electrons=electrons, multiplicity=mult,

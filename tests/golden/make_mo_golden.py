@@ -1,7 +1,7 @@
 """Generate ``mo_transform.npz`` by running the reference's transformations here.
 
 Run from this directory:  ``python make_mo_golden.py``.  It needs the reference source tree
-(``ref_harness.REFERENCE_SRC``) and ``h2o_sto3g.npz`` (the water/STO-3G dense tensor written
+(the GAUSSIUM_REFERENCE environment variable) and ``h2o_sto3g.npz`` (the water/STO-3G dense tensor written
 by make_golden.py); it writes only ``mo_transform.npz`` beside itself.  Contents: a seeded
 orthogonal coefficient matrix C and the reference outputs of
 ``matrixelements/transformations.py``: ``molecular_orbitals`` (lines 5-26),

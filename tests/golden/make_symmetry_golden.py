@@ -1,7 +1,7 @@
 """Generate ``symmetry.npz`` by running the reference's point-group screening here.
 
 Run from this directory:  ``python make_symmetry_golden.py``.  It needs the reference source
-tree (``ref_harness.REFERENCE_SRC``); it writes only ``symmetry.npz`` beside itself.
+tree (the GAUSSIUM_REFERENCE environment variable); it writes only ``symmetry.npz`` beside itself.
 
 For each system the reference's ``MoleculeFactory(symmetry=True).create`` orients the
 nuclei and finds the point group (``factory/molecule_factory.py``), ``read_basis_set_file``
@@ -29,7 +29,7 @@ sys.path.insert(0, HERE)
 import ref_harness  # noqa: E402
 import make_golden  # noqa: E402
 
-START = os.path.join(make_golden.REF, "tests", "testslow", "start")
+START = os.path.join(make_golden.ref_harness.reference_root(), "tests", "testslow", "start")
 PARITIES = [(p & 1, (p >> 1) & 1, (p >> 2) & 1) for p in range(8)]
 
 

@@ -1,7 +1,7 @@
 """Generate ``xc.npz`` by running the reference's exchange-correlation code here.
 
 Run from this directory:  ``python make_xc_golden.py``.  It needs the reference source tree
-(``ref_harness.REFERENCE_SRC``); it writes only ``xc.npz`` beside itself.  Contents:
+(the GAUSSIUM_REFERENCE environment variable); it writes only ``xc.npz`` beside itself.  Contents:
 
 * ``density``: densities from 1e-14 to 1e3 and exactly 0, and at each of them the
   reference's ``SlaterExchange(alpha).energy/potential`` for alpha = 2/3 and 0.7
@@ -46,7 +46,7 @@ def main():
         out[f"{tag}_potential"] = np.array([float(c.potential(d)) for d in density])
 
     mol = make_golden.write_tmp("water.mol", make_golden.water_mol_text())
-    gbs = os.path.join(make_golden.REF, "tests", "testslow", "start", "STO-3G.gbs")
+    gbs = os.path.join(make_golden.ref_harness.reference_root(), "tests", "testslow", "start", "STO-3G.gbs")
     _, _, _, basis = make_golden.load_molecule(mol, gbs)
     n = len(basis)
     rng = np.random.default_rng(31)

@@ -23,7 +23,16 @@ import os
 import sys
 import types
 
-REFERENCE_SRC = os.environ.get("GAUSSIUM_REFERENCE_SRC", "/root/reference/src")
+
+def reference_root():
+    """Root of the reference source tree, from the GAUSSIUM_REFERENCE environment variable
+    (the directory holding ``src/gaussium`` and ``examples/``).  There is no default."""
+    root = os.environ.get("GAUSSIUM_REFERENCE")
+    if not root or not os.path.isdir(os.path.join(root, "src", "gaussium")):
+        raise RuntimeError("set GAUSSIUM_REFERENCE to the reference Gaussium source tree "
+                           "(the directory with src/gaussium and examples/)")
+    return root
+
 
 _loaded = None
 
@@ -68,8 +77,9 @@ def load():
         np.linalg.linalg = types.SimpleNamespace(LinAlgError=np.linalg.LinAlgError)
     elif not hasattr(np.linalg.linalg, "LinAlgError"):
         np.linalg.linalg.LinAlgError = np.linalg.LinAlgError
-    if REFERENCE_SRC not in sys.path:
-        sys.path.insert(0, REFERENCE_SRC)
+    src = os.path.join(reference_root(), "src")
+    if src not in sys.path:
+        sys.path.insert(0, src)
     import gaussium  # noqa: F401
 
     proxy = _make_np_proxy(np)

@@ -16,9 +16,14 @@ sys.path.insert(0, os.path.join(ROOT, "gaussium_gb300", "csrc"))
 import gen_eri  # noqa: E402
 
 
-def emulate(cls, pr, pd, bra, ket):
-    """Run the warp program of `cls` for quartet (bra|ket) with numpy, sequentially."""
+def emulate(cls, pr, pd, bra, ket, grouped=False):
+    """Run the warp program of `cls` (the grouped form's with ``grouped``) for quartet
+    (bra|ket) with numpy.  Writes of a synchronisation step become visible only at the
+    next step, as on the GPU, where the lanes of one step run in no fixed order."""
     p = gen_eri.wide_program(cls)
+    if grouped:
+        pv = gen_eri.vrr_group(cls)[1]
+        p = dict(p, vrec=pv["vrec"], vseg=pv["vseg"], vtgt=pv["vtgt"], nvslot=pv["nvslot"])
     L = p["L"]
     B, K = pr[bra], pr[ket]
     acc = np.zeros(p["nacc"])
@@ -38,22 +43,32 @@ def emulate(cls, pr, pd, bra, ket):
             for k in range(1, 5):
                 c[11 + k] = k * i2p; c[15 + k] = -k * wq * i2p; c[19 + k] = k * i2q
                 c[23 + k] = -k * wp * i2q; c[27 + k] = k * 0.5 / pq
+            c[gen_eri.ZERO_COEF] = 0.0          # padding terms of short nodes in a wave
             node = np.zeros(p["nvslot"])
             node[:L + 1] = F
             rec = p["vrec"]
+            new, reads = {}, set()
             for noff, _, cnt, nt, lv, sync in p["vseg"]:
-                new = {}
+                assert cnt <= 32
+                if sync:
+                    # no lane of a step may overwrite a slot another lane of it still reads
+                    assert not (reads & set(new))
+                    for k, val in new.items():
+                        node[k] = val
+                    new, reads = {}, set()
                 for n in range(cnt):
                     w = rec[8 * (noff + n): 8 * (noff + n) + 8]
                     assert w[0] >> 16 == nt
                     r = 0.0
                     for tt in range(nt):
                         x = w[1 + tt]
+                        reads.add(x & 0xffff)
                         r += c[x >> 16] * node[x & 0xffff]
+                    assert (w[0] & 0xffff) not in new     # one writer per slot and step
                     new[w[0] & 0xffff] = r
-                # all nodes of a segment read values from earlier levels only
-                for k, val in new.items():
-                    node[k] = val
+            assert not (reads & set(new))
+            for k, val in new.items():
+                node[k] = val
             acc += node[np.array(p["vtgt"])]
     H = np.zeros(p["hsize"])
     H[:p["nacc"]] = acc
@@ -68,8 +83,9 @@ def emulate(cls, pr, pd, bra, ket):
     return H[np.array(p["outslot"])]
 
 
+@pytest.mark.parametrize("grouped", [False, True])
 @pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(2) if sum(c) >= 2])
-def test_wide_program_matches_generated_code(cls):
+def test_wide_program_matches_generated_code(cls, grouped):
     shells = synthetic_shells()
     sb = ShellBasis.from_shell_dicts(shells)
     g = golden("synthetic")
@@ -80,7 +96,7 @@ def test_wide_program_matches_generated_code(cls):
         if ls != cls:
             continue
         pr, pd, _ = hostcheck.make_pairs(sb, [(a, b), (c, d)])
-        got = emulate(cls, pr, pd, 0, 1)
+        got = emulate(cls, pr, pd, 0, 1, grouped)
         blk, _ = hostcheck.canonical_block(sb, q, 64)
         s = [sb.comp_scale[x][:n] for x, n in zip((a, b, c, d), blk.shape)]
         blk = blk / (s[0][:, None, None, None] * s[1][None, :, None, None] *
