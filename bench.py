@@ -35,9 +35,12 @@ WORKLOAD = "synthetic ERI microbench: 2,000,000 seeded shell quartets, l uniform
            "K uniform 1-6, exponents log-uniform [0.05,1e4], centres in a 10 A cube"
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of k_wide_write<2,2,2,1,double> on the
-# 200,000-quartet case (9,922 quartets of the class): 11,945,472 + 5,819,392 bytes
-NCU_DRAM_BYTES_PER_QUARTET = {(2, 2, 2, 1): (11945472 + 5819392) / 9922}
+# dram__bytes_read.sum + dram__bytes_write.sum per quartet of the dominant kernel, from one
+# ncu capture of the 1,000,000-quartet case of this workload (its output blocks, 256 MB for
+# (dd|dp), exceed the 129 MB L2, as at full size); empty until such a capture exists, and
+# the line then reports traffic null
+NCU_DRAM_BYTES_PER_QUARTET = {}
+NCU_TRAFFIC_SOURCE = ""
 
 
 def parse():
@@ -50,6 +53,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fock", action="store_true",
+                    help="leave out the (H2O)n / 6-31G* Fock-build arms of the default line")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the built-in kernel form of every class (no autotuning)")
     ap.add_argument("--cpu-sample", type=int, default=1024)
@@ -337,8 +342,42 @@ def run_gpu(args, rank, world):
                "h2d_bytes_per_step": int(pipe.h2d_bytes(host_in)),
                "d2h_bytes_per_step": int(pipe.total * 8), "ms_per_step": e2e_ms,
                "api": "gaussium_gb300.pipeline.BlockPipeline.submit (two device slots, "
-                      "copy-in and copy-out streams overlapping the kernels)"}
-        del pipe
+                      "copy-in and copy-out streams overlapping the kernels)",
+               "planning": "the class-sorted task list of this quartet set is built once, "
+                           "before the timed steps (e2e_with_planning builds it per step)"}
+        del pipe, host_out
+        torch.cuda.empty_cache()
+        # the same batch as a caller with new quartets every step sees it: shells in,
+        # QuartetBatch planning (canonical order, class sort, primitive-pair records), the
+        # kernels and the blocks out, one step after another, nothing overlapped
+        host_blk = torch.empty(batch.total, dtype=torch.float64).pin_memory()
+        nplan = max(1, min(args.steps, 3))
+
+        def planned_step():
+            dsn = engine.DeviceShells(sb)
+            bn = engine.QuartetBatch(dsn, quartets, want32=False, max_exp=args.prim_screen)
+            on = torch.empty(bn.total, dtype=torch.float64, device="cuda")
+            bn.run(on, 64)
+            host_blk.copy_(on)
+            return bn
+        planned_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(nplan):
+            bn = planned_step()
+        torch.cuda.synchronize()
+        plan_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / nplan, world)
+        e2e["e2e_with_planning"] = {
+            "value": args.quartets * world / (plan_ms * 1e-3), "unit": UNIT,
+            "ms_per_step": plan_ms, "steps": nplan,
+            "h2d_bytes_per_step": int(sum(getattr(sb, k).nbytes for k in
+                                          ("centre", "l", "prim_off", "expo", "coef",
+                                           "comp_scale", "func_off")) + bn.tasks.numel()),
+            "d2h_bytes_per_step": int(batch.total * 8),
+            "api": "gaussium_gb300.engine.DeviceShells + QuartetBatch(quartets) + run, "
+                   "blocks copied to pinned host memory"}
+        del host_blk, bn
+        torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -347,7 +386,14 @@ def run_gpu(args, rank, world):
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{args.cpu_sample} seeded shell quartets of the same distribution "
                          f"({nf} function quartets), oracle C restatement of the reference's "
-                         f"Obara-Saika recursion (memoised nodes), {dt:.1f} s on {threads} threads"}
+                         f"Obara-Saika recursion (memoised nodes), {dt:.1f} s on {threads} threads",
+               "memoised": True}
+
+    fock = None
+    if not args.no_fock:
+        # the metric's Fock-build half: (H2O)16 / 6-31G*, plain FP64 vs screened incremental
+        # FP64 vs mixed, on the same engine
+        fock = fock_arms(args.waters, args.waters + rank, args.mixed_cut, tune=not args.no_tune)
 
     n_all = args.quartets * world
     ms64, ms32 = res[64]["ms"], res[32]["ms"]
@@ -355,11 +401,13 @@ def run_gpu(args, rank, world):
     # case of this workload (dram__bytes_read.sum + dram__bytes_write.sum), scaled by the
     # class's quartet count here
     traffic, traffic_src = None, None
+    nq_dom = sum(e - s for c, s, e in batch.segments if c == dom)
     if dom in NCU_DRAM_BYTES_PER_QUARTET:
-        nq_dom = sum(e - s for c, s, e in batch.segments if c == dom)
         traffic = NCU_DRAM_BYTES_PER_QUARTET[dom] * nq_dom
-        traffic_src = ("ncu capture of the 200,000-quartet case, scaled by quartets "
-                       f"({nq_dom} of this class)")
+        traffic_src = NCU_TRAFFIC_SOURCE + f", scaled by quartets ({nq_dom} of this class)"
+    # algorithmic bytes of the dominant launch: its output blocks (written once) and the
+    # primitive-pair records of its quartets (read at least once)
+    out_bytes = 8 * nq_dom * int(np.prod([engine.NCART[x] for x in dom]))
     line = {
         "metric": METRIC,
         "value": n_all / (ms64 * 1e-3),
@@ -388,6 +436,7 @@ def run_gpu(args, rank, world):
                      "frac": achieved / peak64, "traffic": traffic,
                      "traffic_unit": "bytes per launch (dram read + write)",
                      "traffic_source": traffic_src,
+                     "algorithmic_output_bytes": out_bytes,
                      "peak_source": "gs_fma_probe FP64 FMA rate measured in this run "
                                     "(no FP64 figure among the pool's measured peaks)"},
         "fp64": {"value": n_all / (ms64 * 1e-3), "ms_per_step": ms64,
@@ -408,56 +457,96 @@ def run_gpu(args, rank, world):
         "e2e": e2e,
         "gpu_launches": nlaunch * args.steps,
         "cpu_baseline": cpu,
+        "fock": fock,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------- Fock-build workload
-def run_water(args, rank, world):
-    """RHF on a seeded (H2O)n / 6-31G* cluster: plain FP64 integral-direct Fock builds vs
-    the mixed FP32/FP64 incremental builds; times per build, |dE|."""
+def fock_arms(n_waters, seed, mixed_cut, tune=True):
+    """RHF of a seeded (H2O)n / 6-31G* cluster three times on one engine (Schwarz 1e-12):
+      fp64                       plain FP64 integral-direct builds;
+      fp64_screened_incremental  FP64 with density screening at 1e-12 and incremental
+                                 (Delta P) builds, full build every 8;
+      mixed                      the same screening and incremental builds, quartets with
+                                 density-weighted bound below ``mixed_cut`` in FP32.
+    Per arm: mean and total Fock-build time (host density in, Fock matrix out, as the
+    SCF sees it), builds, energy, |dE| against the fp64 arm.  The mixed arm's energy is
+    its own SCF energy (the FP32 error in full); a final FP64 build at its converged
+    density is reported beside it, timed separately."""
     import torch
-    from gaussium_gb300 import build, driver, molecules
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    build.build()
-    mol = molecules.water_cluster(args.waters, seed=args.waters + rank)
-    # warm-up: a small cluster exercises every kernel once
-    driver.rhf(molecules.water_cluster(2, seed=2), max_iter=3)
+    from gaussium_gb300 import driver, molecules
     from gaussium_gb300.engine import JKEngine
+    mol = molecules.water_cluster(n_waters, seed=seed)
     eng = JKEngine(molecules.shell_basis(mol, "6-31G*"), schwarz_thr=1e-12)
     forms = {}
-    if not args.no_tune:
+    if tune:
         from gaussium_gb300 import autotune
         rng = np.random.default_rng(0)
         a = rng.standard_normal((eng.sb.nbf, eng.sb.nbf)) * 0.1
         chosen = autotune.tune_jk(eng, torch.tensor(a + a.T, device="cuda"), reps=2)
         forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
                  for (c, p), r in chosen.items()}
+    # warm-up: one build of each kind
+    driver.rhf(mol, engine=eng, threshold=1e-10, max_iter=2)
+    driver.rhf(mol, engine=eng, threshold=1e-10, max_iter=2, mixed_cut=mixed_cut,
+               screen_thr=1e-12, incremental=True)
+    runs = {
+        "fp64": dict(),
+        "fp64_screened_incremental": dict(screen_thr=1e-12, incremental=True),
+        "mixed": dict(mixed_cut=mixed_cut, screen_thr=1e-12, incremental=True, final_fp64=True),
+    }
+    out = {}
     with ClockSampler() as clk:
-        r64 = driver.rhf(mol, engine=eng, threshold=1e-10)
-        rmx = driver.rhf(mol, engine=eng, threshold=1e-10, mixed_cut=args.mixed_cut,
-                         screen_thr=1e-12, incremental=True, final_fp64=True)
-    t64 = float(np.sum(r64["fock_seconds"]))
-    tmx = float(np.sum(rmx["fock_seconds"]))
-    de = abs(rmx["energy"] - r64["energy"])
-    line = {
-        "metric": METRIC, "value": tmx * 1e3 / max(1, len(rmx["fock_seconds"])),
-        "unit": "ms per Fock build (mixed)", "n_gpus": world, "steps": len(rmx["fock_seconds"]),
-        "warmup": 1, "ms_per_step": tmx * 1e3 / max(1, len(rmx["fock_seconds"])),
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
-        "data": "synthetic (seeded water cluster)",
-        "config": {"workload": f"RHF (H2O){args.waters}/6-31G*, {r64['nbf']} functions, Schwarz 1e-12",
-                   "unique_shell_quartets_after_schwarz": int(r64["ntasks"]),
-                   "mixed_cut": args.mixed_cut, "incremental_reset_every": 8,
-                   "kernel_forms_autotuned": forms},
-        "fp64": {"energy": r64["energy"], "iterations": r64["iterations"],
-                 "fock_ms_mean": t64 * 1e3 / len(r64["fock_seconds"]), "fock_s_total": t64},
-        "mixed": {"energy": rmx["energy"], "iterations": rmx["iterations"],
-                  "fock_ms_mean": tmx * 1e3 / len(rmx["fock_seconds"]), "fock_s_total": tmx,
-                  "builds": len(rmx["fock_seconds"]), "abs_dE_vs_fp64": de,
-                  "speedup_total_fock_time": t64 / tmx},
+        for name, kw in runs.items():
+            r = driver.rhf(mol, engine=eng, threshold=1e-10, **kw)
+            secs = list(r["fock_seconds"])
+            fin = None
+            if kw.get("final_fp64"):
+                fin = secs.pop()            # the final FP64 build, reported on its own
+            out[name] = {"ms_per_build": float(np.mean(secs)) * 1e3,
+                         "fock_ms_total": float(np.sum(secs)) * 1e3, "builds": len(secs),
+                         "iterations": r["iterations"], "converged": bool(r["converged"]),
+                         "energy": r["scf_energy"]}
+            if fin is not None:
+                out[name]["final_fp64_build_ms"] = fin * 1e3
+                out[name]["energy_after_final_fp64_build"] = r["energy"]
+    e64 = out["fp64"]["energy"]
+    for name in out:
+        out[name]["abs_dE_vs_fp64"] = abs(out[name]["energy"] - e64)
+    if "energy_after_final_fp64_build" in out["mixed"]:
+        out["mixed"]["abs_dE_after_final_fp64_build"] = abs(
+            out["mixed"]["energy_after_final_fp64_build"] - e64)
+    t = {k: v["ms_per_build"] for k, v in out.items()}
+    return {
+        "workload": f"RHF (H2O){n_waters}/6-31G* (seed {seed}), {eng.sb.nbf} functions, "
+                    f"Schwarz 1e-12, {eng.ntasks} unique shell quartets",
+        "mixed_cut": mixed_cut, "screen_thr": 1e-12, "incremental_reset_every": 8,
+        "arms": out,
+        "speedup_mixed_vs_fp64": t["fp64"] / t["mixed"],
+        "speedup_screened_incremental_vs_fp64": t["fp64"] / t["fp64_screened_incremental"],
+        "speedup_mixed_vs_screened_incremental": t["fp64_screened_incremental"] / t["mixed"],
+        "kernel_forms_autotuned": forms,
         "clocks": clk.summary(),
+    }
+
+
+def run_water(args, rank, world):
+    """RHF on a seeded (H2O)n / 6-31G* cluster: plain FP64 integral-direct Fock builds vs
+    the mixed FP32/FP64 incremental builds; times per build, |dE|."""
+    import torch
+    from gaussium_gb300 import build
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    build.build()
+    f = fock_arms(args.waters, args.waters + rank, args.mixed_cut, tune=not args.no_tune)
+    mx = f["arms"]["mixed"]
+    line = {
+        "metric": METRIC, "value": mx["ms_per_build"], "unit": "ms per Fock build (mixed)",
+        "n_gpus": world, "steps": mx["builds"], "warmup": 1, "ms_per_step": mx["ms_per_build"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded water cluster)", "config": {"workload": f["workload"]},
+        "fock": f, "clocks": f["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -960,7 +1049,12 @@ def run_reference(args, rank, world):
         "impl": "reference",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.cpu_sample // 4} seeded shell quartets per step, "
-                                   "oracle C restatement of the reference's Obara-Saika recursion"},
+                                   "oracle C restatement of the reference's Obara-Saika "
+                                   "recursion with memoised recursion nodes (bit-identical "
+                                   "results; faster than the reference's unmemoised Python "
+                                   "recursion, so the GPU ratio against it understates the "
+                                   "speed-up over the reference itself)",
+                         "memoised": True},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -53,8 +53,9 @@ class BlockPipeline:
 
     def submit(self, host_shells, host_out):
         """Queue one batch: ``host_shells`` (pinned, as from ``pinned_shells``) in, blocks
-        out into the pinned float64 tensor ``host_out`` (``total`` elements).  Returns the
-        event that completes when ``host_out`` holds the blocks."""
+        out into the pinned float64 tensor ``host_out`` (``total`` elements).  Returns a
+        new event, recorded for this batch only, that completes when ``host_out`` holds
+        the blocks."""
         slot = self.slots[self.n % 2]
         compute = torch.cuda.current_stream()
         if slot["used"]:
@@ -71,12 +72,14 @@ class BlockPipeline:
         slot["batch"].run(slot["out"], self.precision, stream=compute)
         slot["computed"].record(compute)
         self.d2h_stream.wait_event(slot["computed"])
+        done = torch.cuda.Event()
         with torch.cuda.stream(self.d2h_stream):
             host_out.copy_(slot["out"][:self.total], non_blocking=True)
             slot["d2h"].record(self.d2h_stream)
+            done.record(self.d2h_stream)
         slot["used"] = True
         self.n += 1
-        return slot["d2h"]
+        return done
 
     def synchronize(self):
         for s in self.slots:

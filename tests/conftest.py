@@ -19,8 +19,8 @@ def golden(name):
     return np.load(os.path.join(GOLDEN, name + ".npz"))
 
 
-def synthetic_shells():
-    g = golden("synthetic")
+def synthetic_shells(name="synthetic"):
+    g = golden(name)
     return [dict(l=int(g["shell_l"][i]), centre=g["shell_centre"][i],
                  expo=g["shell_expo"][i, :g["shell_k"][i]],
                  coef=g["shell_coef"][i, :g["shell_k"][i]]) for i in range(len(g["shell_l"]))]

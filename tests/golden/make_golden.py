@@ -21,6 +21,15 @@ Each file records what produced it:
                      shell quartets, sampled function quartets through ObaraSaika, and a
                      subset through HeadGordonPople and Cook; also the reference's contracted
                      and primitive normalisations of every shell.
+* ``synthetic_k6.npz`` the microbench's own contraction range: for every canonical
+                     (la lb|lc ld) class two shell quartets, one with K drawn uniform 1-6 per
+                     shell in the 10 A cube, one with K = 6 on all four shells in a 1.5 A
+                     cube; sampled function quartets through ObaraSaika.
+* ``gradient_fd.npz`` reference RHF total energies of water (``examples/molfiles/H2O.mol``
+                     with its first hydrogen moved by (0.05, -0.03, 0.02) bohr) in 6-31G and
+                     6-31G*, at that geometry and with every coordinate moved by +-1e-4
+                     bohr: the reference energy differentiated numerically.  6-31G is the
+                     6-31G* file without its D shells.
 * ``energies.npz``   reference total energies of test_start.py systems run without
                      point-group symmetry (HeH+ STO-3G RHF, O2 UHF/GUHF STO-3G).
 * ``heh_sto3g.npz``, ``o2_sto3g.npz``  their basis functions and S, T, V matrices.
@@ -347,6 +356,110 @@ def make_synthetic(procs, quick):
              cook=val["cook"], os_seconds=sec)
 
 
+def make_synthetic_k6(procs):
+    """Sampled function quartets of shells with the microbench's contraction degrees
+    (K = 1-6, and K = 6 on every shell), one pair of shell quartets per canonical class."""
+    rng = np.random.default_rng(20261204)
+    shells, quartets = [], []
+    pairs = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
+    classes = [p + q for i, p in enumerate(pairs) for q in pairs[:i + 1]]
+    for cls in classes:
+        for rep in range(2):
+            if rep == 0:
+                sh = [synthetic_shell(rng, l, 6, 10.0) for l in cls]
+            else:
+                sh = []
+                for l in cls:
+                    s = synthetic_shell(rng, l, 1, 1.5)
+                    s["expo"] = np.exp(rng.uniform(np.log(0.05), np.log(1e4), size=6))
+                    s["coef"] = rng.standard_normal(6)
+                    sh.append(s)
+            base = len(shells)
+            shells.extend(sh)
+            quartets.append([base, base + 1, base + 2, base + 3])
+    samples = []
+    for qi, q in enumerate(quartets):
+        ls = [shells[s]["l"] for s in q]
+        ncomp = [len(COMPONENTS[l]) for l in ls]
+        nsamp = min(int(np.prod(ncomp)), 4 if sum(ls) <= 5 else 2)
+        all_comp = list(itertools.product(*[range(n) for n in ncomp]))
+        for p in rng.choice(len(all_comp), size=nsamp, replace=False):
+            samples.append((qi, all_comp[p]))
+    tasks = [(si, [shells[s] for s in quartets[qi]], comp, "os")
+             for si, (qi, comp) in enumerate(samples)]
+    # longest first, so the pool does not end on one (dd|dd) K=6 quartet
+    tasks.sort(key=lambda t: -sum(s["l"] for s in t[1]) * np.prod([len(s["expo"]) for s in t[1]]))
+    with mp.get_context("fork").Pool(procs) as pool:
+        res = pool.map(_synthetic_worker, tasks, chunksize=1)
+    val = np.full(len(samples), np.nan)
+    sec = np.zeros(len(samples))
+    for si, which, v, dt in res:
+        val[si], sec[si] = v, dt
+    nsh = len(shells)
+    sh_l = np.array([s["l"] for s in shells]); sh_k = np.array([len(s["expo"]) for s in shells])
+    sh_c = np.array([s["centre"] for s in shells])
+    sh_e = np.zeros((nsh, 6)); sh_cf = np.zeros((nsh, 6))
+    for i, s in enumerate(shells):
+        sh_e[i, :len(s["expo"])] = s["expo"]; sh_cf[i, :len(s["coef"])] = s["coef"]
+    np.savez_compressed(os.path.join(HERE, "synthetic_k6.npz"), shell_l=sh_l, shell_k=sh_k,
+                        shell_centre=sh_c, shell_expo=sh_e, shell_coef=sh_cf,
+                        quartets=np.array(quartets),
+                        sample_quartet=np.array([s[0] for s in samples]),
+                        sample_comp=np.array([s[1] for s in samples]), os=val, os_seconds=sec)
+
+
+FD_STEP = 1e-4
+FD_SHIFT = (0.05, -0.03, 0.02)
+
+
+def _without_d_shells(path):
+    out, skip = [], False
+    for line in open(path).read().splitlines():
+        w = line.split()
+        if w and w[0] in ("S", "L", "P", "D", "F") and len(w) == 2:
+            skip = w[0] == "D"
+        elif not line.strip() or line.startswith("#"):
+            skip = False
+        if not skip:
+            out.append(line)
+    return write_tmp("631g.gbs", "\n".join(out) + "\n")
+
+
+def _mol_text(symbols, z, coords):
+    lines = ["0 1"]
+    for sym, zz, c in zip(symbols, z, coords):
+        mass = {1: 1, 8: 16}[zz]
+        lines.append(f"{sym} {zz} {mass} {float(c[0])!r} {float(c[1])!r} {float(c[2])!r}")
+    return "\n".join(lines) + "\n"
+
+
+def make_gradient_fd(procs):
+    root = ref_harness.reference_root()
+    basis_files = {"6-31G*": f"{root}/examples/basissets/6-31GP.gbs"}
+    basis_files["6-31G"] = _without_d_shells(basis_files["6-31G*"])
+    symbols, z = ["OXYGEN", "HYDROGEN", "HYDROGEN"], [8, 1, 1]
+    x0 = np.array([[0.0, -0.143225816552, 0.0], [1.638036840407, 1.136548822547, 0.0],
+                   [-1.638036840407, 1.136548822547, 0.0]])
+    x0[1] += np.array(FD_SHIFT)
+    out = dict(coords=x0, charges=np.array(z, dtype=np.float64), step=FD_STEP)
+    for name, gbs in basis_files.items():
+        tag = name.replace("*", "s").replace("-", "")
+        e = np.zeros((3, 3, 2))
+        for a in range(3):
+            for k in range(3):
+                for si, sign in enumerate((1.0, -1.0)):
+                    x = x0.copy()
+                    x[a, k] += sign * FD_STEP
+                    mol = write_tmp("fd.mol", _mol_text(symbols, z, x))
+                    nuclei, electrons, _, basis = load_molecule(mol, gbs)
+                    e[a, k, si] = run_rhf(nuclei, electrons, basis, procs)[0]
+        nuclei, electrons, _, basis = load_molecule(write_tmp("fd.mol", _mol_text(symbols, z, x0)), gbs)
+        out[f"energy_{tag}"] = run_rhf(nuclei, electrons, basis, procs)[0]
+        out[f"displaced_{tag}"] = e
+        out[f"fd_gradient_{tag}"] = (e[..., 0] - e[..., 1]) / (2 * FD_STEP)
+    np.savez_compressed(os.path.join(HERE, "gradient_fd.npz"), **out)
+
+
 # ---------------------------------------------------------------- energies of test_start systems
 def make_energies(procs):
     g = ref_harness.load()
@@ -383,6 +496,8 @@ def main():
              "h2o_sto3g": lambda: make_h2o_sto3g(args.procs),
              "h2o_631gs": lambda: make_h2o_631gs(args.procs),
              "synthetic": lambda: make_synthetic(args.procs, args.quick),
+             "synthetic_k6": lambda: make_synthetic_k6(args.procs),
+             "gradient_fd": lambda: make_gradient_fd(args.procs),
              "energies": lambda: make_energies(args.procs)}
     for name, fn in steps.items():
         if args.only and name not in args.only.split(","):

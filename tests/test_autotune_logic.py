@@ -28,14 +28,22 @@ def test_tune_picks_fastest_form(monkeypatch):
 
 
 def test_vrr_group_choice():
+    """Classes whose node program fills a warp's waves poorly get a grouped form, whose
+    waves of 32/VG nodes times VG primitive quartets fill the lanes; the grouped buffers
+    stay within the budget; (dd|dd)'s ungrouped waves are already 94 % full."""
     import os
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
                                     "gaussium_gb300", "csrc"))
     import gen_eri
-    # segments [noff, unused, cnt, nt, level, sync]: narrow levels want a group
-    narrow = [[0, 0, 4, 2, 1, 1], [1, 0, 6, 3, 2, 1]]
-    wide = [[0, 0, 64, 2, 1, 1], [2, 0, 96, 3, 2, 1]]
-    assert gen_eri.vrr_group(narrow, 20) > 1
-    assert gen_eri.vrr_group(wide, 20) == 1
-    assert gen_eri.vrr_group(narrow, 2000) == 1           # buffer budget
+    vg, prog = gen_eri.vrr_group((2, 1, 0, 0))
+    base = gen_eri.wide_program((2, 1, 0, 0))
+    assert vg > 1
+    assert (gen_eri.wave_efficiency(prog["vrec"], prog["vseg"], vg) >
+            gen_eri.wave_efficiency(base["vrec"], base["vseg"]) + 0.3)
+    assert max(s[2] for s in prog["vseg"]) <= 32 // vg
+    for cls in ((2, 2, 2, 1), (2, 2, 2, 2)):
+        vg, prog = gen_eri.vrr_group(cls)
+        assert vg * prog["nvslot"] <= gen_eri.VGROUP_SLOT_BUDGET
+    base = gen_eri.wide_program((2, 2, 2, 2))
+    assert gen_eri.wave_efficiency(base["vrec"], base["vseg"]) > 0.94

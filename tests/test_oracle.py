@@ -89,6 +89,21 @@ def test_synthetic_quartets_and_normalisation():
     assert np.max(np.abs(g["cook"][m] - g["os"][m])) < 5e-9
 
 
+def test_synthetic_k6_quartets():
+    """The microbench's contraction range (K = 1-6, and K = 6 on all four shells) for every
+    canonical class: the oracle against the reference's ObaraSaika values."""
+    g = golden("synthetic_k6")
+    assert g["shell_k"].max() == 6 and g["shell_k"].min() == 1
+    shells = synthetic_shells("synthetic_k6")
+    t = oracle.FunctionTable.from_shells(shells)
+    ncomp = [len(oracle.COMPONENTS[s["l"]]) for s in shells]
+    off = np.concatenate([[0], np.cumsum(ncomp)])
+    q = g["quartets"][g["sample_quartet"]]
+    fq = np.array([[off[q[i, k]] + g["sample_comp"][i, k] for k in range(4)] for i in range(len(q))])
+    got = oracle.eri_functions(t, fq, boys_mode=0)
+    assert np.max(np.abs(got - g["os"])) < 1e-15
+
+
 def test_ao_to_mo_restatements_match_reference():
     """The oracle's restatements of matrixelements/transformations.py against the
     reference's own outputs (tests/golden/make_mo_golden.py)."""

@@ -27,8 +27,9 @@ def test_pipeline_batches_match_direct_evaluation(gpu_lib):
         variants.append((BlockPipeline.pinned_shells(v), ref.cpu().numpy()))
     pipe = BlockPipeline(sb, q, precision=64)
     outs = [torch.full((pipe.total,), np.nan, dtype=torch.float64).pin_memory() for _ in variants]
-    for (host_in, _), o in zip(variants, outs):
-        pipe.submit(host_in, o)
-    pipe.synchronize()
-    for (_, ref), o in zip(variants, outs):
+    events = [pipe.submit(host_in, o) for (host_in, _), o in zip(variants, outs)]
+    assert len({id(e) for e in events}) == len(events)     # one event per batch
+    for (_, ref), o, e in zip(variants, outs, events):
+        e.synchronize()
         assert np.array_equal(o.numpy(), ref)
+    pipe.synchronize()
