@@ -50,6 +50,7 @@ _SIGS = {
     "gs_basis_on_grid": (I, [P, P, P, P, P, P, P, I, I, ctypes.c_longlong, P, P, P]),
     "gs_lda_xc": (I, [ctypes.c_longlong, P, P, D, I, D, D, D, D, P, P, P]),
     "gs_symmetry_zero": (I, [I, I, P, P, P, P, P, P]),
+    "gs_dense_expand": (I, [ctypes.c_longlong, P, P, P, P, P, I, P, P]),
 }
 
 

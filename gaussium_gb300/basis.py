@@ -188,13 +188,30 @@ class ShellBasis:
         cs[:, :] = np.asarray(comp_scale, dtype=np.float64).reshape(len(self.l), -1)[:, :6] \
             if np.asarray(comp_scale).size == 6 * len(self.l) else 1.0
         self.comp_scale = np.ascontiguousarray(cs)
-        if int(self.l.max(initial=0)) > LMAX:
-            raise ValueError(f"angular momentum above {LMAX} is not supported")
+        self._validate()
         nfun = np.array([1, 3, 6], dtype=np.int32)[self.l]
         self.nfunc = nfun
         self.func_off = np.concatenate([[0], np.cumsum(nfun)[:-1]]).astype(np.int32)
         self.nbf = int(nfun.sum())
         self.nprim = np.diff(self.prim_off).astype(np.int32)
+
+    def _validate(self):
+        """Reject shell data a kernel would turn into garbage or out-of-range reads, before
+        anything reaches the device."""
+        ns = len(self.l)
+        if int(self.l.max(initial=0)) > LMAX or int(self.l.min(initial=0)) < 0:
+            raise ValueError(f"angular momentum outside 0..{LMAX}")
+        if self.centre.shape != (ns, 3) or not np.all(np.isfinite(self.centre)):
+            raise ValueError("shell centres must be finite, one (x, y, z) per shell")
+        po = self.prim_off
+        if len(po) != ns + 1 or (ns and po[0] != 0) or np.any(np.diff(po) < 1) or \
+                po[-1] != len(self.expo) or len(self.coef) != len(self.expo):
+            raise ValueError("prim_off must start at 0, increase by at least one primitive per "
+                             "shell and end at the number of exponents (= coefficients)")
+        if not np.all(np.isfinite(self.expo)) or np.any(self.expo <= 0):
+            raise ValueError("primitive exponents must be finite and positive")
+        if not np.all(np.isfinite(self.coef)) or not np.all(np.isfinite(self.comp_scale)):
+            raise ValueError("contraction coefficients and component scales must be finite")
 
     @property
     def nshell(self):

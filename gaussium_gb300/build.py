@@ -148,6 +148,7 @@ def build(jobs=None, verbose=False):
     todo.append((os.path.join(CSRC, "transform.cu"), [], os.path.join(BUILD, "transform.o")))
     todo.append((os.path.join(CSRC, "xc.cu"), [], os.path.join(BUILD, "xc.o")))
     todo.append((os.path.join(CSRC, "symmetry.cu"), [], os.path.join(BUILD, "symmetry.o")))
+    todo.append((os.path.join(CSRC, "dense.cu"), [], os.path.join(BUILD, "dense.o")))
     todo.append((os.path.join(CSRC, "eri_grad.cu"),
                  [os.path.join(CSRC, "eri_grad.cuh")] +
                  [os.path.join(GEN, f"eri_grad_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110", "1111")] +

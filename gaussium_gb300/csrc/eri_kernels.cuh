@@ -179,8 +179,8 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_jk(const JKArgs 
         eri_jk_task<LA, LB, LC, LD, T>(a, t);
 }
 
-// Blocks launched for a task count that lives on the device (enough to fill the GPU).
-constexpr int kDeviceCountBlocks = 152 * 16;
+// Blocks launched for a task count that lives on the device: 16 per SM fill the GPU.
+constexpr int kDeviceCountBlocksPerSM = 16;
 
 // Schwarz bound of shell pairs: q[p] = sqrt(max_ijkl |(ab|ab)|) over the scaled block.
 template <int LA, int LB, typename T>
@@ -214,7 +214,8 @@ int launch_class(int kind, const void* args, cudaStream_t st) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
         int grid = (a.ntask + kBlock - 1) / kBlock;
-        if (a.ntask_dev && grid > kDeviceCountBlocks) grid = kDeviceCountBlocks;
+        if (a.ntask_dev && grid > kDeviceCountBlocksPerSM * sm_count())
+            grid = kDeviceCountBlocksPerSM * sm_count();
         k_eri_jk<LA, LB, LC, LD, T><<<grid, kBlock, 0, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
         if constexpr (LA == LC && LB == LD && PREC == 64) {

@@ -392,8 +392,8 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
     }
 }
 
-// Blocks launched for a task count that lives on the device (enough to fill the GPU).
-constexpr int kWideDeviceCountBlocks = 152 * 16;
+// Blocks launched for a task count that lives on the device: 16 per SM fill the GPU.
+constexpr int kWideDeviceCountBlocksPerSM = 16;
 
 template <int LA, int LB, typename T>
 __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzArgs a) {
@@ -449,7 +449,8 @@ int launch_wide(int kind, const void* args, cudaStream_t st) {
         auto k = k_wide_jk<LA, LB, LC, LD, T, VG>;
         if (set_smem<k_wide_jk<LA, LB, LC, LD, T, VG>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
         int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
-        if (a.ntask_dev && grid > kWideDeviceCountBlocks) grid = kWideDeviceCountBlocks;
+        if (a.ntask_dev && grid > kWideDeviceCountBlocksPerSM * sm_count())
+            grid = kWideDeviceCountBlocksPerSM * sm_count();
         k<<<grid, TPB, Lay::BYTES_JK, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
         if constexpr (LA == LC && LB == LD && PREC == 64 && VG == 1) {

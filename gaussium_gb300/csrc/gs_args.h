@@ -15,6 +15,21 @@
 #define GS_ERR_LIMIT 6
 
 namespace gs {
+// Streaming multiprocessors of the current device (queried once per device; grid caps for
+// launches whose task count lives on the device are multiples of it).
+inline int sm_count() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            return 1;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 struct PairRec;
 struct WriteTask;
 

@@ -58,7 +58,8 @@ int gs_symmetry_zero(int n, int nops, const int* table, const unsigned char* fli
     if (!centre_id || !parity || !tensor || (nops > 0 && (!table || !flip))) return GS_ERR_ARG;
     const long long total = (long long)n * n * n * n;
     long long blocks = (total + kThreads - 1) / kThreads;
-    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    const long long cap = 32LL * gs::sm_count();   // grid-stride beyond 32 blocks per SM
+    if (blocks > cap) blocks = cap;
     k_symmetry_zero<<<(unsigned)blocks, kThreads, 0, (cudaStream_t)stream>>>(
         n, nops, table, flip, centre_id, parity, tensor);
     return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA;

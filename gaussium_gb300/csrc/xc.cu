@@ -105,7 +105,7 @@ k_lda(long long npts, const double* __restrict__ rho, const double* __restrict__
 
 unsigned grid_for(long long work) {
     long long b = (work + kThreads - 1) / kThreads;
-    const long long cap = 152LL * 16;
+    const long long cap = 16LL * gs::sm_count();   // grid-stride beyond 16 blocks per SM
     return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 

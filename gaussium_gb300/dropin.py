@@ -79,33 +79,13 @@ def dense_eri(sb: ShellBasis, device="cuda", precision=64):
     vals = torch.zeros(max(1, batch.total), dtype=torch.float64, device=ds.device)
     batch.run(vals, precision)
     dev = ds.device
-    ncart = torch.as_tensor(engine.NCART[sb.l]).to(dev)
-    fo = torch.as_tensor(sb.func_off.astype(np.int64)).to(dev)
-    qt = torch.as_tensor(q).to(dev)
-    sizes = torch.as_tensor(np.diff(batch.offsets)).to(dev)
-    owner = torch.repeat_interleave(torch.arange(len(q), device=dev), sizes)
-    local = torch.arange(batch.total, device=dev) - torch.as_tensor(batch.offsets[:-1]).to(dev)[owner]
-    nq = ncart[qt[owner]]                     # (total, 4) sizes
-    idx = torch.empty((batch.total, 4), dtype=torch.int64, device=dev)
-    rem = local
-    for k in (3, 2, 1, 0):
-        idx[:, k] = rem % nq[:, k] + fo[qt[owner, k]]
-        rem = rem // nq[:, k]
-    v = vals[:batch.total]
-    a, b, c, d = idx.unbind(1)
-    # one writer per 8-fold orbit: a unique shell quartet holds an orbit more than once only
-    # where shells repeat (A = B, C = D, or bra pair = ket pair); keep one element there
-    sq = qt[owner]
-    same_ab = sq[:, 0] == sq[:, 1]
-    same_cd = sq[:, 2] == sq[:, 3]
-    same_pair = (sq[:, 0] == sq[:, 2]) & (sq[:, 1] == sq[:, 3])
-    keep = (~same_ab | (a >= b)) & (~same_cd | (c >= d)) & \
-        (~same_pair | (a > c) | ((a == c) & (b >= d)))
-    a, b, c, d, v = a[keep], b[keep], c[keep], d[keep], v[keep]
-    t = torch.zeros((n, n, n, n), dtype=torch.float64, device=dev)
-    for (w, x, y, z) in ((a, b, c, d), (b, a, c, d), (a, b, d, c), (b, a, d, c),
-                         (c, d, a, b), (d, c, a, b), (c, d, b, a), (d, c, b, a)):
-        t[w, x, y, z] = v
+    # the 8-fold expansion on the device (gs_dense_expand): one warp per unique block
+    qt = torch.as_tensor(np.ascontiguousarray(q, dtype=np.int32)).to(dev)
+    offs = torch.as_tensor(np.ascontiguousarray(batch.offsets[:-1], dtype=np.int64)).to(dev)
+    t = torch.empty((n, n, n, n), dtype=torch.float64, device=dev)
+    _lib.check(_lib.lib().gs_dense_expand(len(q), _lib.ptr(qt), _lib.ptr(offs), _lib.ptr(vals),
+                                          _lib.ptr(ds.l), _lib.ptr(ds.func_off), n, _lib.ptr(t),
+                                          _lib.stream()), "gs_dense_expand")
     return t
 
 

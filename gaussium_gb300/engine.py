@@ -73,12 +73,20 @@ class DeviceShells:
         self.nbf = sb.nbf
 
 
+def check_shell_indices(idx, nshell, what):
+    """Shell indices handed to the kernels must lie in [0, nshell): a kernel trusts them."""
+    idx = np.asarray(idx)
+    if idx.size and (int(idx.min()) < 0 or int(idx.max()) >= nshell):
+        raise ValueError(f"{what} hold a shell index outside [0, {nshell})")
+
+
 class PairSet:
     """Shell pairs (la >= lb inside each pair) with their primitive-pair records."""
 
     def __init__(self, ds: DeviceShells, pair_shells, want32=True, stream=None, max_exp=0.0):
         ps = np.ascontiguousarray(pair_shells, dtype=np.int32).reshape(-1, 2)
         sb = ds.host
+        check_shell_indices(ps, sb.nshell, "shell pairs")
         if len(ps) and np.any(sb.l[ps[:, 0]] < sb.l[ps[:, 1]]):
             raise ValueError("pair shells must have l[first] >= l[second]")
         npp = sb.nprim[ps[:, 0]].astype(np.int64) * sb.nprim[ps[:, 1]]
@@ -151,6 +159,7 @@ class QuartetBatch:
     def __init__(self, ds: DeviceShells, quartets, want32=True, max_exp=0.0):
         q = np.ascontiguousarray(quartets, dtype=np.int64).reshape(-1, 4)
         sb = ds.host
+        check_shell_indices(q, sb.nshell, "shell quartets")
         n = len(q)
         l4 = sb.l[q]
         pos, code, pcb, pck = canonicalize(l4)

@@ -234,3 +234,10 @@ def install(gaussium, **options):
         originals[(mod.__name__, name)] = getattr(mod, name)
         setattr(mod, name, new)
     return originals
+
+
+def uninstall(originals):
+    """Undo ``install``: put back the attributes it replaced (its return value)."""
+    import sys
+    for (modname, name), value in originals.items():
+        setattr(sys.modules[modname], name, value)

@@ -17,8 +17,15 @@ import numpy as np
 
 
 class LinearAlgebra:
+    # smallest overlap eigenvalue accepted: below it the basis is linearly dependent and
+    # the symmetric orthogonalisation S^-1/2 would amplify rounding without bound
+    MIN_OVERLAP_EIGENVALUE = 1e-10
+
     def __init__(self, orbital_overlap):
         s, u = np.linalg.eigh(orbital_overlap)
+        if not np.all(np.isfinite(s)) or s.min() <= self.MIN_OVERLAP_EIGENVALUE:
+            raise ValueError(f"overlap matrix is singular or not positive definite (smallest "
+                             f"eigenvalue {s.min():.3e}): the basis is linearly dependent")
         order = np.argsort(s)
         s, u = s[order], u[:, order]
         self.transformation_matrix = u @ np.diag(s ** -0.5)

@@ -307,6 +307,15 @@ int gs_lda_xc(long long npts, const double* rho, const double* weights, double s
 int gs_symmetry_zero(int n, int nops, const int* table, const unsigned char* flip,
                      const int* centre_id, const int* parity, double* tensor, void* stream);
 
+/* Dense N^4 ERI tensor from unique shell-quartet blocks: the 8-fold expansion of
+ * TwoElectronRepulsion.create_repulsion_matrix (matrixelements/electron_repulsion_matrix.py:
+ * 43-45).  quartets[4*q..4*q+3] = shells (A, B, C, D) of block q; its n_A n_B n_C n_D values
+ * (row-major) start at vals[offsets[q]]; l and func_off per shell; out is n^4 doubles
+ * (C order), every element written at least once when the quartets cover all unique ones. */
+int gs_dense_expand(long long nq, const int* quartets, const long long* offsets,
+                    const double* vals, const int* l, const int* func_off, int n, double* out,
+                    void* stream);
+
 /* FMA throughput probe (FP64 or FP32) used to measure the roofline peaks; sink must hold
  * blocks*threads elements of the chosen type.  No reference counterpart. */
 int gs_fma_probe(int precision, int blocks, int threads, int iters, void* sink, void* stream);

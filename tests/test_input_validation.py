@@ -1,0 +1,79 @@
+"""Host-side failure injection: malformed shell data, out-of-range shell indices and a
+singular overlap are rejected on the host, with ValueError, before anything reaches a
+kernel (the kernels trust their inputs).  No GPU is needed: every check runs before the
+first device allocation.  The reference's own failure handling on this path is Python
+exceptions (e.g. the DIIS fallback on a singular B matrix, diismethod/diis.py:105-112)."""
+import types
+
+import numpy as np
+import pytest
+import torch
+
+from gaussium_gb300 import engine, scf
+from gaussium_gb300.basis import ShellBasis
+
+
+def _shells():
+    # an s shell (2 primitives) and a p shell (1 primitive)
+    return dict(l=[0, 1], centre=[[0, 0, 0], [0, 0, 1.4]], prim_off=[0, 2, 3],
+                expo=[3.4, 0.6, 0.8], coef=[0.4, 0.6, 1.0], comp_scale=np.ones((2, 6)))
+
+
+def test_valid_shells_accepted():
+    sb = ShellBasis(**_shells())
+    assert sb.nshell == 2 and sb.nbf == 4
+
+
+@pytest.mark.parametrize("field,value", [
+    ("expo", [3.4, np.nan, 0.8]),
+    ("expo", [3.4, -0.6, 0.8]),
+    ("expo", [3.4, 0.0, 0.8]),
+    ("coef", [0.4, np.inf, 1.0]),
+    ("centre", [[0, 0, np.nan], [0, 0, 1.4]]),
+    ("prim_off", [0, 2, 2]),          # a shell without primitives
+    ("prim_off", [0, 3, 2]),          # not monotone
+    ("prim_off", [1, 2, 3]),          # does not start at 0
+    ("prim_off", [0, 2, 4]),          # past the last exponent
+    ("l", [0, 3]),                    # above the built classes
+    ("l", [-1, 1]),
+])
+def test_malformed_shells_rejected(field, value):
+    kw = _shells()
+    kw[field] = value
+    with pytest.raises(ValueError):
+        ShellBasis(**kw)
+
+
+def _host_only(sb):
+    # stands in for DeviceShells: the checks run before any device buffer is touched
+    return types.SimpleNamespace(host=sb, device=torch.device("cpu"))
+
+
+@pytest.mark.parametrize("q", [[[0, 1, 0, 2]], [[0, 1, -1, 0]], [[5, 0, 0, 0]]])
+def test_out_of_range_shell_indices_rejected(q):
+    sb = ShellBasis(**_shells())
+    with pytest.raises(ValueError):
+        engine.QuartetBatch(_host_only(sb), np.array(q))
+    with pytest.raises(ValueError):
+        engine.PairSet(_host_only(sb), np.array(q)[:, :2])
+
+
+def test_singular_overlap_rejected():
+    s = np.array([[1.0, 1.0], [1.0, 1.0]])           # two identical functions
+    with pytest.raises(ValueError):
+        scf.LinearAlgebra(s)
+    with pytest.raises(ValueError):
+        scf.LinearAlgebra(np.array([[1.0, np.nan], [np.nan, 1.0]]))
+
+
+def test_diis_falls_back_on_singular_b_matrix():
+    """The reference's only recovery on this path: a singular DIIS B matrix drops the
+    oldest vector and retries (diismethod/diis.py:105-112)."""
+    la = scf.LinearAlgebra(np.eye(2))
+    d = scf.DIIS(np.eye(2), la)
+    e = np.array([[0.0, 1e-3], [-1e-3, 0.0]])
+    d.error_array = [e, e, e]                          # identical: B is singular
+    d.fock_array = [np.eye(2), 2 * np.eye(2), 3 * np.eye(2)]
+    c = d._coefficients()
+    assert np.isfinite(c).all()
+    assert len(d.fock_array) < 3
