@@ -33,6 +33,7 @@ THREAD64_MAX = int(os.environ.get("GS_THREAD64_MAX", "4"))
 THREAD32_MAX = 7
 WIDE32_FROM = 5
 WIDE_PROG_MIN = 2          # classes that get generated warp programs
+GRAD_THREAD_LMAX = 3       # gradient classes with a thread-per-quartet form (gen_grad.py)
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -68,7 +69,7 @@ def classes():
 def generate():
     os.makedirs(GEN, exist_ok=True)
     _run([sys.executable, os.path.join(CSRC, "gen_eri.py"), GEN, str(LMAX)])
-    _run([sys.executable, os.path.join(CSRC, "gen_grad.py"), GEN, "1"])
+    _run([sys.executable, os.path.join(CSRC, "gen_grad.py"), GEN, str(LMAX)])
     table = os.path.join(GEN, "boys_table.h")
     gen_src = os.path.join(CSRC, "boys_table_gen.c")
     exe = os.path.join(BUILD, "boys_table_gen")
@@ -120,6 +121,24 @@ def generate():
         if L >= WIDE_PROG_MIN:
             deps.append(os.path.join(GEN, f"eri_wide_{tag}.h"))
         units.append((path, deps))
+    # one translation unit per gradient class (the fused adjoint kernels, csrc/eri_grad.cuh)
+    for cls in built:
+        tag = "".join(map(str, cls))
+        thread = sum(cls) <= GRAD_THREAD_LMAX
+        inc = '#include "eri_grad_%s.h"\n' % tag + ('#include "eri_gradt_%s.h"\n' % tag if thread else "")
+        body = ('    if (thread) return gs::launch_grad_thread<%d, %d, %d, %d>(a, st);\n' % cls
+                if thread else '    (void)thread;\n')
+        code = ('#include "eri_grad.cuh"\n%s'
+                'int gs_grad_launch_%s(const gs::GradArgs& a, bool thread, cudaStream_t st) {\n%s'
+                '    return gs::launch_grad<%d, %d, %d, %d>(a, st);\n}\n' % (inc, tag, body, *cls))
+        path = os.path.join(GEN, f"eri_grad_k_{tag}.cu")
+        if not os.path.exists(path) or open(path).read() != code:
+            with open(path, "w") as f:
+                f.write(code)
+        deps = [os.path.join(CSRC, "eri_grad.cuh"), os.path.join(GEN, f"eri_grad_{tag}.h")]
+        if thread:
+            deps.append(os.path.join(GEN, f"eri_gradt_{tag}.h"))
+        units.append((path, deps))
     return units
 
 
@@ -150,9 +169,7 @@ def build(jobs=None, verbose=False):
     todo.append((os.path.join(CSRC, "symmetry.cu"), [], os.path.join(BUILD, "symmetry.o")))
     todo.append((os.path.join(CSRC, "dense.cu"), [], os.path.join(BUILD, "dense.o")))
     todo.append((os.path.join(CSRC, "eri_grad.cu"),
-                 [os.path.join(CSRC, "eri_grad.cuh")] +
-                 [os.path.join(GEN, f"eri_grad_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110", "1111")] +
-                 [os.path.join(GEN, f"eri_gradt_{t}.h") for t in ("0000", "1000", "1010", "1100", "1110")],
+                 [os.path.join(CSRC, "eri_grad.cuh"), os.path.join(GEN, "eri_grad_list.h")],
                  os.path.join(BUILD, "eri_grad.o")))
     jobs = jobs or max(1, os.cpu_count() or 1)
     changed = False

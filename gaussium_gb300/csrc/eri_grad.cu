@@ -1,24 +1,19 @@
-// C-ABI entry of the fused ERI adjoint (gradient) kernels, csrc/eri_grad.cuh.
+// C-ABI entry of the fused ERI adjoint (gradient) kernels, csrc/eri_grad.cuh.  Each
+// gradient class is compiled in its own translation unit (written by build.py), which
+// defines gs_grad_launch_<class>.
 #include <cuda_runtime.h>
 #include "eri_grad.cuh"
 #include "eri_grad_list.h"
 
-#include "eri_grad_0000.h"
-#include "eri_grad_1000.h"
-#include "eri_grad_1010.h"
-#include "eri_grad_1100.h"
-#include "eri_grad_1110.h"
-#include "eri_grad_1111.h"
-#include "eri_gradt_0000.h"
-#include "eri_gradt_1000.h"
-#include "eri_gradt_1010.h"
-#include "eri_gradt_1100.h"
-#include "eri_gradt_1110.h"
+#define GS_GDECL(A, B, C, D) \
+    int gs_grad_launch_##A##B##C##D(const gs::GradArgs&, bool, cudaStream_t);
+GS_FOR_EACH_GRAD(GS_GDECL)
+#undef GS_GDECL
 
 namespace {
 // Kernel form per gradient class: 0 = default (thread per quartet up to total angular
 // momentum 2, warp above), 1 = thread per quartet, 2 = warp per quartet.
-int g_grad_variant[2][2][2][2] = {};
+int g_grad_variant[3][3][3][3] = {};
 
 constexpr bool has_thread(int la, int lb, int lc, int ld) { return la + lb + lc + ld <= 3; }
 
@@ -56,14 +51,9 @@ extern "C" int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec,
                    func_off, shell_atom, (const int2*)tasks, ntask, nbf, density, grad, natom};
     cudaStream_t st = (cudaStream_t)stream;
     const int v = g_grad_variant[la][lb][lc][ld];
-    const bool thread = v ? v == 1 : la + lb + lc + ld <= 2;
-#define GS_GL(A, B, C, D)                                                                 \
-    if (la == A && lb == B && lc == C && ld == D) {                                       \
-        if constexpr (A + B + C + D <= 3) {                                               \
-            if (thread) return gs::launch_grad_thread<A, B, C, D>(a, st);                 \
-        }                                                                                 \
-        return gs::launch_grad<A, B, C, D>(a, st);                                        \
-    }
+    const bool thread = has_thread(la, lb, lc, ld) && (v ? v == 1 : la + lb + lc + ld <= 2);
+#define GS_GL(A, B, C, D) \
+    if (la == A && lb == B && lc == C && ld == D) return gs_grad_launch_##A##B##C##D(a, thread, st);
     GS_FOR_EACH_GRAD(GS_GL)
 #undef GS_GL
     return GS_ERR_CLASS;

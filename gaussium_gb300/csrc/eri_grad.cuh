@@ -27,16 +27,27 @@ struct GradArgs {
     int natom;
 };
 
-constexpr int kGradWarps = 2;
+constexpr int kGradWarps = 2;        // warps per block, unless the class's buffer is too large
 constexpr int kNCoefG = 36;
+// classes with more contracted accumulators than this per warp (3 per lane... 24 per lane)
+// keep them in shared memory at their HRR positions instead of in registers
+constexpr int kGradRegAcc = 32 * 24;
 
+// Per-warp shared memory of one class: the VRR buffers (coefficients, Boys values, node
+// slots) and, in the shared-accumulator form, the accumulators [0, NACC) ahead of them;
+// the HRR reuses the whole buffer afterwards.
 template <int LA, int LB, int LC, int LD> struct GradLayout {
     using W = GradProg<LA, LB, LC, LD>;
+    static constexpr bool SMEM_ACC = W::NACC > kGradRegAcc;
+    static constexpr int ACC = SMEM_ACC ? W::NACC : 0;
     static constexpr int SC = kSetupBatch * kNCoefG;
     static constexpr int SF = kSetupBatch * (W::L + 1);
-    static constexpr int VRR = SC + SF + W::NVSLOT;
+    static constexpr int VRR = ACC + SC + SF + W::NVSLOT;
     static constexpr int WARP = VRR > W::HSIZE ? VRR : W::HSIZE;
-    static constexpr size_t BYTES = (size_t)WARP * sizeof(double) * kGradWarps;
+    // two warps per block while they fit the 227 KB a block may use, else one
+    static constexpr int WARPS = (size_t)WARP * sizeof(double) * kGradWarps <= 227 * 1024 ? kGradWarps : 1;
+    static constexpr size_t BYTES = (size_t)WARP * sizeof(double) * WARPS;
+    static_assert((size_t)WARP * sizeof(double) <= 227 * 1024, "gradient class buffer exceeds shared memory");
 };
 
 __device__ __forceinline__ int g_ncart(int l) { return (l + 1) * (l + 2) / 2; }
@@ -82,11 +93,12 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
     using W = GradProg<LA, LB, LC, LD>;
     using Lay = GradLayout<LA, LB, LC, LD>;
     constexpr int L = W::L;
-    constexpr int NACCW = (W::NACC + 31) / 32;
+    constexpr bool SMEM_ACC = Lay::SMEM_ACC;
+    constexpr int NACCW = SMEM_ACC ? 1 : (W::NACC + 31) / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double* sm = reinterpret_cast<double*>(smem_raw) + (size_t)warp * Lay::WARP;
-    const int t = blockIdx.x * kGradWarps + warp;
+    const int t = blockIdx.x * Lay::WARPS + warp;
     if (t >= a.ntask) return;
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
@@ -101,9 +113,13 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
         accs[k] = e & 0xffff;
         acck[k] = q < W::NACC ? (int)(e >> 16) : -1;
     }
-    double* sC = sm;
-    double* sF = sm + Lay::SC;
-    double* node = sm + Lay::SC + Lay::SF;
+    if constexpr (SMEM_ACC) {
+        // accumulators at their HRR positions H[accpos[q]], which fill [0, NACC)
+        for (int q = lane; q < W::NACC; q += 32) sm[q] = 0.0;
+    }
+    double* sC = sm + Lay::ACC;
+    double* sF = sC + Lay::SC;
+    double* node = sF + Lay::SF;
     const int nK = K.nprim;
     const int ntot = B.nprim * nK;
     const uint4* __restrict__ vrec = W::vrec();
@@ -118,7 +134,7 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
             c[32] = 2.0 * P.pad;               // 2 alpha (first bra shell)
             c[33] = 2.0 * (P.p - P.pad);       // 2 beta
             c[34] = 2.0 * Q.pad;               // 2 gamma (first ket shell)
-            c[35] = 1.0;
+            c[35] = 5.0 * c[28];               // 5/(2(p+q)), raised (dd|..) classes
         }
         __syncwarp();
         const int nb = min(kSetupBatch, ntot - base);
@@ -151,21 +167,33 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
                 }
             }
             __syncwarp();
+            if constexpr (SMEM_ACC) {
+                for (int q = lane; q < W::NACC; q += 32) {
+                    const unsigned e = __ldg(W::acc() + q);
+                    const int kind = (int)(e >> 16);
+                    const double w = kind == 0 ? 1.0 : c[31 + kind];
+                    const int pos = __ldg(W::accpos() + q);
+                    sm[pos] = fma(w, node[e & 0xffff], sm[pos]);
+                }
+            } else {
 #pragma unroll
-            for (int k = 0; k < NACCW; ++k) {
-                if (acck[k] >= 0) {
-                    const double w = acck[k] == 0 ? 1.0 : c[31 + acck[k]];
-                    acc[k] = fma(w, node[accs[k]], acc[k]);
+                for (int k = 0; k < NACCW; ++k) {
+                    if (acck[k] >= 0) {
+                        const double w = acck[k] == 0 ? 1.0 : c[31 + acck[k]];
+                        acc[k] = fma(w, node[accs[k]], acc[k]);
+                    }
                 }
             }
             __syncwarp();
         }
     }
     double* H = sm;
+    if constexpr (!SMEM_ACC) {
 #pragma unroll
-    for (int k = 0; k < NACCW; ++k) {
-        const int q = lane + 32 * k;
-        if (q < W::NACC) H[__ldg(W::accpos() + q)] = acc[k];
+        for (int k = 0; k < NACCW; ++k) {
+            const int q = lane + 32 * k;
+            if (q < W::NACC) H[__ldg(W::accpos() + q)] = acc[k];
+        }
     }
     __syncwarp();
     const unsigned int* __restrict__ hop = W::hop();
@@ -378,7 +406,7 @@ int launch_grad(const GradArgs& a, cudaStream_t st) {
     using Lay = GradLayout<LA, LB, LC, LD>;
     auto k = k_eri_grad<LA, LB, LC, LD>;
     if (set_smem<k_eri_grad<LA, LB, LC, LD>>(Lay::BYTES)) return GS_ERR_CUDA;
-    k<<<(a.ntask + kGradWarps - 1) / kGradWarps, 32 * kGradWarps, Lay::BYTES, st>>>(a);
+    k<<<(a.ntask + Lay::WARPS - 1) / Lay::WARPS, 32 * Lay::WARPS, Lay::BYTES, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 

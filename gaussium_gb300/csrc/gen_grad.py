@@ -17,10 +17,13 @@ import sys
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 import gen_eri  # noqa: E402
-from gen_eri import COEF_ID, HrrGen, VrrGen, cart, ncart, _alloc, _release  # noqa: E402
+from gen_eri import HrrGen, VrrGen, cart, ncart, _alloc, _release  # noqa: E402
 
 WEIGHT_SLOT = {0: None, 1: 32, 2: 33, 3: 34}    # coefficient slots holding 2alpha, 2beta, 2gamma
 NCOEF_G = 36
+# the ERI programs' coefficient slots, plus 5/(2(p+q)) in slot 35: the raised bra of a
+# (dd|..) class reaches e_i = 5 in the electron-transfer term
+COEF_ID = dict(gen_eri.COEF_ID, i2pq_5=35)
 
 
 def _range(lo, hi):

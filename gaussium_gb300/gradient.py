@@ -36,8 +36,11 @@ def combined_basis(sb: ShellBasis):
     """Original shells, then a raised copy of every shell, then a lowered copy of every
     shell with l >= 1.  Returns the ShellBasis and the raised/lowered shell indices."""
     if np.any(sb.l >= 2):
-        raise NotImplementedError("gradients need f-type raised shells for d functions; "
-                                  "supported for s/p basis sets")
+        # the raised copies of d shells are f shells, which the ERI class kernels of this
+        # host cross-check do not cover; the fused adjoint kernels (eri_gradient) and the
+        # one-electron derivative kernel handle d shells themselves
+        raise NotImplementedError("the block-path cross-check covers s/p shells; use "
+                                  "eri_gradient / one_electron_gradient_kernel for d shells")
     ns = sb.nshell
     l, cen, expo, coef, scale, off = [], [], [], [], [], [0]
 
@@ -171,8 +174,6 @@ def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom, classes=None, host=
     class over the engine's Schwarz-screened unique quartets (``classes``: only those).
     Returns natom x 3 (host numpy, or the device tensor with ``host=False``)."""
     _check_atoms(shell_atom, natom)
-    if np.any(sb.l >= 2):
-        raise NotImplementedError("the fused gradient kernels cover s/p shells")
     dev = engine.dev
     grad = torch.zeros(natom * 3, dtype=torch.float64, device=dev)
     pt = torch.as_tensor(np.ascontiguousarray(P)).to(dev)
@@ -241,9 +242,19 @@ def shell_atoms(mol, sb):
     return out
 
 
-def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
-                        want_gradient=True):
-    """Converged RHF energy and analytic gradient (Eh, Eh/bohr)."""
+class RHFState:
+    """A converged RHF solution with what its gradient needs: the molecule, basis, engine
+    (pair records, Schwarz-screened quartet tasks), the density P and the energy-weighted
+    density W."""
+
+    def __init__(self, mol, sb, engine, energy, scf_result, P, W):
+        self.mol, self.sb, self.engine = mol, sb, engine
+        self.energy, self.scf = energy, scf_result
+        self.P, self.W = P, W
+
+
+def rhf_state(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14):
+    """Converged RHF energy (Eh) and the densities its analytic gradient contracts."""
     sb = shell_basis(mol, basis)
     S, T, V = one_electron(sb, mol.coords, mol.charges)
     hcore = T + V
@@ -252,33 +263,50 @@ def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
     res = scf.restricted_scf(S, hcore, mol.electrons, fb, threshold=threshold, max_iter=200)
     if not res.converged:
         raise RuntimeError("SCF did not converge")
-    if not want_gradient:
-        return res.energy + mol.nuclear_repulsion(), None, res
     nocc = mol.electrons // 2
     la = scf.LinearAlgebra(S)
     eps, C = la.diagonalize(res.fock)
     P = 2.0 * C[:, :nocc] @ C[:, :nocc].T
     W = 2.0 * (C[:, :nocc] * eps[:nocc]) @ C[:, :nocc].T
-    sa = shell_atoms(mol, sb)
-    g = one_electron_gradient_kernel(sb, mol, sa, P, W)
-    g += eri_gradient(sb, eng, sa, P, len(mol.symbols))
-    g += nuclear_repulsion_gradient(mol)
-    energy = res.energy + mol.nuclear_repulsion()
-    return energy, g, res
+    return RHFState(mol, sb, eng, res.energy + mol.nuclear_repulsion(), res, P, W)
+
+
+def gradient_from_state(st: RHFState):
+    """dE/dR (natom x 3, Eh/bohr) from a converged state: the one-electron derivative
+    kernel (P dH/dR - W dS/dR), the fused ERI adjoint kernels contracting d(ab|cd)/dR with
+    the density-weighted quartet weights Gamma(P), and the nuclear repulsion."""
+    sa = shell_atoms(st.mol, st.sb)
+    g = one_electron_gradient_kernel(st.sb, st.mol, sa, st.P, st.W)
+    g += eri_gradient(st.sb, st.engine, sa, st.P, len(st.mol.symbols))
+    g += nuclear_repulsion_gradient(st.mol)
+    return g
+
+
+def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
+                        want_gradient=True):
+    """Converged RHF energy and analytic gradient (Eh, Eh/bohr)."""
+    st = rhf_state(mol, basis, threshold, schwarz_thr)
+    if not want_gradient:
+        return st.energy, None, st.scf
+    return st.energy, gradient_from_state(st), st.scf
 
 
 class EnergyGradient(torch.autograd.Function):
-    """E(R) for nuclear coordinates R (natom x 3, bohr) with the analytic gradient as its
-    backward pass."""
+    """E(R) for nuclear coordinates R (natom x 3, bohr).  The forward pass runs the SCF
+    only and keeps the converged state (densities, engine); the backward pass launches the
+    adjoint kernels on it -- the ERI adjoint takes the density-weighted quartet weights
+    dE/d(ab|cd) = Gamma_abcd(P) and returns the nuclear-coordinate gradient -- and scales
+    it by the incoming gradient.  A forward without backward computes no gradient."""
 
     @staticmethod
     def forward(ctx, coords, symbols, basis):
         mol = Molecule(symbols, coords.detach().cpu().numpy())
-        e, g, _ = rhf_energy_gradient(mol, basis)
-        ctx.save_for_backward(torch.as_tensor(g, dtype=coords.dtype))
-        return torch.tensor(e, dtype=coords.dtype)
+        ctx.state = rhf_state(mol, basis)
+        ctx.dtype = coords.dtype
+        return torch.tensor(ctx.state.energy, dtype=coords.dtype)
 
     @staticmethod
     def backward(ctx, grad_out):
-        (g,) = ctx.saved_tensors
+        g = torch.as_tensor(gradient_from_state(ctx.state), dtype=ctx.dtype)
+        ctx.state = None
         return grad_out * g, None, None

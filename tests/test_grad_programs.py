@@ -42,7 +42,7 @@ def emulate(cls, pr, pd, alpha_bra, alpha_ket):
                 c[11 + k] = k * P[1]; c[15 + k] = -k * wq * P[1]; c[19 + k] = k * Q[1]
                 c[23 + k] = -k * wp * Q[1]; c[27 + k] = k * 0.5 / pq
             a, gmm = alpha_bra[i // K["nprim"]] if False else P[9], Q[9]
-            c[32], c[33], c[34], c[35] = 2 * P[9], 2 * (P[0] - P[9]), 2 * Q[9], 1.0
+            c[32], c[33], c[34], c[35] = 2 * P[9], 2 * (P[0] - P[9]), 2 * Q[9], 5 * 0.5 / pq
             node = np.zeros(p["nvslot"])
             node[:L + 1] = F
             rec = p["vrec"]
@@ -103,6 +103,43 @@ def test_grad_program_blocks(cls):
         assert np.max(np.abs(outs[which] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), which
 
 
+@pytest.mark.parametrize("cls", [(2, 0, 0, 0), (2, 1, 1, 0), (2, 2, 1, 0), (2, 1, 2, 1),
+                                 (2, 2, 2, 2)])
+def test_grad_program_blocks_d_shells(cls):
+    """d classes, whose raised shells are f: the six derivative blocks from the program
+    against the oracle's Obara-Saika integrals of the modified shells (any l)."""
+    rng = np.random.default_rng(sum(cls) + 41)
+    cents = rng.uniform(-1.0, 1.0, size=(4, 3))
+    shells = [_shell(rng, l, int(rng.integers(1, 3)), cents[i]) for i, l in enumerate(cls)]
+    sb = ShellBasis.from_shell_dicts(shells)
+    pr, pd, _ = hostcheck.make_pairs(sb, [(0, 1), (2, 3)])
+    pd[:, 9] = [sb.expo[sb.prim_off[0] + i // sb.nprim[1]] for i in range(sb.nprim[0] * sb.nprim[1])] + \
+        [sb.expo[sb.prim_off[2] + i // sb.nprim[3]] for i in range(sb.nprim[2] * sb.nprim[3])]
+    outs = emulate(cls, pr, pd, None, None)
+    for which, (cen, raised) in enumerate([(0, True), (1, True), (2, True), (0, False), (1, False), (2, False)]):
+        if outs[which] is None:
+            continue
+        centre, lmn, prims, first = [], [], [], []
+        for s in range(4):
+            k0, k1 = sb.prim_off[s], sb.prim_off[s + 1]
+            l = int(sb.l[s])
+            cf = sb.coef[k0:k1].copy()
+            if s == cen:
+                l = l + 1 if raised else l - 1
+                if raised:
+                    cf = cf * 2 * sb.expo[k0:k1]
+            first.append(len(centre))
+            for comp in gen_eri.cart(l):
+                centre.append(sb.centre[s]); lmn.append(comp)
+                prims.append(list(zip(cf, sb.expo[k0:k1], np.ones(k1 - k0))))
+        table = oracle.FunctionTable(np.array(centre), np.array(lmn), np.ones(len(centre)), prims)
+        n = [len(gen_eri.cart(sum(lmn[first[s]]))) for s in range(4)]
+        fq = np.stack(np.meshgrid(*[first[s] + np.arange(n[s]) for s in range(4)], indexing="ij"),
+                      -1).reshape(-1, 4)
+        ref = oracle.eri_functions(table, fq, boys_mode=1)
+        assert np.max(np.abs(outs[which] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), which
+
+
 def _body(code, fn):
     """Statements of a generated thread-code function, as Python (they are plain
     assignments over arrays with fma)."""
@@ -122,7 +159,7 @@ def _fma(a, b, c):
     return a * b + c
 
 
-@pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(1) if sum(c) <= gen_grad.THREAD_LMAX])
+@pytest.mark.parametrize("cls", [c for c in gen_eri.canonical_classes(2) if sum(c) <= gen_grad.THREAD_LMAX])
 def test_thread_gradient_code_matches_program(cls):
     rng = np.random.default_rng(sum(cls) + 29)
     cents = rng.uniform(-1.0, 1.0, size=(4, 3))

@@ -33,16 +33,26 @@ def test_water_631g_gradient_matches_finite_differences(gpu_lib):
     assert np.max(np.abs(g.sum(0))) < 1e-8          # translational invariance
 
 
-def test_autograd_function(gpu_lib):
+@pytest.mark.parametrize("basis", ["6-31G", "6-31G*"])
+def test_autograd_function(gpu_lib, monkeypatch, basis):
+    """Forward runs the SCF only; backward launches the adjoint kernels on the saved
+    density and scales the gradient by the incoming one."""
     import torch
+    from gaussium_gb300 import gradient
     from gaussium_gb300.molecules import water_cluster
-    from gaussium_gb300.gradient import EnergyGradient, rhf_energy_gradient
+    calls = []
+    real = gradient.gradient_from_state
+    monkeypatch.setattr(gradient, "gradient_from_state",
+                        lambda st: calls.append(1) or real(st))
     m = water_cluster(1, seed=4)
     c = torch.tensor(m.coords, requires_grad=True)
-    e = EnergyGradient.apply(c, m.symbols, "6-31G")
-    e.backward()
-    _, g, _ = rhf_energy_gradient(m, "6-31G")
-    assert np.allclose(c.grad.numpy(), g, atol=1e-12)
+    e = gradient.EnergyGradient.apply(c, m.symbols, basis)
+    assert not calls                                   # no gradient work in forward
+    (3.0 * e).backward()
+    assert len(calls) == 1
+    e_ref, g, _ = gradient.rhf_energy_gradient(m, basis)
+    assert abs(float(e) - e_ref) < 1e-10
+    assert np.allclose(c.grad.numpy(), 3.0 * g, atol=1e-12)
 
 
 @pytest.mark.parametrize("form", [0, 1, 2])
