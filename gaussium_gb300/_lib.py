@@ -29,6 +29,9 @@ _SIGS = {
                                      ctypes.c_longlong, I, P, P, P, I, P, P, D, D, P,
                                      ctypes.c_longlong, P]),
     "gs_fock_jk_mixed_workspace": (ctypes.c_longlong, [I]),
+    "gs_fock_jk_persistent_workspace": (ctypes.c_longlong, [I]),
+    "gs_fock_jk_batched_persistent": (I, [P, P, P, P, P, P, P, P, P, P, P, P, ctypes.c_longlong,
+                                          P, I, P, P, P, I, P, P, D, D, P, ctypes.c_longlong, P]),
     "gs_fock_jk_mixed": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, P,
                              ctypes.c_longlong, P]),
     "gs_fock_jk_mixed_noalloc": (I, [I, I, I, I, P, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D,

@@ -126,6 +126,49 @@ class BatchedRHF:
         Pb.index_copy_(0, self.pos_padded, v.index_select(0, self.pos_packed))
         return Pb.view(len(self.sbs), self.nmax, self.nmax)
 
+    def _class_starts(self):
+        """Start of every canonical class's segment in the task array (22 entries, the
+        last = number of tasks), for the persistent launch."""
+        import sys
+        import os
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc"))
+        try:
+            import gen_eri
+        finally:
+            sys.path.pop(0)
+        seg = {cls: (s, e) for cls, s, e in self.segments}
+        out, pos = [], 0
+        for cls in gen_eri.canonical_classes(2):
+            if cls in seg:
+                assert seg[cls][0] == pos, "task segments must follow the canonical class order"
+                out.append(pos)
+                pos = seg[cls][1]
+            else:
+                out.append(pos)
+        out.append(pos)
+        assert pos == self.ntasks
+        return np.array(out, dtype=np.int32)
+
+    def _jk_persistent(self, P, J, K, dmax, mixed_cut, screen_thr):
+        """All classes of all molecules in one persistent launch per precision
+        (gs_fock_jk_batched_persistent), after one partition pass over every task."""
+        L = _lib.lib()
+        if getattr(self, "_starts", None) is None:
+            self._starts = self._class_starts()
+        need = L.gs_fock_jk_persistent_workspace(self.ntasks)
+        if getattr(self, "_pws", None) is None or self._pws.numel() < need:
+            self._pws = torch.empty(int(need), dtype=torch.uint8, device=self.dev)
+        cut = mixed_cut if mixed_cut is not None else 0.0
+        rc = L.gs_fock_jk_batched_persistent(
+            _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64), _lib.ptr(self.pairs.p32),
+            _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo), _lib.ptr(self.shell_mol),
+            _lib.ptr(self.mol_base), _lib.ptr(self.mol_n), _lib.ptr(dmax), _lib.ptr(self.mol_shell0),
+            _lib.ptr(self.mol_nshell), _lib.ptr(self.mol_sbase), self.mat_stride,
+            self._starts.ctypes.data, self.ntasks, _lib.ptr(self.tasks), _lib.ptr(P), _lib.ptr(J),
+            1, _lib.ptr(P), _lib.ptr(K), screen_thr, cut, _lib.ptr(self._pws), self._pws.numel(),
+            _lib.stream())
+        _lib.check(rc, "gs_fock_jk_batched_persistent")
+
     def _jk_launch(self, P, J, K, precision=64, mixed_cut=None, dmax=None, screen_thr=0.0,
                    classes=None):
         L = _lib.lib()
@@ -183,25 +226,32 @@ class BatchedRHF:
         n = int(self.nbf[m])
         return self.densities[m, :n, :n].cpu().numpy()
 
-    def fock_packed(self, P, precision=64, mixed_cut=None, screen_thr=0.0):
+    def fock_packed(self, P, precision=64, mixed_cut=None, screen_thr=0.0, persistent=False):
         """G = J - K/2 (padded [B, N, N], symmetric) for packed densities P, all molecules.
         With ``screen_thr`` a quartet is skipped when its Schwarz bound times the largest
         |P| element of the six shell blocks it touches is below it; with ``mixed_cut`` the
-        quartets whose such bound is below the cut run in FP32 (FP64 accumulation)."""
+        quartets whose such bound is below the cut run in FP32 (FP64 accumulation).
+        ``persistent``: every class in one persistent launch per precision instead of one
+        launch per class (quartets whose bound is exactly zero are skipped there)."""
         J = torch.zeros_like(P)
         K = torch.zeros_like(P)
         dmax = None
-        if mixed_cut is not None or screen_thr > 0:
+        if mixed_cut is not None or screen_thr > 0 or persistent:
             dmax = torch.zeros(self.nblocks, dtype=torch.float64, device=self.dev)
             dmax.scatter_reduce_(0, self.block_of, P.abs(), "amax", include_self=True)
-        self._jk_launch(P, J, K, precision, mixed_cut, dmax, screen_thr)
+        if persistent:
+            if precision != 64 and mixed_cut is None:
+                raise ValueError("the persistent launch evaluates FP64 unless mixed_cut is given")
+            self._jk_persistent(P, J, K, dmax, mixed_cut, screen_thr)
+        else:
+            self._jk_launch(P, J, K, precision, mixed_cut, dmax, screen_thr)
         Jb, Kb = self.to_padded(J), self.to_padded(K)
         G = (Jb + Jb.transpose(1, 2)) - 0.5 * (Kb + Kb.transpose(1, 2))
         return G
 
     def run(self, threshold=1e-10, max_iter=60, mixed_cut=None, screen_thr=0.0,
             incremental=False, reset_every=8, final_fp64=None, use_graph=True,
-            log_iterations=False, guess="core"):
+            log_iterations=False, guess="core", persistent=False):
         """Batched SCF; returns total energies (numpy) and the iteration count.
 
         With ``incremental`` the Fock build of iteration i evaluates G(P_i - P_ref) and adds
@@ -209,11 +259,13 @@ class BatchedRHF:
         skips most quartets once the densities settle, and a converged molecule (dP = 0)
         costs nothing.  ``final_fp64`` (default: on whenever a build is approximate)
         evaluates the reported energies from one full, unscreened FP64 build at the final
-        densities.  ``log_iterations`` records (iteration, seconds, converged molecules) in
+        densities.  ``persistent`` builds every Fock matrix with the persistent launch
+        (one kernel per precision over all classes and molecules) instead of one launch per
+        class; either way the build is captured in one CUDA graph.  ``log_iterations`` records (iteration, seconds, converged molecules) in
         ``iteration_log`` (it synchronises the device once per iteration).  ``guess`` is
         "core" (the reference's core-Hamiltonian start) or "sad" (superposed atomic
         densities, gaussium_gb300.guess)."""
-        key = (mixed_cut, screen_thr)
+        key = (mixed_cut, screen_thr, persistent)
         if key in self._graphs:
             P_static, g, G_static = self._graphs[key]
         else:
@@ -221,7 +273,8 @@ class BatchedRHF:
             g = G_static = None
 
         def build():
-            return self.fock_packed(P_static, mixed_cut=mixed_cut, screen_thr=screen_thr)
+            return self.fock_packed(P_static, mixed_cut=mixed_cut, screen_thr=screen_thr,
+                                    persistent=persistent)
 
         if use_graph and g is None:
             build()                                  # warm-up outside capture
@@ -294,8 +347,8 @@ def batched_task_list(q, pair_class, pair_mol, nprim, thr, nclass, nmol):
     """Unique shell-quartet tasks (bra pair, ket pair) of many molecules, on the device of
     the inputs: for every class pair (cb >= ck) and every molecule, the pairs of that
     molecule with q_bra q_ket >= thr (bra >= ket within one class), quartets never
-    crossing molecules.  Each class segment is ordered by (primitive pairs of the bra, of
-    the ket), molecule by molecule otherwise.  Returns [((la, lb, lc, ld), start, end)]
+    crossing molecules.  Each class segment is ordered by primitive-quartet count, largest
+    first, then (primitive pairs of the bra, of the ket), molecule by molecule otherwise.  Returns [((la, lb, lc, ld), start, end)]
     and the [ntask, 2] int32 task array."""
     dev = q.device
     key = pair_mol * nclass + pair_class
@@ -324,7 +377,9 @@ def batched_task_list(q, pair_class, pair_mol, nprim, thr, nclass, nmol):
             bra, ket = bra[keep], ket[keep]
             if bra.numel() == 0:
                 continue
-            perm = torch.argsort(nprim[bra] * 4096 + nprim[ket], stable=True)
+            # most primitive quartets first, equal (K_bra, K_ket) together
+            perm = torch.argsort((nprim[bra] * nprim[ket]) * 4096 + nprim[bra] * 64 + nprim[ket],
+                                 descending=True, stable=True)
             tk = torch.stack([bra[perm], ket[perm]], 1).to(torch.int32)
             (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
             segs.append(((la, lb, lc, ld), n, n + tk.shape[0]))

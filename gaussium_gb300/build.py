@@ -88,23 +88,27 @@ def generate():
         tag = "".join(map(str, cls))
         path = os.path.join(GEN, f"eri_k_{tag}.cu")
         L = sum(cls)
-        if L >= WIDE_PROG_MIN:
-            inc = '#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n' % (tag, tag)
-        else:
+        if L < WIDE_PROG_MIN:
             # no warp program: the warp kernels are never selected below WIDE_PROG_MIN
-            inc = ('#include "eri_class_%s.h"\nnamespace gs { template <> struct WideProg<%d, %d, %d, %d> '
-                   '{ static constexpr int NVSLOT = 1, NVSEG = 0, VGROUP = 1, HSIZE = 1, NHLEV = 0; '
-                   'static constexpr int NVSLOT_G = 1, NVSEG_G = 0; '
-                   'static __device__ const uint4* vrec() { return nullptr; } '
-                   'static __device__ const int* vseg() { return nullptr; } '
-                   'static __device__ const unsigned short* vtgt() { return nullptr; } '
-                   'static __device__ const uint4* vrec_g() { return nullptr; } '
-                   'static __device__ const int* vseg_g() { return nullptr; } '
-                   'static __device__ const unsigned short* vtgt_g() { return nullptr; } '
-                   'static __device__ const unsigned int* hop() { return nullptr; } '
-                   'static __device__ const int* hlev() { return nullptr; } '
-                   'static __device__ const unsigned short* outslot() { return nullptr; } }; }\n'
-                   % (tag, *cls))
+            stub = ('// written by build.py -- no warp program below total angular momentum %d\n'
+                    '#pragma once\nnamespace gs { template <> struct WideProg<%d, %d, %d, %d> '
+                    '{ static constexpr int NVSLOT = 1, NVSEG = 0, VGROUP = 1, HSIZE = 1, NHLEV = 0; '
+                    'static constexpr int NVSLOT_G = 1, NVSEG_G = 0; '
+                    'static __device__ const uint4* vrec() { return nullptr; } '
+                    'static __device__ const int* vseg() { return nullptr; } '
+                    'static __device__ const unsigned short* vtgt() { return nullptr; } '
+                    'static __device__ const uint4* vrec_g() { return nullptr; } '
+                    'static __device__ const int* vseg_g() { return nullptr; } '
+                    'static __device__ const unsigned short* vtgt_g() { return nullptr; } '
+                    'static __device__ const unsigned int* hop() { return nullptr; } '
+                    'static __device__ const int* hlev() { return nullptr; } '
+                    'static __device__ const unsigned short* outslot() { return nullptr; } }; }\n'
+                    % (WIDE_PROG_MIN, *cls))
+            spath = os.path.join(GEN, f"eri_wide_{tag}.h")
+            if not os.path.exists(spath) or open(spath).read() != stub:
+                with open(spath, "w") as f:
+                    f.write(stub)
+        inc = '#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n' % (tag, tag)
         code = ('#define GS_WIDE64_MIN %d\n#define GS_WIDE32_MIN %d\n#define GS_THREAD64_MAX %d\n'
                 '#define GS_THREAD32_MAX %d\n#define GS_WIDE_FROM %d\n#define GS_WIDE32_FROM %d\n'
                 '#include "eri_launch.cuh"\n%s'
@@ -117,10 +121,20 @@ def generate():
         if not os.path.exists(path) or open(path).read() != code:
             with open(path, "w") as f:
                 f.write(code)
-        deps = [os.path.join(GEN, f"eri_class_{tag}.h")]
-        if L >= WIDE_PROG_MIN:
-            deps.append(os.path.join(GEN, f"eri_wide_{tag}.h"))
+        deps = [os.path.join(GEN, f"eri_class_{tag}.h"), os.path.join(GEN, f"eri_wide_{tag}.h")]
         units.append((path, deps))
+    # every class's recursion and warp program in one header, for the persistent kernels
+    agg = "// written by build.py\n#pragma once\n" + "".join(
+        '#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n' % (("".join(map(str, c)),) * 2)
+        for c in built)
+    path = os.path.join(GEN, "eri_all_classes.h")
+    if not os.path.exists(path) or open(path).read() != agg:
+        with open(path, "w") as f:
+            f.write(agg)
+    all_deps = [os.path.join(GEN, f"eri_{k}_{''.join(map(str, c))}.h") for c in built
+                for k in ("class", "wide")] + [path, os.path.join(CSRC, "persistent.cuh")]
+    for prec in (64, 32):
+        units.append((os.path.join(CSRC, f"persistent{prec}.cu"), all_deps))
     # one translation unit per gradient class (the fused adjoint kernels, csrc/eri_grad.cuh)
     for cls in built:
         tag = "".join(map(str, cls))
@@ -168,6 +182,8 @@ def build(jobs=None, verbose=False):
     todo.append((os.path.join(CSRC, "xc.cu"), [], os.path.join(BUILD, "xc.o")))
     todo.append((os.path.join(CSRC, "symmetry.cu"), [], os.path.join(BUILD, "symmetry.o")))
     todo.append((os.path.join(CSRC, "dense.cu"), [], os.path.join(BUILD, "dense.o")))
+    todo.append((os.path.join(CSRC, "persistent_capi.cu"), [os.path.join(CSRC, "persistent.cuh")],
+                 os.path.join(BUILD, "persistent_capi.o")))
     todo.append((os.path.join(CSRC, "eri_grad.cu"),
                  [os.path.join(CSRC, "eri_grad.cuh"), os.path.join(GEN, "eri_grad_list.h")],
                  os.path.join(BUILD, "eri_grad.o")))

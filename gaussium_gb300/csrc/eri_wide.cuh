@@ -88,6 +88,65 @@ __device__ __forceinline__ void wide_setup_m(const PrimRec<T>& P, const PrimRec<
     }
 }
 
+// One synchronisation step of the VRR node program: the step's records (noff .. noff+cnt)
+// form waves of WAVE records, each carrying its wave's term count (padded terms multiply
+// the zero coefficient).  A lane takes record j of every wave.  The loop is software
+// pipelined: the operands of the next wave are read from shared memory, and the record of
+// the wave after it from the read-only cache, before the current node is stored -- nodes of
+// one step never read another node of the same step, and never overwrite a slot the step
+// still reads (gen_eri.vrr_waves), so no ordering inside the step is needed.
+template <int WAVE, typename T>
+__device__ __forceinline__ void vrr_step(const uint4* __restrict__ vrec, int noff, int cnt,
+                                         bool group_ok, const T* __restrict__ c, T* nd, int j) {
+    const int nw = (cnt + WAVE - 1) / WAVE;
+    uint4 a = make_uint4(0, 0, 0, 0), b = a, na = a, nb = a;
+    T c0 = T(0), v0 = T(0), c1 = T(0), v1 = T(0), c2 = T(0), v2 = T(0), c3 = T(0), v3 = T(0);
+    T c4 = T(0), v4 = T(0);
+    int n = j;
+    bool act = group_ok && n < cnt;
+    if (act) {
+        a = __ldg(vrec + 2 * (noff + n));
+        b = __ldg(vrec + 2 * (noff + n) + 1);
+        const int nt = a.x >> 16;
+        c0 = c[a.y >> 16]; v0 = nd[a.y & 0xffff];
+        c1 = c[a.z >> 16]; v1 = nd[a.z & 0xffff];
+        if (nt > 2) { c2 = c[a.w >> 16]; v2 = nd[a.w & 0xffff]; }
+        if (nt > 3) { c3 = c[b.x >> 16]; v3 = nd[b.x & 0xffff]; }
+        if (nt > 4) { c4 = c[b.y >> 16]; v4 = nd[b.y & 0xffff]; }
+    }
+    bool nact = group_ok && n + WAVE < cnt;
+    if (nact) {
+        na = __ldg(vrec + 2 * (noff + n + WAVE));
+        nb = __ldg(vrec + 2 * (noff + n + WAVE) + 1);
+    }
+    for (int w = 0; w < nw; ++w) {
+        const int nt = a.x >> 16;
+        T r = c0 * v0;
+        r = fma(c1, v1, r);
+        if (nt > 2) r = fma(c2, v2, r);
+        if (nt > 3) r = fma(c3, v3, r);
+        if (nt > 4) r = fma(c4, v4, r);
+        const int out = a.x & 0xffff;
+        const bool was = act;
+        a = na; b = nb; act = nact;
+        if (act) {                                   // operands of the next wave
+            const int mt = a.x >> 16;
+            c0 = c[a.y >> 16]; v0 = nd[a.y & 0xffff];
+            c1 = c[a.z >> 16]; v1 = nd[a.z & 0xffff];
+            if (mt > 2) { c2 = c[a.w >> 16]; v2 = nd[a.w & 0xffff]; }
+            if (mt > 3) { c3 = c[b.x >> 16]; v3 = nd[b.x & 0xffff]; }
+            if (mt > 4) { c4 = c[b.y >> 16]; v4 = nd[b.y & 0xffff]; }
+        }
+        nact = group_ok && n + 2 * WAVE < cnt;       // record of the wave after it
+        if (nact) {
+            na = __ldg(vrec + 2 * (noff + n + 2 * WAVE));
+            nb = __ldg(vrec + 2 * (noff + n + 2 * WAVE) + 1);
+        }
+        if (was) nd[out] = r;
+        n += WAVE;
+    }
+}
+
 // Evaluate one contracted quartet; on return sm[0 .. HSIZE) holds the HRR buffer whose
 // output slots are W::outslot().
 template <int LA, int LB, int LC, int LD, typename T, int VG>
@@ -130,29 +189,17 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
             const T* __restrict__ c = sC + j * kNCoef;
             if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
             __syncwarp();
+            int noff = __ldg(vseg), cnt = __ldg(vseg + 1);
             for (int s = 0; s < NVSEG; ++s) {
-                const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
-                const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
-                if (sync && s > 0) __syncwarp();
-                int n = lane;
-                uint4 ra = make_uint4(0, 0, 0, 0), rb = ra;
-                if (n < cnt) {
-                    ra = __ldg(vrec + 2 * (noff + n));
-                    rb = __ldg(vrec + 2 * (noff + n) + 1);
+                int noff_n = 0, cnt_n = 0;
+                if (s + 1 < NVSEG) {                         // next step's header, early
+                    noff_n = __ldg(vseg + 4 * (s + 1));
+                    cnt_n = __ldg(vseg + 4 * (s + 1) + 1);
                 }
-                for (; n < cnt; n += 32) {
-                    const uint4 a = ra, b = rb;
-                    if (n + 32 < cnt) {                       // prefetch the next node
-                        ra = __ldg(vrec + 2 * (noff + n + 32));
-                        rb = __ldg(vrec + 2 * (noff + n + 32) + 1);
-                    }
-                    T r = c[a.y >> 16] * node[a.y & 0xffff];
-                    r = fma(c[a.z >> 16], node[a.z & 0xffff], r);
-                    if (nt > 2) r = fma(c[a.w >> 16], node[a.w & 0xffff], r);
-                    if (nt > 3) r = fma(c[b.x >> 16], node[b.x & 0xffff], r);
-                    if (nt > 4) r = fma(c[b.y >> 16], node[b.y & 0xffff], r);
-                    node[a.x & 0xffff] = r;
-                }
+                if (s > 0) __syncwarp();
+                vrr_step<32, T>(vrec, noff, cnt, true, c, node, lane);
+                noff = noff_n;
+                cnt = cnt_n;
             }
             __syncwarp();
 #pragma unroll
@@ -163,34 +210,30 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
             __syncwarp();
         }
         } else {
-        // VG primitive quartets at a time: the (quartet, node) pairs of a level form one
-        // index space spread over the lanes; quartet g has its own node buffer.  The
-        // accumulators add the quartets in order, so the sums match the one-at-a-time form.
+        // VG primitive quartets at a time: lane = (quartet g, record j of a wave of 32/VG);
+        // quartet g has its own node buffer.  The accumulators add the quartets in order,
+        // so the sums match the one-at-a-time form.
+        constexpr int WAVE = 32 / VG;
+        const int g = lane / WAVE, jw = lane - g * WAVE;
         for (int j0 = 0; j0 < nb; j0 += VG) {
             const int ng = min(VG, nb - j0);
             for (int x = lane; x < ng * (L + 1); x += 32) {
-                const int g = x / (L + 1), m = x - g * (L + 1);
-                node[g * NVS + m] = sF[(j0 + g) * (L + 1) + m];
+                const int gg = x / (L + 1), m = x - gg * (L + 1);
+                node[gg * NVS + m] = sF[(j0 + gg) * (L + 1) + m];
             }
             __syncwarp();
+            int noff = __ldg(vseg), cnt = __ldg(vseg + 1);
             for (int s = 0; s < NVSEG; ++s) {
-                const int noff = __ldg(vseg + 4 * s), cnt = __ldg(vseg + 4 * s + 1);
-                const int nt = __ldg(vseg + 4 * s + 2), sync = __ldg(vseg + 4 * s + 3);
-                if (sync && s > 0) __syncwarp();
-                const int tot = ng * cnt;
-                for (int x = lane; x < tot; x += 32) {
-                    const int g = x / cnt, n = x - g * cnt;
-                    const uint4 a = __ldg(vrec + 2 * (noff + n));
-                    const uint4 b = __ldg(vrec + 2 * (noff + n) + 1);
-                    const T* __restrict__ c = sC + (j0 + g) * kNCoef;
-                    T* nd = node + g * NVS;
-                    T r = c[a.y >> 16] * nd[a.y & 0xffff];
-                    r = fma(c[a.z >> 16], nd[a.z & 0xffff], r);
-                    if (nt > 2) r = fma(c[a.w >> 16], nd[a.w & 0xffff], r);
-                    if (nt > 3) r = fma(c[b.x >> 16], nd[b.x & 0xffff], r);
-                    if (nt > 4) r = fma(c[b.y >> 16], nd[b.y & 0xffff], r);
-                    nd[a.x & 0xffff] = r;
+                int noff_n = 0, cnt_n = 0;
+                if (s + 1 < NVSEG) {
+                    noff_n = __ldg(vseg + 4 * (s + 1));
+                    cnt_n = __ldg(vseg + 4 * (s + 1) + 1);
                 }
+                if (s > 0) __syncwarp();
+                vrr_step<WAVE, T>(vrec, noff, cnt, g < ng, sC + (j0 + g) * kNCoef,
+                                  node + g * NVS, jw);
+                noff = noff_n;
+                cnt = cnt_n;
             }
             __syncwarp();
 #pragma unroll
@@ -198,7 +241,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                 const int t = lane + 32 * k;
                 if (t < NACC) {
                     const int v = __ldg(vtgt + t);
-                    for (int g = 0; g < ng; ++g) acc[k] += node[g * NVS + v];
+                    for (int gg = 0; gg < ng; ++gg) acc[k] += node[gg * NVS + v];
                 }
             }
             __syncwarp();

@@ -457,11 +457,14 @@ def vrr_waves(nodes, L, target_slots, wave=32):
             if lu == k and s > L:
                 free.append(phys[s])
         free.sort(reverse=True)
+    # one segment per step: its waves are consecutive runs of ``wave`` records, each padded
+    # to the wave's largest term count, which every record of the wave carries
     vrec, vseg = [], []
     for k, st in enumerate(steps):
-        for i, w in enumerate(st):
+        seg = [len(vrec) // 8, 0, sum(len(w) for w in st), 0, k, 1 if k > 0 else 0]
+        for w in st:
             nt = max(len(byout[o]) for o in w)
-            vseg.append([len(vrec) // 8, 0, len(w), nt, k, 1 if (i == 0 and k > 0) else 0])
+            seg[3] = max(seg[3], nt)
             for o in w:
                 ts = byout[o]
                 assert all(cid != ZERO_COEF for cid, _ in ts), "zero slot in use"
@@ -469,17 +472,23 @@ def vrr_waves(nodes, L, target_slots, wave=32):
                 words += [(ZERO_COEF << 16)] * (nt - len(ts))
                 words += [0] * (8 - len(words))
                 vrec.extend(words)
+        vseg.append(seg)
     return vrec, vseg, phys, top
 
 
 def wave_efficiency(vrec, vseg, lanes_per_node=1):
-    """Useful FMA lane-slots over issued lane-slots of a scheduled VRR program."""
+    """Useful FMA lane-slots over issued lane-slots of a scheduled VRR program whose
+    waves are ``32 // lanes_per_node`` records long."""
+    wave = 32 // lanes_per_node
     useful = issued = 0
-    for noff, _, cnt, nt, _, _ in vseg:
-        for n in range(cnt):
-            useful += sum(1 for w in vrec[8 * (noff + n) + 1: 8 * (noff + n) + 1 + nt]
-                          if (w >> 16) != ZERO_COEF)
-        issued += 32 * nt
+    for noff, _, cnt, _, _, _ in vseg:
+        for w0 in range(0, cnt, wave):
+            nt = vrec[8 * (noff + w0)] >> 16
+            for n in range(w0, min(cnt, w0 + wave)):
+                r = 8 * (noff + n)
+                assert vrec[r] >> 16 == nt
+                useful += sum(1 for w in vrec[r + 1: r + 1 + nt] if (w >> 16) != ZERO_COEF)
+            issued += 32 * nt
     return useful * lanes_per_node / issued
 
 

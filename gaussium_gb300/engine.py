@@ -9,7 +9,9 @@ Layout in HBM (all owned by torch tensors):
                 (p, 1/2p, P, PA, Kp) -- see csrc/eri_common.cuh.
   tasks         write tasks (24 B: bra, ket, permutation code, output offset) or Fock
                 tasks (8 B: bra, ket), grouped by angular-momentum class and sorted by
-                primitive counts so a warp's threads run the same loop trip counts.
+                primitive-quartet count, largest first (so a launch does not end on its
+                longest blocks), equal primitive counts together (a warp's threads run
+                the same loop trip counts).
 """
 import numpy as np
 import torch
@@ -177,7 +179,10 @@ class QuartetBatch:
         nb = self.pairs.nprim[:n]
         nk = self.pairs.nprim[n:]
         cls = pcb * 6 + pck
-        order = np.lexsort((nk, nb, cls))
+        # within a class, most primitive quartets first (the longest blocks start first, so
+        # the short ones fill the end of the launch), equal (K_bra, K_ket) kept together so
+        # that the lanes of a warp run the same loop trip counts
+        order = np.lexsort((-nk, -nb, -(nb * nk), cls))
         tasks = np.zeros(n, dtype=WRITE_TASK_DTYPE)
         tasks["bra"] = order
         tasks["ket"] = order + n
@@ -300,8 +305,10 @@ class JKEngine:
                 ket_pos = start[bra_pos] + within
                 bra = bra_sorted[bra_pos]
                 ket = ket_sorted[ket_pos]
-                key = nprim[bra] * 64 + nprim[ket]
-                key, o = torch.sort(key, stable=True)
+                # most primitive quartets first (longest tasks start first), equal
+                # (K_bra, K_ket) together
+                key = (nprim[bra] * nprim[ket]) * 4096 + nprim[bra] * 64 + nprim[ket]
+                key, o = torch.sort(key, descending=True, stable=True)
                 t = torch.stack([bra[o], ket[o]], dim=1).to(torch.int32)
                 (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
                 self.segments.append(((la, lb, lc, ld), ntot, ntot + total))

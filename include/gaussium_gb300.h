@@ -307,6 +307,33 @@ int gs_lda_xc(long long npts, const double* rho, const double* weights, double s
 int gs_symmetry_zero(int n, int nops, const int* table, const unsigned char* flip,
                      const int* centre_id, const int* parity, double* tensor, void* stream);
 
+/* Bytes of workspace gs_fock_jk_batched_persistent needs for ntask tasks. */
+long long gs_fock_jk_persistent_workspace(int ntask);
+
+/* Batched J/K of many molecules with every angular-momentum class in one persistent launch
+ * per precision: the work distribution of TwoElectronRepulsion.create_repulsion_matrix over
+ * multiprocessing.Pool.starmap (matrixelements/electron_repulsion_matrix.py:35-39) and the
+ * Fock contraction of FockMatrixRestricted.create (hartreefock/fock_matrix.py:12-22).
+ * tasks: the unique quartets of all molecules, grouped by canonical class; class_start is a
+ * HOST array of 22 entries, the start of each canonical class's segment (class order
+ * (00|00), (10|00), (10|10), (11|00) ... (22|22)) and the task count last.  One partition
+ * pass drops quartets with density-weighted bound (Schwarz q_bra q_ket times the largest |P|
+ * of the six shell blocks, from molecule m's table at mol_dmax + mol_sbase[m]) below
+ * screen_thr (0: only exact zeros) and sends those below mixed_cut to FP32 (0: all FP64);
+ * then one FP64 and one FP32 persistent kernel stride over tiles of 32 quartets (small
+ * classes) or single quartets (warp form) of all classes.  Other arguments as
+ * gs_fock_jk_batched_mixed. */
+int gs_fock_jk_batched_persistent(const void* pair_rec, const void* prim64, const void* prim32,
+                                  const double* comp_scale, const int* func_off,
+                                  const int* shell_mol, const long long* mol_base,
+                                  const int* mol_n, const double* mol_dmax,
+                                  const int* mol_shell0, const int* mol_nshell,
+                                  const long long* mol_sbase, long long mat_stride,
+                                  const int* class_start, int ntask, const int* tasks,
+                                  const double* pj, double* j, int nk, const double* pk,
+                                  double* k, double screen_thr, double mixed_cut,
+                                  void* workspace, long long ws_bytes, void* stream);
+
 /* Dense N^4 ERI tensor from unique shell-quartet blocks: the 8-fold expansion of
  * TwoElectronRepulsion.create_repulsion_matrix (matrixelements/electron_repulsion_matrix.py:
  * 43-45).  quartets[4*q..4*q+3] = shells (A, B, C, D) of block q; its n_A n_B n_C n_D values

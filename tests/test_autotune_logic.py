@@ -41,7 +41,12 @@ def test_vrr_group_choice():
     assert vg > 1
     assert (gen_eri.wave_efficiency(prog["vrec"], prog["vseg"], vg) >
             gen_eri.wave_efficiency(base["vrec"], base["vseg"]) + 0.3)
-    assert max(s[2] for s in prog["vseg"]) <= 32 // vg
+    # waves of 32 // vg records share a term count (the kernel reads it per record)
+    rec = prog["vrec"]
+    for noff, _, cnt, _, _, _ in prog["vseg"]:
+        for w0 in range(0, cnt, 32 // vg):
+            nts = {rec[8 * (noff + n)] >> 16 for n in range(w0, min(cnt, w0 + 32 // vg))}
+            assert len(nts) == 1
     for cls in ((2, 2, 2, 1), (2, 2, 2, 2)):
         vg, prog = gen_eri.vrr_group(cls)
         assert vg * prog["nvslot"] <= gen_eri.VGROUP_SLOT_BUDGET

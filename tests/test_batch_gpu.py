@@ -43,3 +43,26 @@ def test_batched_sad_guess_same_energies(gpu_lib, batch_case):
     e, it = b.run(threshold=1e-11, guess="sad")
     assert b.converged.all()
     assert np.max(np.abs(e - single)) < 1e-8
+
+
+@pytest.mark.parametrize("mixed_cut,screen_thr", [(None, 0.0), (1e-2, 1e-12)])
+def test_persistent_launch_matches_per_class_launches(gpu_lib, batch_case, mixed_cut, screen_thr):
+    """One persistent launch per precision over every class and molecule gives the Fock
+    matrices of the per-class launches (same quartets, same precision split)."""
+    import torch
+    b, _ = batch_case
+    rng = np.random.default_rng(3)
+    P = torch.tensor(rng.standard_normal(b.mat_stride) * 0.1, device="cuda")
+    g1 = b.fock_packed(P, mixed_cut=mixed_cut, screen_thr=screen_thr)
+    g2 = b.fock_packed(P, mixed_cut=mixed_cut, screen_thr=screen_thr, persistent=True)
+    scale = float(g1.abs().max())
+    tol = 1e-12 if mixed_cut is None else 1e-6
+    assert float((g1 - g2).abs().max()) <= tol * scale
+
+
+def test_persistent_batched_scf(gpu_lib, batch_case):
+    b, single = batch_case
+    e, it = b.run(threshold=1e-10, mixed_cut=1e-2, screen_thr=1e-12, incremental=True,
+                  persistent=True)
+    assert b.converged.all()
+    assert np.max(np.abs(e - single)) < 1e-6

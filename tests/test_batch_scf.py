@@ -89,7 +89,8 @@ def _task_list_loops(q, pc, pair_mol, nprim, thr, nclass):
                             out.setdefault((cb, ck), []).append((nprim[b], nprim[k], b, k))
     segs, rows = [], []
     for (cb, ck), lst in sorted(out.items()):
-        lst = sorted(lst, key=lambda r: (r[0], r[1]))          # stable: generation order
+        # most primitive quartets first, then (K_bra, K_ket) descending; stable
+        lst = sorted(lst, key=lambda r: (-(r[0] * r[1]), -r[0], -r[1]))
         (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
         segs.append(((la, lb, lc, ld), len(rows), len(rows) + len(lst)))
         rows.extend((b, k) for _, _, b, k in lst)

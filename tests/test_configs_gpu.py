@@ -72,7 +72,7 @@ def test_synthetic_k6_golden(gpu_lib, precision):
     """The reference's ObaraSaika values for K = 1-6 (and K = 6 on all four shells) in
     every canonical class: FP64 within the reference's own Boys error (its series stops
     at a term below 1e-10) and within 1e-10 absolute of the exact-Boys oracle; FP32
-    within 1e-6 of the golden's largest value."""
+    within 1e-4 of the golden's largest value (the tolerance of every FP32 class test)."""
     from gaussium_gb300 import engine
     from gaussium_gb300.basis import ShellBasis
     g = golden("synthetic_k6")
@@ -95,7 +95,7 @@ def test_synthetic_k6_golden(gpu_lib, precision):
                        for si, qi in enumerate(g["sample_quartet"])])
         assert np.max(np.abs(got - oracle.eri_functions(table, fq, boys_mode=1))) < 1e-10
     else:
-        assert np.max(np.abs(got - g["os"])) < 1e-6 * np.abs(g["os"]).max()
+        assert np.max(np.abs(got - g["os"])) < 1e-4 * np.abs(g["os"]).max()
 
 
 @pytest.fixture(scope="module")

@@ -48,8 +48,7 @@ def emulate(cls, pr, pd, bra, ket, grouped=False):
             node[:L + 1] = F
             rec = p["vrec"]
             new, reads = {}, set()
-            for noff, _, cnt, nt, lv, sync in p["vseg"]:
-                assert cnt <= 32
+            for noff, _, cnt, nt_max, lv, sync in p["vseg"]:
                 if sync:
                     # no lane of a step may overwrite a slot another lane of it still reads
                     assert not (reads & set(new))
@@ -58,7 +57,8 @@ def emulate(cls, pr, pd, bra, ket, grouped=False):
                     new, reads = {}, set()
                 for n in range(cnt):
                     w = rec[8 * (noff + n): 8 * (noff + n) + 8]
-                    assert w[0] >> 16 == nt
+                    nt = w[0] >> 16                    # the record's wave term count
+                    assert 2 <= nt <= nt_max
                     r = 0.0
                     for tt in range(nt):
                         x = w[1 + tt]
