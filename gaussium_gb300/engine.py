@@ -41,13 +41,23 @@ def _check_sizes():
         raise _lib.GsError(f"record sizes mismatch: library {tuple(sizes)}")
 
 
+def indexed_device(device):
+    """The device with its index made explicit ('cuda' -> 'cuda:<current>'), so that a
+    comparison with a tensor's device is exact."""
+    d = torch.device(device)
+    if d.type == "cuda" and d.index is None:
+        d = torch.device("cuda", torch.cuda.current_device())
+    return d
+
+
 def _check_device_tensor(t, device, what, shape=None):
     """Tensors handed to a kernel must be float64 on the engine's CUDA device (a host
-    pointer or a float32 buffer would be read as the wrong memory)."""
+    pointer or a float32 buffer would be read as the wrong memory, a tensor on another
+    GPU as another device's memory)."""
     if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64:
         raise _lib.GsError(f"{what} must be a float64 CUDA tensor")
-    if t.device != torch.device(device) and torch.device(device).index is not None:
-        raise _lib.GsError(f"{what} is on {t.device}, the engine on {device}")
+    if t.device != indexed_device(device):
+        raise _lib.GsError(f"{what} is on {t.device}, the engine on {indexed_device(device)}")
     if shape is not None and tuple(t.shape) != tuple(shape):
         raise ValueError(f"{what} has shape {tuple(t.shape)}, expected {tuple(shape)}")
     if shape is None and not t.is_contiguous():
@@ -59,7 +69,7 @@ class DeviceShells:
 
     def __init__(self, sb: ShellBasis, device="cuda"):
         self.host = sb
-        self.device = torch.device(device)
+        self.device = indexed_device(device)
 
         def t(a, dt):
             return torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.device)

@@ -144,7 +144,10 @@ int gs_fock_jk_mixed(int la, int lb, int lc, int ld, const void* pair_rec, const
  * every GPU that loads the library until the process exits; ntask above
  * gs_fock_jk_mixed_noalloc_max_tasks() (2^20) returns GS_ERR_LIMIT.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) with that device
- * current, so make that first call before any stream capture.  All calls share the one
+ * current, so make that first call before any stream capture.  The address is kept for
+ * the life of the process: after cudaDeviceReset (or anything else that re-creates the
+ * device's primary context) the kept address is stale, so do not call this entry point
+ * again in that process.  All calls share the one
  * array: the counts are cleared at the start of every call, and calls that overlap on
  * the GPU (different streams, no ordering) race.  No counterpart in the reference. */
 int gs_fock_jk_mixed_noalloc(int la, int lb, int lc, int ld, const void* pair_rec,

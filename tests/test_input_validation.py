@@ -77,3 +77,25 @@ def test_diis_falls_back_on_singular_b_matrix():
     c = d._coefficients()
     assert np.isfinite(c).all()
     assert len(d.fock_array) < 3
+
+
+def test_device_comparison_is_exact(monkeypatch):
+    """An engine on 'cuda' means the current device: a tensor on another GPU is refused
+    (its pointer would be read as this device's memory)."""
+    from gaussium_gb300 import _lib
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 0)
+    assert engine.indexed_device("cuda") == torch.device("cuda", 0)
+    assert engine.indexed_device("cuda:1") == torch.device("cuda", 1)
+
+    class FakeCuda:                 # stands in for a float64 tensor on cuda:1
+        is_cuda = True
+        dtype = torch.float64
+        device = torch.device("cuda", 1)
+        shape = (2, 2)
+
+        def is_contiguous(self):
+            return True
+    monkeypatch.setattr(engine.torch, "Tensor", FakeCuda)
+    with pytest.raises(_lib.GsError):
+        engine._check_device_tensor(FakeCuda(), "cuda", "density matrix")
+    engine._check_device_tensor(FakeCuda(), "cuda:1", "density matrix")
