@@ -4,9 +4,12 @@
 //
 // One warp per unique shell quartet (A B | C D): its lanes stride over the block's
 // n_A n_B n_C n_D elements (row-major, as the class kernels write them at offset[q]) and
-// store each value at its eight index images.  Images that coincide (A = B, C = D or
-// AB = CD) receive the same value from several lanes, so no element needs an owner.
-// HBM-bound: every tensor element is written at least once, 8 bytes each.
+// store each value at its eight index images.  Where shells repeat (A = B, C = D, or
+// AB = CD) a block holds an index orbit more than once, with values equal only to
+// rounding (they come from different recursion paths); there only the element with
+// a >= b, c >= d and (a, b) >= (c, d) writes, so every orbit has one writer and the tensor
+// has the reference's exact 8-fold symmetry.  HBM-bound: every element written once or
+// more, 8 bytes each.
 #include <cuda_runtime.h>
 #include "gs_args.h"
 
@@ -32,6 +35,9 @@ k_dense_expand(long long nq, const int4* __restrict__ quartets,
     for (int e = lane; e < size; e += 32) {
         const int id = e % nd, ic = (e / nd) % nc, ib = (e / (nd * nc)) % nb, ia = e / (nd * nc * nb);
         const long long a = fa + ia, b = fb + ib, c = fc + ic, d = fd + id;
+        if ((s.x == s.y && a < b) || (s.z == s.w && c < d) ||
+            (s.x == s.z && s.y == s.w && (a < c || (a == c && b < d))))
+            continue;                              // another element of the orbit writes
         const double x = v[e];
         out[((a * n + b) * n + c) * n + d] = x;
         out[((b * n + a) * n + c) * n + d] = x;

@@ -304,6 +304,7 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
             c[32] = 2.0 * P.pad;               // 2 alpha (first bra shell)
             c[33] = 2.0 * (P.p - P.pad);       // 2 beta
             c[34] = 2.0 * Q.pad;               // 2 gamma (first ket shell)
+            c[35] = 5.0 * c[28];               // 5/(2(p+q)), raised (dd|..) classes
             W::prim(c, n, H);
         }
         const double dv[6] = {B.ABx, B.ABy, B.ABz, K.ABx, K.ABy, K.ABz};

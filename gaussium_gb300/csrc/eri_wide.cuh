@@ -25,6 +25,9 @@ template <int LA, int LB, int LC, int LD> struct WideProg;
 #ifndef GS_SETUP_BATCH
 #define GS_SETUP_BATCH 32
 #endif
+#ifndef GS_WIDE_MINB
+#define GS_WIDE_MINB 1        // minimum resident blocks per SM asked of the compiler
+#endif
 constexpr int kWideWarps = GS_WIDE_WARPS;     // warps per block
 constexpr int kNCoef = 32;                    // coefficient slots per primitive quartet
 // coefficient slot set to zero after the set-up: the padding term of nodes whose wave holds
@@ -42,7 +45,15 @@ template <int LA, int LB, int LC, int LD, typename T, int VG = 1> struct WideLay
     // half as many, so that its shared memory stays near the ungrouped form's
     // node slots of the program this form runs (the grouped form has its own schedule)
     static constexpr int NVS = VG == 1 ? W::NVSLOT : W::NVSLOT_G;
-    static constexpr int SB = (VG > 1 && VG * NVS > 1024 && kSetupBatch > 16) ? 16 : kSetupBatch;
+    // primitive quartets set up per round: 32, or 16 for a form whose node buffers are
+    // large -- grouped with more than 1024 slots, or an ungrouped class of total angular
+    // momentum 7 or more whose VRR buffers would outgrow the HRR's (measured: (dd|dp)
+    // 17.7 -> 16.0 ms at 2,000,000 quartets; the smaller classes lose setup parallelism)
+    static constexpr int VRR32 = 32 * kNCoef + 32 * (G::L + 1) + VG * NVS;
+    static constexpr int HRR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
+    static constexpr int SB = kSetupBatch > 16 && ((VG > 1 && VG * NVS > 1024) ||
+                                                   (VG == 1 && G::L >= 7 && VRR32 > HRR_W))
+                                  ? 16 : kSetupBatch;
     static constexpr int SC = SB * kNCoef;                       // coefficients
     static constexpr int SF = SB * (G::L + 1);                   // Boys values
     static constexpr int VRR = SC + SF + VG * NVS;
@@ -260,30 +271,51 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     const int* __restrict__ hlev = W::hlev();
     const T dv0 = T(B.ABx), dv1 = T(B.ABy), dv2 = T(B.ABz);
     const T dv3 = T(K.ABx), dv4 = T(K.ABy), dv5 = T(K.ABz);
+    // Software pipelined per level like the VRR steps: an element of a level reads only
+    // earlier levels' slots, and no level overwrites a slot it reads (gen_eri.py allocates
+    // a level's outputs before releasing the arrays it reads last), so the operands of the
+    // next element are loaded before the current one is stored.
+    int e0 = __ldg(hlev), e1 = __ldg(hlev + 1);
     for (int lv = 0; lv < W::NHLEV; ++lv) {
-        const int e1 = __ldg(hlev + lv + 1);
-        int e = __ldg(hlev + lv) + lane;
-        unsigned int ra = 0, rb = 0;
+        const int e2 = lv + 2 <= W::NHLEV ? __ldg(hlev + lv + 2) : 0;   // next level's end
+        int e = e0 + lane;
+        unsigned int a = 0, b = 0, na = 0, nb = 0;
+        T x = T(0), y = T(0);
         if (e < e1) {
-            ra = __ldg(hop + 2 * e);
-            rb = __ldg(hop + 2 * e + 1);
+            a = __ldg(hop + 2 * e);
+            b = __ldg(hop + 2 * e + 1);
+            x = H[a >> 16];
+            y = H[b & 0xffff];
+        }
+        if (e + 32 < e1) {
+            na = __ldg(hop + 2 * (e + 32));
+            nb = __ldg(hop + 2 * (e + 32) + 1);
         }
         for (; e < e1; e += 32) {
-            const unsigned int a = ra, b = rb;
-            if (e + 32 < e1) {                            // prefetch the next element
-                ra = __ldg(hop + 2 * (e + 32));
-                rb = __ldg(hop + 2 * (e + 32) + 1);
-            }
             const int d = b >> 16;
             const T dv = d == 0 ? dv0 : d == 1 ? dv1 : d == 2 ? dv2 : d == 3 ? dv3 : d == 4 ? dv4 : dv5;
-            H[a & 0xffff] = fma(dv, H[b & 0xffff], H[a >> 16]);
+            const T r = fma(dv, y, x);
+            const int out = a & 0xffff;
+            a = na;
+            b = nb;
+            if (e + 32 < e1) {                            // operands of the next element
+                x = H[a >> 16];
+                y = H[b & 0xffff];
+            }
+            if (e + 64 < e1) {                            // record of the one after it
+                na = __ldg(hop + 2 * (e + 64));
+                nb = __ldg(hop + 2 * (e + 64) + 1);
+            }
+            H[out] = r;
         }
+        e0 = e1;
+        e1 = e2;
         __syncwarp();
     }
 }
 
 template <int LA, int LB, int LC, int LD, typename T, int VG>
-__global__ void __launch_bounds__(32 * kWideWarps) k_wide_write(const WriteArgs a) {
+__global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_write(const WriteArgs a) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
     using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
@@ -423,7 +455,7 @@ __device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restri
 // One warp per task; with a task count on the device (after a partition) the grid is
 // capped and each warp strides over the tasks.
 template <int LA, int LB, int LC, int LD, typename T, int VG>
-__global__ void __launch_bounds__(32 * kWideWarps) k_wide_jk(const JKArgs a) {
+__global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_jk(const JKArgs a) {
     using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

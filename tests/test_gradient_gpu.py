@@ -90,3 +90,46 @@ def test_one_electron_gradient_kernel_matches_host_assembly(gpu_lib):
     g1 = gradient.one_electron_gradient_kernel(sb, mol, sa, P, W)
     g2 = gradient.one_electron_gradient(sb, mol, sa, P, W)
     assert np.max(np.abs(g1 - g2)) < 1e-9
+
+
+@pytest.mark.parametrize("basis", ["6-31G", "6-31G*"])
+def test_gradient_parts_against_fixed_density_differences(gpu_lib, basis):
+    """Each part of the analytic gradient against central differences of its own energy
+    expression with the densities held fixed: the one-electron part
+    sum P (T + V) - sum W S (operator and basis-function derivatives), and the
+    two-electron part 1/2 sum P (J[P] - K[P]/2) (the ERI adjoint kernels)."""
+    from gaussium_gb300 import gradient, molecules
+    from gaussium_gb300.engine import JKEngine
+    from gaussium_gb300.hamiltonian import one_electron
+    from gaussium_gb300.molecules import Molecule
+    import torch
+    base = molecules.water_cluster(1, seed=3)
+    coords = base.coords.copy()
+    coords[1] += np.array([0.05, -0.03, 0.02])
+    mol = Molecule(["O", "H", "H"], coords)
+    st = gradient.rhf_state(mol, basis)
+    P, W = st.P, st.W
+    sa = gradient.shell_atoms(mol, st.sb)
+    g1 = gradient.one_electron_gradient_kernel(st.sb, mol, sa, P, W)
+    g2 = gradient.eri_gradient(st.sb, st.engine, sa, P, 3)
+
+    def parts(xyz):
+        m = Molecule(["O", "H", "H"], xyz)
+        sb = molecules.shell_basis(m, basis)
+        S, T, V = one_electron(sb, m.coords, m.charges)
+        e1 = float(np.sum(P * (T + V)) - np.sum(W * S))
+        eng = JKEngine(sb, schwarz_thr=0.0)
+        pt = torch.tensor(P, device="cuda")
+        J, (K,) = eng.jk(pt, [pt])
+        e2 = 0.5 * float(torch.sum(pt * (J - 0.5 * K)))
+        return e1, e2
+
+    h = 1e-4
+    for a, x in ((0, 0), (1, 1), (2, 2), (1, 0)):
+        xp, xm = coords.copy(), coords.copy()
+        xp[a, x] += h
+        xm[a, x] -= h
+        (p1, p2), (m1, m2) = parts(xp), parts(xm)
+        fd1, fd2 = (p1 - m1) / (2 * h), (p2 - m2) / (2 * h)
+        assert abs(g1[a, x] - fd1) < 1e-6, ("one-electron", a, x, g1[a, x], fd1)
+        assert abs(g2[a, x] - fd2) < 1e-6, ("two-electron", a, x, g2[a, x], fd2)

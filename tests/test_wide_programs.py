@@ -74,10 +74,15 @@ def emulate(cls, pr, pd, bra, ket, grouped=False):
     H[:p["nacc"]] = acc
     dv = [B["AB"][0], B["AB"][1], B["AB"][2], K["AB"][0], K["AB"][1], K["AB"][2]]
     for lv in range(len(p["hlev"]) - 1):
-        new = {}
+        new, reads = {}, set()
         for e in range(p["hlev"][lv], p["hlev"][lv + 1]):
             out, x, y, d = p["hops"][e]
+            reads.update((x, y))
+            assert out not in new                  # one writer per slot and level
             new[out] = H[x] + dv[d] * H[y]
+        # the kernel loads the next element's operands before storing the current one:
+        # no element of a level may write a slot the level reads
+        assert not (reads & set(new))
         for k, v in new.items():
             H[k] = v
     return H[np.array(p["outslot"])]
