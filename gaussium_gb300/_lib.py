@@ -38,6 +38,7 @@ _SIGS = {
                                      D, P]),
     "gs_fock_jk_mixed_noalloc_max_tasks": (I, []),
     "gs_class_variants": (I, [I, I, I, I, I]),
+    "gs_class_form": (I, [I, I, I, I, I]),
     "gs_set_class_variant": (I, [I, I, I, I, I, I]),
     "gs_boys_eval": (I, [I, I, I, P, P, P]),
     "gs_fma_probe": (I, [I, I, I, I, P, P]),

@@ -15,7 +15,8 @@ import torch
 
 from . import _lib
 from .basis import ShellBasis
-from .engine import PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut
+from .engine import (HEAVY_PRIM_QUARTETS, PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut,
+                     split_forms)
 from .hamiltonian import one_electron
 from .molecules import shell_basis
 
@@ -101,6 +102,11 @@ class BatchedRHF:
         self.segments, self.tasks = batched_task_list(q, pc_d, pm_d, nprim, thr, len(PAIR_ORDER),
                                                       len(self.sbs))
         self.ntasks = int(self.tasks.shape[0])
+        # tasks of each segment with many primitive quartets (a prefix: the segments are
+        # sorted by descending primitive work); they run in the warp form (engine.split_forms)
+        work = nprim[self.tasks[:, 0].long()] * nprim[self.tasks[:, 1].long()] \
+            if self.ntasks else torch.zeros(0, dtype=torch.int64, device=self.dev)
+        self.heavy = [int((work[s:e] >= HEAVY_PRIM_QUARTETS).sum()) for _, s, e in self.segments]
 
     def _padded_setup(self):
         B, N = len(self.sbs), self.nmax
@@ -201,16 +207,18 @@ class BatchedRHF:
             runs = [(64, mixed_cut, float("inf")), (32, 0.0, mixed_cut)]
         for prec, lo, hi in runs:
             prims = self.pairs.prims(prec)
-            for cls, s, e in self.segments:
+            for (cls, s, e), heavy in zip(self.segments, self.heavy):
                 if classes is not None and cls not in classes:
                     continue
-                rc = L.gs_fock_jk_batched(*cls, prec, _lib.ptr(self.pairs.rec), _lib.ptr(prims),
-                                          _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
-                                          _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base),
-                                          _lib.ptr(self.mol_n), _lib.ptr(dmax), self.mat_stride,
-                                          e - s, base + s * 8, _lib.ptr(P), _lib.ptr(J), 1,
-                                          _lib.ptr(P), _lib.ptr(K), thr, lo, hi, st)
-                _lib.check(rc, f"gs_fock_jk_batched{cls}")
+                for form, first, count in split_forms(cls, prec, heavy):
+                    m = (e - s - first) if count is None else count
+                    rc = L.gs_fock_jk_batched(
+                        *cls, prec | (form << 8), _lib.ptr(self.pairs.rec), _lib.ptr(prims),
+                        _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
+                        _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
+                        _lib.ptr(dmax), self.mat_stride, m, base + (s + first) * 8, _lib.ptr(P),
+                        _lib.ptr(J), 1, _lib.ptr(P), _lib.ptr(K), thr, lo, hi, st)
+                    _lib.check(rc, f"gs_fock_jk_batched{cls}")
 
     def tune(self, precisions=(64, 32), reps=3):
         """Choose the kernel form of every class with two on this batch's task lists."""

@@ -31,8 +31,9 @@ WIDE64_MIN = int(os.environ.get("GS_WIDE64_MIN", "3"))
 WIDE32_MIN = int(os.environ.get("GS_WIDE32_MIN", "8"))
 THREAD64_MAX = int(os.environ.get("GS_THREAD64_MAX", "4"))
 THREAD32_MAX = 7
-WIDE32_FROM = 5
-WIDE_PROG_MIN = 2          # classes that get generated warp programs
+WIDE32_FROM = 0
+WIDE_PROG_MIN = 0          # classes that get generated warp programs (all: the heavy
+                           # quartets of a thread-form class run in the warp form)
 GRAD_THREAD_LMAX = 3       # gradient classes with a thread-per-quartet form (gen_grad.py)
 
 NVCC = os.environ.get("NVCC", "nvcc")

@@ -43,6 +43,17 @@ inline int pv(int la, int lb, int lc, int ld, int prec) {
     return prec | (g_variant[la][lb][lc][ld][prec == 64 ? 0 : 1] << 8);
 }
 
+// The precision argument of the launch entry points: 64 or 32, optionally with an explicit
+// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp; 0 = the class's configured
+// form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
+int decode_precision(int la, int lb, int lc, int ld, int precision) {
+    const int prec = precision & 0xff, form = precision >> 8;
+    if ((prec != 64 && prec != 32) || form < 0 || form > 3) return -1;
+    if (form == 0) return pv(la, lb, lc, ld, prec);
+    if (!(find_variants(la, lb, lc, ld, prec) & (1 << (form - 1)))) return -1;
+    return prec | (form << 8);
+}
+
 inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
 
 int check_launch() { return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_CUDA; }
@@ -238,6 +249,13 @@ int gs_class_variants(int la, int lb, int lc, int ld, int precision) {
     return find_variants(la, lb, lc, ld, precision);
 }
 
+int gs_class_form(int la, int lb, int lc, int ld, int precision) {
+    launch_fn f = find_class(la, lb, lc, ld);
+    if (!f) return -GS_ERR_CLASS;
+    if (precision != 64 && precision != 32) return -GS_ERR_ARG;
+    return f(GS_KIND_FORM, pv(la, lb, lc, ld, precision), nullptr, nullptr);
+}
+
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant) {
     if (!find_class(la, lb, lc, ld)) return GS_ERR_CLASS;
     if ((precision != 64 && precision != 32) || variant < 0 || variant > 3) return GS_ERR_ARG;
@@ -280,12 +298,12 @@ int gs_eri_blocks(int la, int lb, int lc, int ld, int precision, const void* pai
                   double* out, void* stream) {
     launch_fn f = find_class(la, lb, lc, ld);
     if (!f) return GS_ERR_CLASS;
-    if ((precision != 64 && precision != 32) || ntask < 0 || !pair_rec || !prim || !comp_scale ||
-        !out || (ntask > 0 && !tasks))
+    const int pf = decode_precision(la, lb, lc, ld, precision);
+    if (pf < 0 || ntask < 0 || !pair_rec || !prim || !comp_scale || !out || (ntask > 0 && !tasks))
         return GS_ERR_ARG;
     gs::WriteArgs a{(const gs::PairRec*)pair_rec, prim, comp_scale, (const gs::WriteTask*)tasks,
                     ntask, out};
-    return f(GS_KIND_WRITE, pv(la, lb, lc, ld, precision), &a, S(stream));
+    return f(GS_KIND_WRITE, pf, &a, S(stream));
 }
 
 int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
@@ -295,9 +313,10 @@ int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_r
                double prec_lo, double prec_hi, void* stream) {
     launch_fn f = find_class(la, lb, lc, ld);
     if (!f) return GS_ERR_CLASS;
-    if ((precision != 64 && precision != 32) || ntask < 0 || nbf <= 0 || nk < 0 || !pair_rec ||
-        !prim || !comp_scale || !func_off || (ntask > 0 && !tasks) || (!!pj != !!j) ||
-        (nk > 0 && (!pk || !k)) || (screen_thr > 0 && !shell_dmax))
+    const int pf = decode_precision(la, lb, lc, ld, precision);
+    if (pf < 0 || ntask < 0 || nbf <= 0 || nk < 0 || !pair_rec || !prim || !comp_scale ||
+        !func_off || (ntask > 0 && !tasks) || (!!pj != !!j) || (nk > 0 && (!pk || !k)) ||
+        (screen_thr > 0 && !shell_dmax))
         return GS_ERR_ARG;
     gs::JKArgs a;
     a.pairs = (const gs::PairRec*)pair_rec;
@@ -323,7 +342,7 @@ int gs_fock_jk(int la, int lb, int lc, int ld, int precision, const void* pair_r
     a.mol_dmax = nullptr;
     a.mat_stride = (long long)nbf * nbf;
     a.ntask_dev = nullptr;
-    return f(GS_KIND_JK, pv(la, lb, lc, ld, precision), &a, S(stream));
+    return f(GS_KIND_JK, pf, &a, S(stream));
 }
 
 int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void* pair_rec,
@@ -334,10 +353,11 @@ int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void
                        double screen_thr, double prec_lo, double prec_hi, void* stream) {
     launch_fn f = find_class(la, lb, lc, ld);
     if (!f) return GS_ERR_CLASS;
-    if ((precision != 64 && precision != 32) || ntask < 0 || nk < 0 || nk > 1 || !pair_rec ||
-        !prim || !comp_scale || !func_off || !shell_mol || !mol_base || !mol_n ||
-        (ntask > 0 && !tasks) || (!!pj != !!j) || (nk > 0 && (!pk || !k)) ||
-        (screen_thr > 0 && !mol_dmax) || mat_stride <= 0)
+    const int pf = decode_precision(la, lb, lc, ld, precision);
+    if (pf < 0 || ntask < 0 || nk < 0 || nk > 1 || !pair_rec || !prim || !comp_scale ||
+        !func_off || !shell_mol || !mol_base || !mol_n || (ntask > 0 && !tasks) ||
+        (!!pj != !!j) || (nk > 0 && (!pk || !k)) || (screen_thr > 0 && !mol_dmax) ||
+        mat_stride <= 0)
         return GS_ERR_ARG;
     gs::JKArgs a;
     a.pairs = (const gs::PairRec*)pair_rec;
@@ -363,7 +383,7 @@ int gs_fock_jk_batched(int la, int lb, int lc, int ld, int precision, const void
     a.mol_dmax = mol_dmax;
     a.mat_stride = mat_stride;
     a.ntask_dev = nullptr;
-    return f(GS_KIND_JK, pv(la, lb, lc, ld, precision), &a, S(stream));
+    return f(GS_KIND_JK, pf, &a, S(stream));
 }
 
 // Bytes of workspace gs_fock_jk_mixed needs for ntask tasks.

@@ -65,6 +65,12 @@ int launch_prec(int kind, int variant, const void* args, cudaStream_t st) {
     int v = variant;
     if (v == 0) v = (!thread || F::L >= wide_min) ? (grouped && F::VG >= 4 ? 3 : 2) : 1;
     if (kind == GS_KIND_SCHWARZ && v == 3) v = 2;
+    if (kind == GS_KIND_FORM) {
+        // the form a launch with this variant resolves to
+        if (v == 3 && grouped) return 3;
+        if (v >= 2 && wide) return 2;
+        return thread ? 1 : (wide ? 2 : 0);
+    }
     if constexpr (grouped) {
         if (v == 3) return launch_wide<LA, LB, LC, LD, PREC, F::VG>(kind, args, st);
     }

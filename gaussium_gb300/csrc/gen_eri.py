@@ -346,8 +346,6 @@ def main():
         with open(path, "w") as f:
             f.write(lst)
     for cls in classes:
-        if sum(cls) < 2:
-            continue
         code, _ = emit_wide(cls)
         path = os.path.join(out, "eri_wide_%s.h" % "".join(map(str, cls)))
         if not os.path.exists(path) or open(path).read() != code:
@@ -489,7 +487,7 @@ def wave_efficiency(vrec, vseg, lanes_per_node=1):
                 assert vrec[r] >> 16 == nt
                 useful += sum(1 for w in vrec[r + 1: r + 1 + nt] if (w >> 16) != ZERO_COEF)
             issued += 32 * nt
-    return useful * lanes_per_node / issued
+    return useful * lanes_per_node / issued if issued else 1.0
 
 
 def wide_program(cls, wave=32):

@@ -5,6 +5,7 @@
 #define GS_KIND_WRITE 0
 #define GS_KIND_JK 1
 #define GS_KIND_SCHWARZ 2
+#define GS_KIND_FORM 3      // launch nothing: return the form a launch would use
 
 #define GS_OK 0
 #define GS_ERR_ARG 1

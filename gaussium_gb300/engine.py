@@ -29,9 +29,29 @@ PRIM_SCREEN = 55.262
 WRITE_TASK_DTYPE = np.dtype([("bra", "<i4"), ("ket", "<i4"), ("code", "<i4"), ("pad", "<i4"),
                              ("off", "<i8")])
 
+# Quartets with at least this many primitive quartets (after the pair screen) run in the
+# warp form even when their class runs one thread per quartet: a warp then sets up 32 of
+# one quartet's primitive quartets at once instead of one thread walking them all, which
+# would make the launch end on a few long-running warps.
+HEAVY_PRIM_QUARTETS = 32
+THREAD_FORM, WARP_FORM, GROUPED_FORM = 1, 2, 3
+
 _pc_lut = np.full((3, 3), -1, dtype=np.int64)
 for _i, (_a, _b) in enumerate(PAIR_ORDER):
     _pc_lut[_a, _b] = _i
+
+
+def split_forms(cls, precision, heavy):
+    """[(form, first, count)] for a class segment whose tasks are sorted by descending
+    primitive-quartet count, ``heavy`` of them at or above HEAVY_PRIM_QUARTETS: the heavy
+    prefix in the class's warp form when the class otherwise runs one thread per quartet.
+    form 0 = the class's configured form."""
+    L = _lib.lib()
+    if heavy <= 0 or L.gs_class_form(*cls, precision) != THREAD_FORM:
+        return [(0, 0, None)]
+    built = L.gs_class_variants(*cls, precision)
+    warp = GROUPED_FORM if built & 4 else WARP_FORM
+    return [(warp, 0, heavy), (THREAD_FORM, heavy, None)]
 
 
 def _check_sizes():
@@ -212,6 +232,9 @@ class QuartetBatch:
         self.ds = ds
         self.sorted_bra_nprim = nb[order]
         self.sorted_ket_nprim = nk[order]
+        work = self.sorted_bra_nprim * self.sorted_ket_nprim
+        self.heavy = [int(np.count_nonzero(work[s:e] >= HEAVY_PRIM_QUARTETS))
+                      for _, s, e in self.segments]
 
     def class_counts(self):
         return {cls: e - s for cls, s, e in self.segments}
@@ -224,13 +247,15 @@ class QuartetBatch:
         st = _lib.stream(stream)
         base = self.tasks.data_ptr()
         prims = self.pairs.prims(precision)
-        for cls, s, e in self.segments:
+        for (cls, s, e), heavy in zip(self.segments, self.heavy):
             if classes is not None and cls not in classes:
                 continue
-            rc = L.gs_eri_blocks(*cls, precision, _lib.ptr(self.pairs.rec), _lib.ptr(prims),
-                                 _lib.ptr(self.ds.comp_scale), e - s,
-                                 base + s * WRITE_TASK, _lib.ptr(out), st)
-            _lib.check(rc, f"gs_eri_blocks{cls}")
+            for form, first, count in split_forms(cls, precision, heavy):
+                n = (e - s - first) if count is None else count
+                rc = L.gs_eri_blocks(*cls, precision | (form << 8), _lib.ptr(self.pairs.rec),
+                                     _lib.ptr(prims), _lib.ptr(self.ds.comp_scale), n,
+                                     base + (s + first) * WRITE_TASK, _lib.ptr(out), st)
+                _lib.check(rc, f"gs_eri_blocks{cls}")
         return out
 
 
@@ -282,6 +307,7 @@ class JKEngine:
         q = self.q
         nprim = torch.as_tensor(self.pairs.nprim).to(dev)
         self.segments = []
+        self.heavy = []           # tasks of each segment with >= HEAVY_PRIM_QUARTETS
         chunks = []
         ntot = 0
         thr = self.schwarz_thr
@@ -322,6 +348,7 @@ class JKEngine:
                 t = torch.stack([bra[o], ket[o]], dim=1).to(torch.int32)
                 (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
                 self.segments.append(((la, lb, lc, ld), ntot, ntot + total))
+                self.heavy.append(int((key >= HEAVY_PRIM_QUARTETS * 4096).sum()))
                 chunks.append(t)
                 ntot += total
         self.tasks = torch.cat(chunks, 0).contiguous() if chunks else \
@@ -389,15 +416,18 @@ class JKEngine:
             runs = []
         for prec, lo, hi in runs:
             prims = self.pairs.prims(prec)
-            for cls, s, e in self.segments:
+            for (cls, s, e), heavy in zip(self.segments, self.heavy):
                 if classes is not None and cls not in classes:
                     continue
-                rc = L.gs_fock_jk(*cls, prec, _lib.ptr(self.pairs.rec), _lib.ptr(prims),
-                                  _lib.ptr(self.ds.comp_scale), _lib.ptr(self.ds.func_off),
-                                  self.sb.nshell, n, e - s, base + s * 8, _lib.ptr(pj_c),
-                                  _lib.ptr(jbuf), nk, _lib.ptr(pk_c), _lib.ptr(kbuf),
-                                  _lib.ptr(dmax), thr, lo, hi, st)
-                _lib.check(rc, f"gs_fock_jk{cls}")
+                for form, first, count in split_forms(cls, prec, heavy):
+                    m = (e - s - first) if count is None else count
+                    rc = L.gs_fock_jk(*cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
+                                      _lib.ptr(prims), _lib.ptr(self.ds.comp_scale),
+                                      _lib.ptr(self.ds.func_off), self.sb.nshell, n, m,
+                                      base + (s + first) * 8, _lib.ptr(pj_c), _lib.ptr(jbuf), nk,
+                                      _lib.ptr(pk_c), _lib.ptr(kbuf), _lib.ptr(dmax), thr, lo,
+                                      hi, st)
+                    _lib.check(rc, f"gs_fock_jk{cls}")
         J = (jbuf + jbuf.T) if jbuf is not None else None
         K = [kbuf[s] + kbuf[s].T for s in range(nk)]
         return J, K

@@ -64,6 +64,15 @@ int gs_class_variants(int la, int lb, int lc, int ld, int precision);
  * forms on the caller's task lists.  No reference counterpart. */
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant);
 
+/* The kernel form (1 thread, 2 warp, 3 grouped warp) a launch of (la lb|lc ld) in that
+ * precision uses with no explicit form: the configured variant, or the built-in default.
+ * The precision argument of gs_eri_blocks, gs_fock_jk and gs_fock_jk_batched may carry an
+ * explicit form in its bits 8.. (precision | form << 8) for that call only; the engine uses
+ * it to run the quartets of a thread-form class that have many primitive quartets in the
+ * warp form, whose lanes share a quartet's primitive quartets.  Negative status on a bad
+ * class or precision.  No reference counterpart. */
+int gs_class_form(int la, int lb, int lc, int ld, int precision);
+
 /* K0 shell-pair builder.  Replaces the per-primitive-quartet prologue of
  * ObaraSaika.integrate (integrals/twoelectronrepulsion/obara_saika_scheme.py:52-70:
  * Gaussian product centre, exponent sums, exp(-ab/p |AB|^2) and the contraction/
