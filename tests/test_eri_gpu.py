@@ -152,3 +152,27 @@ def test_primitive_screening_changes_nothing_measurable(gpu_lib):
         kept = b.prim_quartets / b.full_prim_quartets
     assert float((outs[0] - outs[1]).abs().max()) < 1e-13
     assert kept < 0.8      # the screen does drop work on this distribution
+
+
+def test_heavy_quartets_split_matches_single_form(gpu_lib):
+    """A thread-form class runs its quartets with many primitive quartets in the warp
+    form; the blocks agree with every class on one form."""
+    import torch
+    from gaussium_gb300 import autotune, engine
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(6000, seed=21)
+    ds = engine.DeviceShells(sb)
+    b = engine.QuartetBatch(ds, q, want32=False, max_exp=engine.PRIM_SCREEN)
+    assert sum(b.heavy) > 0
+    split = torch.zeros(b.total, dtype=torch.float64, device="cuda")
+    b.run(split, 64)
+    classes = [c for c, _, _ in b.segments]
+    try:
+        for c in classes:
+            autotune.set_form(c, 64, autotune.WARP)
+        warp = torch.zeros_like(split)
+        b.run(warp, 64)
+    finally:
+        autotune.reset([(c, 0, 0) for c in classes], (64,))
+    scale = float(split.abs().max())
+    assert float((split - warp).abs().max()) <= 1e-12 * scale
