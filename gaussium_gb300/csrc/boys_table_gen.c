@@ -10,6 +10,8 @@
  * F_{m-1} = (2T F_m + exp(-T)) / (2m-1), which is stable.  The kernels evaluate
  * F_m(T) by a Taylor expansion about the nearest grid point and the downward recursion
  * (Helgaker, Jorgensen & Olsen, Molecular Electronic-Structure Theory, sec. 9.8.2).
+ * The grid reaches T = 80, beyond which exp(-T) < 2e-35 changes no F_m (m <= 16) in double
+ * precision, so the kernels' large-T branch needs no exponential.
  *
  * usage: boys_table_gen OUT.h
  */
@@ -17,7 +19,7 @@
 #include <stdio.h>
 
 #define BOYS_INV_H 16
-#define BOYS_TMAX 36
+#define BOYS_TMAX 80
 #define BOYS_ROWS (BOYS_TMAX * BOYS_INV_H + 1)
 #define BOYS_NCOL 18 /* F_0..F_16 and exp(-T) */
 

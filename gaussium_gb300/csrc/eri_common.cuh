@@ -139,10 +139,13 @@ GS_HD GS_INLINE void boys_small(double t, double pref, double* __restrict__ F) {
     }
 }
 
-// F[m] = pref * F_m(t), m = 0..M.  Below BOYS_TMAX: boys_small in FP64 for either T (in
-// FP32 quartets the FP64 values are rounded to float once, so neither the series nor the
-// downward recursion accumulates FP32 rounding).  Above it: F_0 = sqrt(pi/t)/2
-// (erf(sqrt t) = 1 to 2e-17) and upward recursion in T, stable for t > M.
+// F[m] = pref * F_m(t), m = 0..M.  Below BOYS_TMAX (80): boys_small in FP64 for either T
+// (in FP32 quartets the FP64 values are rounded to float once, so neither the series nor
+// the downward recursion accumulates FP32 rounding).  Above it: F_0 = sqrt(pi/t)/2
+// (erf(sqrt t) = 1 to 1e-36) and the upward recursion F_{m+1} = (2m+1) F_m / (2t), whose
+// dropped exp(-t) term changes F_m (m <= 10) by less than 1e-23 relative at t >= 80.  The
+// wide table keeps the large-T branch free of an exponential: lanes of one warp that take
+// different branches cost the sum of both.
 template <int M, typename T>
 GS_HD GS_INLINE void boys(T t, T pref, T* __restrict__ F) {
     constexpr bool dbl = sizeof(T) == 8;
@@ -159,8 +162,7 @@ GS_HD GS_INLINE void boys(T t, T pref, T* __restrict__ F) {
         F[0] = pref * T(0.88622692545275801365) * rs;   // sqrt(pi)/2
         if (M > 0) {
             const T hit = T(0.5) * rs * rs;
-            const T et = t < T(dbl ? 700 : 85) ? pref * gs_exp(-t) : T(0);
-            GS_UNROLL for (int m = 0; m < M; ++m) F[m + 1] = (T(2 * m + 1) * F[m] - et) * hit;
+            GS_UNROLL for (int m = 0; m < M; ++m) F[m + 1] = (T(2 * m + 1) * hit) * F[m];
         }
     }
 }
