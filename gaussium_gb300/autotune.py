@@ -16,8 +16,8 @@ import torch
 
 from . import _lib
 
-THREAD, WARP, GROUPED = 1, 2, 3
-NAMES = {THREAD: "thread", WARP: "warp", GROUPED: "warp-grouped"}
+THREAD, WARP, GROUPED, SPLIT = 1, 2, 3, 4
+NAMES = {THREAD: "thread", WARP: "warp", GROUPED: "warp-grouped", SPLIT: "thread-split"}
 
 
 def forms(cls, precision):
@@ -25,6 +25,8 @@ def forms(cls, precision):
     m = _lib.lib().gs_class_variants(*cls, precision)
     if m < 0:
         _lib.check(-m, f"gs_class_variants{cls}")
+    # the split form serves the heavy quartets of a thread-form class (engine.split_forms);
+    # as a whole-class form it would leave most lanes idle on light quartets
     return [v for v in (THREAD, WARP, GROUPED) if m & (1 << (v - 1))]
 
 
@@ -53,6 +55,7 @@ def tune(segments, run_class, precisions=(64, 32), reps=3, min_tasks=1):
     has two; ``run_class(cls, precision)`` launches that class's work once on the current
     stream.  Returns {(cls, precision): {"form": v, "ms": {v: t}}}."""
     chosen = {}
+    from . import engine
     for prec in precisions:
         for cls, s, e in segments:
             if e - s < min_tasks:
@@ -66,7 +69,18 @@ def tune(segments, run_class, precisions=(64, 32), reps=3, min_tasks=1):
                 times[v] = _time(lambda: run_class(cls, prec), reps)
             best = min(times, key=times.get)
             set_form(cls, prec, best)
-            chosen[(cls, prec)] = {"form": best, "ms": times}
+            row = {"form": best, "ms": times}
+            if best == THREAD:
+                # the thread form runs its heavy quartets in the split form; keep that only
+                # where it measures faster than leaving them on threads
+                engine.SPLIT_OFF.add((cls, prec))
+                off = _time(lambda: run_class(cls, prec), reps)
+                engine.SPLIT_OFF.discard((cls, prec))
+                row["heavy_split"] = off >= times[THREAD]
+                row["ms_without_split"] = off
+                if not row["heavy_split"]:
+                    engine.SPLIT_OFF.add((cls, prec))
+            chosen[(cls, prec)] = row
     return chosen
 
 
@@ -114,10 +128,13 @@ def tune_gradient(segments, run_class, reps=3):
 
 
 def reset(segments, precisions=(64, 32)):
-    """Back to the built-in default form for every class of ``segments``."""
+    """Back to the built-in default form for every class of ``segments`` (heavy quartets
+    of thread-form classes in the split form again)."""
+    from . import engine
     for prec in precisions:
         for cls, _, _ in segments:
             set_form(cls, prec, 0)
+            engine.SPLIT_OFF.discard((cls, prec))
 
 
 def save(chosen, path):

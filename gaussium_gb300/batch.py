@@ -15,7 +15,7 @@ import torch
 
 from . import _lib
 from .basis import ShellBasis
-from .engine import (HEAVY_PRIM_QUARTETS, PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut,
+from .engine import (PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut, heavy_threshold,
                      split_forms)
 from .hamiltonian import one_electron
 from .molecules import shell_basis
@@ -103,10 +103,10 @@ class BatchedRHF:
                                                       len(self.sbs))
         self.ntasks = int(self.tasks.shape[0])
         # tasks of each segment with many primitive quartets (a prefix: the segments are
-        # sorted by descending primitive work); they run in the warp form (engine.split_forms)
+        # sorted by descending primitive work); they run in the split form (engine.split_forms)
         work = nprim[self.tasks[:, 0].long()] * nprim[self.tasks[:, 1].long()] \
             if self.ntasks else torch.zeros(0, dtype=torch.int64, device=self.dev)
-        self.heavy = [int((work[s:e] >= HEAVY_PRIM_QUARTETS).sum()) for _, s, e in self.segments]
+        self.heavy = [int((work[s:e] >= heavy_threshold(cls)).sum()) for cls, s, e in self.segments]
 
     def _padded_setup(self):
         B, N = len(self.sbs), self.nmax

@@ -36,7 +36,8 @@ int find_variants(int la, int lb, int lc, int ld, int prec) {
 // Kernel form per class and precision chosen at run time: 0 = the built-in default by
 // total angular momentum, 1 = one thread per quartet, 2 = one warp per quartet, 3 = one warp
 // per quartet with several primitive quartets per VRR pass.  It rides in bits 8.. of the
-// precision argument of the class launchers.
+// precision argument of the class launchers; 4 = the thread form's code with one warp per
+// quartet over its primitive quartets (split form).
 int g_variant[3][3][3][3][2] = {};
 
 inline int pv(int la, int lb, int lc, int ld, int prec) {
@@ -44,11 +45,11 @@ inline int pv(int la, int lb, int lc, int ld, int prec) {
 }
 
 // The precision argument of the launch entry points: 64 or 32, optionally with an explicit
-// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp; 0 = the class's configured
-// form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
+// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp, 4 split; 0 = the class's
+// configured form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
 int decode_precision(int la, int lb, int lc, int ld, int precision) {
     const int prec = precision & 0xff, form = precision >> 8;
-    if ((prec != 64 && prec != 32) || form < 0 || form > 3) return -1;
+    if ((prec != 64 && prec != 32) || form < 0 || form > 4) return -1;
     if (form == 0) return pv(la, lb, lc, ld, prec);
     if (!(find_variants(la, lb, lc, ld, prec) & (1 << (form - 1)))) return -1;
     return prec | (form << 8);
@@ -258,7 +259,7 @@ int gs_class_form(int la, int lb, int lc, int ld, int precision) {
 
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant) {
     if (!find_class(la, lb, lc, ld)) return GS_ERR_CLASS;
-    if ((precision != 64 && precision != 32) || variant < 0 || variant > 3) return GS_ERR_ARG;
+    if ((precision != 64 && precision != 32) || variant < 0 || variant > 4) return GS_ERR_ARG;
     if (variant && !(find_variants(la, lb, lc, ld, precision) & (1 << (variant - 1))))
         return GS_ERR_ARG;
     g_variant[la][lb][lc][ld][precision == 64 ? 0 : 1] = variant;

@@ -202,6 +202,38 @@ GS_HD GS_INLINE void eri_quartet(const PairRec& B, const PairRec& K,
     G::hrr(acc, T(B.ABx), T(B.ABy), T(B.ABz), T(K.ABx), T(K.ABy), T(K.ABz), blk);
 }
 
+// Contraction accumulators of the quartet over primitive quartets start, start + stride,
+// ... (flat index i * K.nprim + j): the lanes of a warp that shares one quartet's primitive
+// quartets each call this with their own start and stride 32, then sum the accumulators.
+template <int LA, int LB, int LC, int LD, typename T>
+GS_HD GS_INLINE void eri_accumulate(const PairRec& B, const PairRec& K,
+                                    const PrimRec<T>* __restrict__ prims, T* __restrict__ acc,
+                                    int start, int stride) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    const int nK = K.nprim, ntot = B.nprim * nK;
+    for (int x = start; x < ntot; x += stride) {
+        const PrimRec<T> P = prims[B.prim_off + x / nK];
+        const PrimRec<T> Q = prims[K.prim_off + x % nK];
+        const T pq = P.p + Q.p;
+        const T rs = gs_rsqrt(pq);
+        const T ipq = rs * rs;
+        const T PQx = Q.Px - P.Px, PQy = Q.Py - P.Py, PQz = Q.Pz - P.Pz;
+        const T wq = Q.p * ipq, wp = P.p * ipq;
+        const T t = P.p * wq * (PQx * PQx + PQy * PQy + PQz * PQz);
+        T F[G::L + 1];
+        boys<G::L, T>(t, P.Kp * Q.Kp * rs, F);
+        VrrCoef<T> c;
+        c.PAx = P.PAx; c.PAy = P.PAy; c.PAz = P.PAz;
+        c.WPx = wq * PQx; c.WPy = wq * PQy; c.WPz = wq * PQz;
+        c.QCx = Q.PAx; c.QCy = Q.PAy; c.QCz = Q.PAz;
+        c.WQx = -wp * PQx; c.WQy = -wp * PQy; c.WQz = -wp * PQz;
+        c.i2p = P.i2p; c.i2q = Q.i2p;
+        c.rp2 = wq * P.i2p; c.rq2 = wp * Q.i2p;
+        c.i2pq = T(0.5) * ipq;
+        G::vrr(F, c, acc);
+    }
+}
+
 // ------------------------------------------------------------------ shell-pair records
 // Shells as the engine stores them: centre (bohr), angular momentum l, primitives
 // [prim_off[s], prim_off[s+1]) with exponent and effective coefficient (contraction times

@@ -16,16 +16,12 @@ constexpr int kBlock = 128;
 #define GS_THREAD_MINB 1
 #endif
 
+// Block write epilogue: the canonical block of `task`, scaled per component, at its
+// original-order position.
 template <int LA, int LB, int LC, int LD, typename T>
-__global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_write(const WriteArgs a) {
+__device__ __forceinline__ void write_block(const WriteArgs& a, const WriteTask& task,
+                                            const PairRec& B, const PairRec& K, const T* blk) {
     using G = ClassGen<LA, LB, LC, LD>;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.ntask) return;
-    const WriteTask task = a.tasks[t];
-    const PairRec B = a.pairs[task.bra];
-    const PairRec K = a.pairs[task.ket];
-    T blk[G::NBLK];
-    eri_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, blk);
     long long s[4];
     block_strides(task.code, G::NA, G::NB, G::NC, G::ND, s);
     double sab[G::NA * G::NB], scd[G::NC * G::ND];
@@ -46,46 +42,82 @@ __global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_write(const Writ
     }
 }
 
-// Digest the unique quartet (ab|cd) into the symmetric-accumulation matrices
-//   J'_ab += 2 v P_cd,  J'_cd += 2 v P_ab,
-//   K'_ac += v P_bd, K'_ad += v P_bc, K'_bc += v P_ad, K'_bd += v P_ac   (per density)
-// with v = (ab|cd) / ((1+d_ab)(1+d_cd)(1+d_ab,cd)), so that J = J' + J'^T and
-// K = K' + K'^T sum every permutation of every quartet once.
 template <int LA, int LB, int LC, int LD, typename T>
-__device__ __forceinline__ void eri_jk_task(const JKArgs& a, int t) {
+__global__ void __launch_bounds__(kBlock, GS_THREAD_MINB) k_eri_write(const WriteArgs a) {
     using G = ClassGen<LA, LB, LC, LD>;
-    constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
-    const int2 task = a.tasks[t];
-    const PairRec B = a.pairs[task.x];
-    const PairRec K = a.pairs[task.y];
-    int n = a.nbf;
-    long long mbase = 0;
-    if (a.shell_mol) {
-        const int m = a.shell_mol[B.sa];
-        n = a.mol_n[m];
-        mbase = a.mol_base[m];
-    }
-    if (a.screen_thr > 0.0) {
-        // density-weighted Schwarz screening and precision selection
-        const double bound = (double)B.qmax * (double)K.qmax;
-        double dm;
-        if (a.shell_mol) {
-            dm = a.mol_dmax[a.shell_mol[B.sa]];
-        } else {
-            const int ns = a.nshell;
-            dm = a.shell_dmax[B.sa * ns + B.sb];
-            dm = fmax(dm, a.shell_dmax[K.sa * ns + K.sb]);
-            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sa]);
-            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sb]);
-            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sa]);
-            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sb]);
-        }
-        const double est = bound * dm;
-        if (est < a.screen_thr) return;
-        if (est < a.prec_lo || est >= a.prec_hi) return;
-    }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.ntask) return;
+    const WriteTask task = a.tasks[t];
+    const PairRec B = a.pairs[task.bra];
+    const PairRec K = a.pairs[task.ket];
     T blk[G::NBLK];
     eri_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, blk);
+    write_block<LA, LB, LC, LD, T>(a, task, B, K, blk);
+}
+
+// Split form of the thread kernel for quartets with many primitive quartets: one warp per
+// quartet, lane l takes primitive quartets l, l + 32, ... with the thread form's
+// straight-line recursion, the warp sums the contraction accumulators (butterfly), and
+// lane 0 runs the horizontal recursion and the epilogue.
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ bool split_accumulate(const PairRec& B, const PairRec& K,
+                                                 const PrimRec<T>* prims, T* acc, int lane) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    GS_UNROLL for (int i = 0; i < G::NACC; ++i) acc[i] = T(0);
+    eri_accumulate<LA, LB, LC, LD, T>(B, K, prims, acc, lane, 32);
+    GS_UNROLL for (int i = 0; i < G::NACC; ++i)
+        GS_UNROLL for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+    return lane == 0;
+}
+
+constexpr int kSplitWarps = 4;          // warps (quartets) per block of the split form
+
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(32 * kSplitWarps) k_eri_write_split(const WriteArgs a) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kSplitWarps + (threadIdx.x >> 5);
+    if (t >= a.ntask) return;                      // warp-uniform
+    const WriteTask task = a.tasks[t];
+    const PairRec B = a.pairs[task.bra];
+    const PairRec K = a.pairs[task.ket];
+    T acc[G::NACC];
+    if (split_accumulate<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, acc, lane)) {
+        T blk[G::NBLK];
+        G::hrr(acc, T(B.ABx), T(B.ABy), T(B.ABz), T(K.ABx), T(K.ABy), T(K.ABz), blk);
+        write_block<LA, LB, LC, LD, T>(a, task, B, K, blk);
+    }
+}
+
+
+// Density-weighted screening bound of a J/K task: true when the task is to be evaluated
+// (always, without screening).
+__device__ __forceinline__ bool jk_keep(const JKArgs& a, const PairRec& B, const PairRec& K) {
+    if (a.screen_thr <= 0.0) return true;
+    const double bound = (double)B.qmax * (double)K.qmax;
+    double dm;
+    if (a.shell_mol) {
+        dm = a.mol_dmax[a.shell_mol[B.sa]];
+    } else {
+        const int ns = a.nshell;
+        dm = a.shell_dmax[B.sa * ns + B.sb];
+        dm = fmax(dm, a.shell_dmax[K.sa * ns + K.sb]);
+        dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sa]);
+        dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sb]);
+        dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sa]);
+        dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sb]);
+    }
+    const double est = bound * dm;
+    return !(est < a.screen_thr || est < a.prec_lo || est >= a.prec_hi);
+}
+
+// The J/K digestion of one evaluated block (see eri_jk_task).
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void jk_digest(const JKArgs& a, const int2 task, const PairRec& B,
+                                          const PairRec& K, const T* blk, int n,
+                                          long long mbase) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
     const double deg = (B.sa == B.sb ? 0.5 : 1.0) * (K.sa == K.sb ? 0.5 : 1.0) *
                        (task.x == task.y ? 0.5 : 1.0);
     const double* cs = a.comp_scale;
@@ -170,6 +202,60 @@ __device__ __forceinline__ void eri_jk_task(const JKArgs& a, int t) {
     }
 }
 
+// Digest the unique quartet (ab|cd) into the symmetric-accumulation matrices
+//   J'_ab += 2 v P_cd,  J'_cd += 2 v P_ab,
+//   K'_ac += v P_bd, K'_ad += v P_bc, K'_bc += v P_ad, K'_bd += v P_ac   (per density)
+// with v = (ab|cd) / ((1+d_ab)(1+d_cd)(1+d_ab,cd)), so that J = J' + J'^T and
+// K = K' + K'^T sum every permutation of every quartet once.
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void jk_target(const JKArgs& a, const PairRec& B, int& n,
+                                          long long& mbase) {
+    n = a.nbf;
+    mbase = 0;
+    if (a.shell_mol) {
+        const int m = a.shell_mol[B.sa];
+        n = a.mol_n[m];
+        mbase = a.mol_base[m];
+    }
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void eri_jk_task(const JKArgs& a, int t) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    if (!jk_keep(a, B, K)) return;           // density-weighted screening, precision band
+    int n;
+    long long mbase;
+    jk_target<LA, LB, LC, LD, T>(a, B, n, mbase);
+    T blk[G::NBLK];
+    eri_quartet<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, blk);
+    jk_digest<LA, LB, LC, LD, T>(a, task, B, K, blk, n, mbase);
+}
+
+// Split form (see k_eri_write_split): one warp per task.
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(32 * kSplitWarps) k_eri_jk_split(const JKArgs a) {
+    using G = ClassGen<LA, LB, LC, LD>;
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kSplitWarps + (threadIdx.x >> 5);
+    if (t >= a.ntask) return;                      // warp-uniform
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    if (!jk_keep(a, B, K)) return;                 // warp-uniform: one task per warp
+    T acc[G::NACC];
+    if (split_accumulate<LA, LB, LC, LD, T>(B, K, (const PrimRec<T>*)a.prims, acc, lane)) {
+        int n;
+        long long mbase;
+        jk_target<LA, LB, LC, LD, T>(a, B, n, mbase);
+        T blk[G::NBLK];
+        G::hrr(acc, T(B.ABx), T(B.ABy), T(B.ABz), T(K.ABx), T(K.ABy), T(K.ABz), blk);
+        jk_digest<LA, LB, LC, LD, T>(a, task, B, K, blk, n, mbase);
+    }
+}
+
 // One thread per task; with a task count on the device (after a partition) the grid is
 // capped and each thread strides over the tasks.
 template <int LA, int LB, int LC, int LD, typename T>
@@ -201,6 +287,28 @@ __global__ void __launch_bounds__(kBlock) k_schwarz(const SchwarzArgs a) {
         m = fmax(m, fabs((double)blk[ab * G::NA * G::NB + ab]) * s * s);
     }
     a.q[p] = sqrt(m);
+}
+
+// The split form (one warp per quartet over its primitive quartets, thread-form code).
+// Task counts on the device (partitioned lists) are not supported; those launches use the
+// thread form.
+template <int LA, int LB, int LC, int LD, int PREC>
+int launch_class_split(int kind, const void* args, cudaStream_t st) {
+    using T = typename std::conditional<PREC == 64, double, float>::type;
+    constexpr int TPB = 32 * kSplitWarps;
+    if (kind == GS_KIND_WRITE) {
+        const WriteArgs& a = *(const WriteArgs*)args;
+        if (a.ntask <= 0) return 0;
+        k_eri_write_split<LA, LB, LC, LD, T><<<(a.ntask + kSplitWarps - 1) / kSplitWarps, TPB, 0, st>>>(a);
+    } else if (kind == GS_KIND_JK) {
+        const JKArgs& a = *(const JKArgs*)args;
+        if (a.ntask <= 0) return 0;
+        if (a.ntask_dev) return GS_ERR_ARG;
+        k_eri_jk_split<LA, LB, LC, LD, T><<<(a.ntask + kSplitWarps - 1) / kSplitWarps, TPB, 0, st>>>(a);
+    } else {
+        return GS_ERR_ARG;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 
 template <int LA, int LB, int LC, int LD, int PREC>

@@ -29,12 +29,25 @@ PRIM_SCREEN = 55.262
 WRITE_TASK_DTYPE = np.dtype([("bra", "<i4"), ("ket", "<i4"), ("code", "<i4"), ("pad", "<i4"),
                              ("off", "<i8")])
 
-# Quartets with at least this many primitive quartets (after the pair screen) run in the
-# warp form even when their class runs one thread per quartet: a warp then sets up 32 of
-# one quartet's primitive quartets at once instead of one thread walking them all, which
-# would make the launch end on a few long-running warps.
+# Quartets with many primitive quartets (after the pair screen) of a class that runs one
+# thread per quartet run in the split form instead: one warp per quartet, its lanes taking
+# the primitive quartets 32 at a time with the same straight-line code, then summing their
+# contraction accumulators.  One thread walking them all would make the launch end on a
+# few long-running warps.  "Many" is at least HEAVY_PRIM_QUARTETS and twice the class's
+# accumulator count (the warp's final sum costs five additions per accumulator).
 HEAVY_PRIM_QUARTETS = 32
-THREAD_FORM, WARP_FORM, GROUPED_FORM = 1, 2, 3
+THREAD_FORM, WARP_FORM, GROUPED_FORM, SPLIT_FORM = 1, 2, 3, 4
+# (class, precision) pairs whose heavy quartets stay on the thread form (set by the
+# autotuner where that measured faster)
+SPLIT_OFF = set()
+
+
+def heavy_threshold(cls):
+    """Primitive quartets from which a quartet of class ``cls`` is run in the split form."""
+    la, lb, lc, ld = cls
+    ne = sum(int(NCART[x]) for x in range(la, la + lb + 1))
+    nf = sum(int(NCART[x]) for x in range(lc, lc + ld + 1))
+    return max(HEAVY_PRIM_QUARTETS, 2 * ne * nf)
 
 _pc_lut = np.full((3, 3), -1, dtype=np.int64)
 for _i, (_a, _b) in enumerate(PAIR_ORDER):
@@ -43,15 +56,14 @@ for _i, (_a, _b) in enumerate(PAIR_ORDER):
 
 def split_forms(cls, precision, heavy):
     """[(form, first, count)] for a class segment whose tasks are sorted by descending
-    primitive-quartet count, ``heavy`` of them at or above HEAVY_PRIM_QUARTETS: the heavy
-    prefix in the class's warp form when the class otherwise runs one thread per quartet.
-    form 0 = the class's configured form."""
+    primitive-quartet count, ``heavy`` of them at or above heavy_threshold(cls): the heavy
+    prefix in the split form when the class otherwise runs one thread per quartet.
+    form 0 = the class's configured form; count None = to the end of the segment."""
     L = _lib.lib()
-    if heavy <= 0 or L.gs_class_form(*cls, precision) != THREAD_FORM:
+    if heavy <= 0 or (cls, precision) in SPLIT_OFF or \
+            L.gs_class_form(*cls, precision) != THREAD_FORM:
         return [(0, 0, None)]
-    built = L.gs_class_variants(*cls, precision)
-    warp = GROUPED_FORM if built & 4 else WARP_FORM
-    return [(warp, 0, heavy), (THREAD_FORM, heavy, None)]
+    return [(SPLIT_FORM, 0, heavy), (THREAD_FORM, heavy, None)]
 
 
 def _check_sizes():
@@ -233,8 +245,8 @@ class QuartetBatch:
         self.sorted_bra_nprim = nb[order]
         self.sorted_ket_nprim = nk[order]
         work = self.sorted_bra_nprim * self.sorted_ket_nprim
-        self.heavy = [int(np.count_nonzero(work[s:e] >= HEAVY_PRIM_QUARTETS))
-                      for _, s, e in self.segments]
+        self.heavy = [int(np.count_nonzero(work[s:e] >= heavy_threshold(cls)))
+                      for cls, s, e in self.segments]
 
     def class_counts(self):
         return {cls: e - s for cls, s, e in self.segments}
@@ -348,7 +360,7 @@ class JKEngine:
                 t = torch.stack([bra[o], ket[o]], dim=1).to(torch.int32)
                 (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
                 self.segments.append(((la, lb, lc, ld), ntot, ntot + total))
-                self.heavy.append(int((key >= HEAVY_PRIM_QUARTETS * 4096).sum()))
+                self.heavy.append(int((key >= heavy_threshold((la, lb, lc, ld)) * 4096).sum()))
                 chunks.append(t)
                 ntot += total
         self.tasks = torch.cat(chunks, 0).contiguous() if chunks else \

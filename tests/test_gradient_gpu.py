@@ -133,3 +133,41 @@ def test_gradient_parts_against_fixed_density_differences(gpu_lib, basis):
         fd1, fd2 = (p1 - m1) / (2 * h), (p2 - m2) / (2 * h)
         assert abs(g1[a, x] - fd1) < 1e-6, ("one-electron", a, x, g1[a, x], fd1)
         assert abs(g2[a, x] - fd2) < 1e-6, ("two-electron", a, x, g2[a, x], fd2)
+
+
+def test_eri_gradient_per_class_against_differences(gpu_lib):
+    """Water / 6-31G*: the fused ERI adjoint of every angular-momentum class on its own
+    against central differences of that class's two-electron energy
+    1/2 sum P (J[P] - K[P]/2) at fixed density (the same quartet list at every geometry)."""
+    import torch
+    from gaussium_gb300 import gradient, molecules
+    from gaussium_gb300.engine import JKEngine
+    from gaussium_gb300.molecules import Molecule
+    base = molecules.water_cluster(1, seed=3)
+    coords = base.coords.copy()
+    coords[1] += np.array([0.05, -0.03, 0.02])
+    mol = Molecule(["O", "H", "H"], coords)
+    st = gradient.rhf_state(mol, "6-31G*")
+    P = st.P
+    sb = st.sb
+    eng = JKEngine(sb, schwarz_thr=0.0)
+    sa = gradient.shell_atoms(mol, sb)
+    pt = torch.tensor(P, device="cuda")
+
+    def e2(xyz, cls):
+        m = Molecule(["O", "H", "H"], xyz)
+        e = JKEngine(molecules.shell_basis(m, "6-31G*"), schwarz_thr=0.0)
+        J, (K,) = e.jk(pt, [pt], classes=[cls])
+        return 0.5 * float(torch.sum(pt * (J - 0.5 * K)))
+
+    h, bad = 1e-4, []
+    for cls, _, _ in eng.segments:
+        g = gradient.eri_gradient(sb, eng, sa, P, 3, classes=[cls])
+        for a, x in ((0, 0), (1, 1), (2, 2)):
+            xp, xm = coords.copy(), coords.copy()
+            xp[a, x] += h
+            xm[a, x] -= h
+            fd = (e2(xp, cls) - e2(xm, cls)) / (2 * h)
+            if abs(g[a, x] - fd) > 1e-7:
+                bad.append((cls, a, x, float(g[a, x]), fd))
+    assert not bad, bad
