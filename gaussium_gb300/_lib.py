@@ -19,7 +19,7 @@ _SIGS = {
     "gs_status_string": (ctypes.c_char_p, [I]),
     "gs_record_sizes": (I, [P]),
     "gs_class_available": (I, [I, I, I, I]),
-    "gs_pairs_build": (I, [P, P, P, P, P, I, P, P, P, P, P, D, P, P]),
+    "gs_pairs_build": (I, [P, P, P, P, P, I, P, P, P, P, P, D, P, I, P, P]),
     "gs_schwarz": (I, [I, I, P, P, P, I, P, P, I, P]),
     "gs_eri_blocks": (I, [I, I, I, I, I, P, P, P, I, P, P, P]),
     "gs_fock_jk": (I, [I, I, I, I, I, P, P, P, P, I, I, I, P, P, P, I, P, P, P, D, D, D, P]),

@@ -62,15 +62,12 @@ int check_launch() { return cudaGetLastError() == cudaSuccess ? GS_OK : GS_ERR_C
 // K0: one warp per shell pair.  Lane k takes primitive pair k (k = i nb + j, then k + 32),
 // a ballot ranks the kept ones so that they are written contiguously in the same order as
 // the host form (make_pair), and consecutive lanes write consecutive records.
-__global__ void __launch_bounds__(256) k_pairs_build(gs::ShellView sv, int npairs,
-                                                     const int* __restrict__ pair_shells,
-                                                     const int* __restrict__ pair_prim_off,
-                                                     gs::PairRec* pairs, gs::PrimRec<double>* p64,
-                                                     gs::PrimRec<float>* p32, double max_exp,
-                                                     int* __restrict__ kept) {
-    const int lane = threadIdx.x & 31;
-    const long long pi = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (pi >= npairs) return;
+__device__ __forceinline__ void build_pair(const gs::ShellView& sv, long long pi,
+                                           const int* __restrict__ pair_shells,
+                                           const int* __restrict__ pair_prim_off,
+                                           gs::PairRec* pairs, gs::PrimRec<double>* p64,
+                                           gs::PrimRec<float>* p32, double max_exp,
+                                           int* __restrict__ kept, int lane) {
     const int sa = pair_shells[2 * pi], sb = pair_shells[2 * pi + 1];
     const double* A = sv.centre + 3 * sa;
     const double* B = sv.centre + 3 * sb;
@@ -111,6 +108,96 @@ __global__ void __launch_bounds__(256) k_pairs_build(gs::ShellView sv, int npair
         pr.qmax = 0.0f; pr.pad = 0;
         pairs[pi] = pr;
         if (kept) kept[pi] = n;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pairs_build(gs::ShellView sv, int npairs,
+                                                     const int* __restrict__ pair_shells,
+                                                     const int* __restrict__ pair_prim_off,
+                                                     gs::PairRec* pairs, gs::PrimRec<double>* p64,
+                                                     gs::PrimRec<float>* p32, double max_exp,
+                                                     int* __restrict__ kept) {
+    const int lane = threadIdx.x & 31;
+    const long long pi = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (pi >= npairs) return;
+    build_pair(sv, pi, pair_shells, pair_prim_off, pairs, p64, p32, max_exp, kept, lane);
+}
+
+// K0, packed form: warp g builds the shell pairs [group_start[g], group_start[g+1]) whose
+// primitive pairs fit one warp together (a group of one pair may have more; it runs the
+// one-pair loop).  Lane l takes primitive pair k of the pair whose lanes contain l, so the
+// FP64 work of small pairs (a K = 1-6 basis has 12 primitive pairs per shell pair on
+// average) is not issued with most lanes idle.  Records and counts as k_pairs_build.
+__global__ void __launch_bounds__(256) k_pairs_build_packed(
+    gs::ShellView sv, int ngroups, const int* __restrict__ group_start,
+    const int* __restrict__ pair_shells, const int* __restrict__ pair_prim_off,
+    gs::PairRec* pairs, gs::PrimRec<double>* p64, gs::PrimRec<float>* p32, double max_exp,
+    int* __restrict__ kept) {
+    const int lane = threadIdx.x & 31;
+    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= ngroups) return;
+    const int first = group_start[g], np = group_start[g + 1] - first;
+    if (np == 1) {                                    // one pair (possibly > 32 primitive pairs)
+        build_pair(sv, first, pair_shells, pair_prim_off, pairs, p64, p32, max_exp, kept, lane);
+        return;
+    }
+    // this lane's pair (lanes [off_j, off_j + size_j) belong to pair j of the group)
+    int size = 0;
+    if (lane < np) {
+        const int sa = pair_shells[2 * (first + lane)], sb = pair_shells[2 * (first + lane) + 1];
+        size = (sv.prim_off[sa + 1] - sv.prim_off[sa]) * (sv.prim_off[sb + 1] - sv.prim_off[sb]);
+    }
+    int off = size;                                   // inclusive scan of the pair sizes
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, off, o);
+        if (lane >= o) off += y;
+    }
+    off -= size;                                      // exclusive: first lane of pair j
+    const int total = __shfl_sync(0xffffffffu, off + size, 31);
+    int j = 0;
+    for (int q = 1; q < np; ++q)
+        if (__shfl_sync(0xffffffffu, off, q) <= lane) j = q;
+    const int my_off = __shfl_sync(0xffffffffu, off, j);
+    const int my_size = __shfl_sync(0xffffffffu, size, j);
+    const int pi = first + j;
+    const bool in = lane < total;
+    const int sa = pair_shells[2 * pi], sb = pair_shells[2 * pi + 1];
+    const double* A = sv.centre + 3 * sa;
+    const double* B = sv.centre + 3 * sb;
+    const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
+    const double ab2 = ABx * ABx + ABy * ABy + ABz * ABz;
+    const int a0 = sv.prim_off[sa], b0 = sv.prim_off[sb];
+    const int nb = sv.prim_off[sb + 1] - b0;
+    const int k = lane - my_off;
+    bool keep = false;
+    double a = 0.0, b = 0.0;
+    int i = 0, jj = 0;
+    if (in) {
+        i = a0 + k / nb;
+        jj = b0 + k % nb;
+        a = sv.expo[i];
+        b = sv.expo[jj];
+        keep = gs::prim_pair_kept(a, b, ab2, max_exp);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const unsigned pair_mask = (my_size >= 32 ? 0xffffffffu : ((1u << my_size) - 1u)) << my_off;
+    const unsigned mine = m & pair_mask;
+    const int base = pair_prim_off[pi];
+    if (keep) {
+        const int r = base + __popc(mine & ((1u << lane) - 1u));
+        const gs::PrimRec<double> rec = gs::prim_pair(A, B, a, b, ab2, sv.coef[i], sv.coef[jj]);
+        p64[r] = rec;
+        if (p32) p32[r] = gs::prim_pair32(rec);
+    }
+    if (in && lane == my_off) {
+        gs::PairRec pr;
+        pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
+        pr.prim_off = base;
+        pr.nprim = __popc(mine);
+        pr.sa = sa; pr.sb = sb;
+        pr.qmax = 0.0f; pr.pad = 0;
+        pairs[pi] = pr;
+        if (kept) kept[pi] = pr.nprim;
     }
 }
 
@@ -269,11 +356,19 @@ int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int vari
 int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
                    const double* coef, int npairs, const int* pair_shells,
                    const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
-                   double max_exp, int* kept, void* stream) {
-    if (npairs < 0 || !centre || !l || !prim_off || !expo || !coef || !pair_rec || !prim64)
+                   double max_exp, int* kept, int ngroups, const int* group_start,
+                   void* stream) {
+    if (npairs < 0 || !centre || !l || !prim_off || !expo || !coef || !pair_rec || !prim64 ||
+        ngroups < 0 || (ngroups > 0 && !group_start))
         return GS_ERR_ARG;
     if (npairs == 0) return GS_OK;
     gs::ShellView sv{centre, l, prim_off, expo, coef};
+    if (ngroups > 0) {
+        k_pairs_build_packed<<<(unsigned)(((long long)ngroups * 32 + 255) / 256), 256, 0, S(stream)>>>(
+            sv, ngroups, group_start, pair_shells, pair_prim_off, (gs::PairRec*)pair_rec,
+            (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32, max_exp, kept);
+        return check_launch();
+    }
     k_pairs_build<<<(unsigned)(((long long)npairs * 32 + 255) / 256), 256, 0, S(stream)>>>(
         sv, npairs, pair_shells, pair_prim_off, (gs::PairRec*)pair_rec,
         (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32, max_exp, kept);

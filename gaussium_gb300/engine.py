@@ -117,6 +117,26 @@ class DeviceShells:
         self.nbf = sb.nbf
 
 
+def pair_groups(sizes, lanes=32):
+    """Start indices (and the end) of groups of consecutive shell pairs whose primitive
+    pairs total at most ``lanes``: aligned runs of four pairs when they fit, else of two,
+    else single pairs (vectorised; a pair with more primitive pairs is a group of its own)."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    n = len(sizes)
+    if n == 0:
+        return np.zeros(1, dtype=np.int32)
+    m = -(-n // 4) * 4
+    sz = np.zeros(m, dtype=np.int64)
+    sz[:n] = sizes
+    quad = sz.reshape(-1, 4).sum(1) <= lanes
+    half = sz.reshape(-1, 2).sum(1) <= lanes
+    i = np.arange(m)
+    q, r = i // 4, i % 4
+    start = (r == 0) | ((r == 2) & ~quad[q]) | (((r == 1) | (r == 3)) & ~quad[q] & ~half[i // 2])
+    out = np.flatnonzero(start[:n]).astype(np.int32)
+    return np.concatenate([out, np.array([n], dtype=np.int32)])
+
+
 def check_shell_indices(idx, nshell, what):
     """Shell indices handed to the kernels must lie in [0, nshell): a kernel trusts them."""
     idx = np.asarray(idx)
@@ -153,6 +173,9 @@ class PairSet:
         self.p32 = torch.empty(total * PRIM32, dtype=torch.uint8, device=dev) if want32 else None
         self.nprim_pairs = int(off[-1])
         self.max_exp = max_exp
+        # consecutive pairs packed into warps of at most 32 primitive pairs (the pair build)
+        self.groups = torch.as_tensor(pair_groups(npp)).to(dev)
+        self.ngroups = int(self.groups.numel()) - 1
         self.kept = torch.zeros(max(1, self.n), dtype=torch.int32, device=dev)
         self.build(stream)
         # primitive pairs kept per shell pair (the work per pair after screening)
@@ -168,8 +191,8 @@ class PairSet:
                                     _lib.ptr(ds.expo), _lib.ptr(ds.coef), self.n,
                                     _lib.ptr(self.shells), _lib.ptr(self.prim_start),
                                     _lib.ptr(self.rec), _lib.ptr(self.p64), _lib.ptr(p32),
-                                    float(self.max_exp), _lib.ptr(self.kept),
-                                    _lib.stream(stream)), "gs_pairs_build")
+                                    float(self.max_exp), _lib.ptr(self.kept), self.ngroups,
+                                    _lib.ptr(self.groups), _lib.stream(stream)), "gs_pairs_build")
 
     def prims(self, precision):
         return self.p64 if precision == 64 else self.p32

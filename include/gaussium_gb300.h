@@ -82,11 +82,15 @@ int gs_class_form(int la, int lb, int lc, int ld, int precision);
  * pair_prim_off[npairs] (first primitive-pair record of each pair, Ka*Kb reserved).
  * Outputs: pair_rec[npairs], prim64, prim32 (may be NULL), kept[npairs] (may be NULL:
  * primitive pairs kept).  max_exp > 0 drops primitive pairs with
- * alpha*beta/(alpha+beta)*|AB|^2 > max_exp (0 keeps all, as the reference does). */
+ * alpha*beta/(alpha+beta)*|AB|^2 > max_exp (0 keeps all, as the reference does).
+ * group_start[ngroups+1] (device; ngroups 0 = one warp per pair) packs consecutive pairs
+ * into groups whose primitive pairs (Ka*Kb each) total at most 32, or single pairs:
+ * one warp per group keeps its lanes busy on small pairs. */
 int gs_pairs_build(const double* centre, const int* l, const int* prim_off, const double* expo,
                    const double* coef, int npairs, const int* pair_shells,
                    const int* pair_prim_off, void* pair_rec, void* prim64, void* prim32,
-                   double max_exp, int* kept, void* stream);
+                   double max_exp, int* kept, int ngroups, const int* group_start,
+                   void* stream);
 
 /* K1 Schwarz bounds q[p] = sqrt(max |(ab|ab)|) for the npair pairs pair_index[] of class
  * (la lb), in FP64; then copies all npairs_total bounds into pair_rec[].qmax.  No

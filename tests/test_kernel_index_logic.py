@@ -141,3 +141,52 @@ def test_symmetry_kernel_element_decomposition():
     zero = zero.reshape((n,) * 4)
     keys = oracle.canonical_keys(g["o2_table"].shape[0])
     assert np.array_equal(~zero[keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3]], g["o2_nonzero"])
+
+
+def test_packed_pair_build_lane_mapping():
+    """k_pairs_build_packed restated lane by lane: every primitive pair of every shell pair
+    is taken by exactly one lane, and the kept ones land at the same record slots, in the
+    same order, as the one-pair-per-warp form (rank among the pair's kept lanes)."""
+    from gaussium_gb300.engine import pair_groups
+    rng = np.random.default_rng(5)
+    ka = rng.integers(1, 7, 400)
+    kb = rng.integers(1, 7, 400)
+    sizes = ka * kb
+    groups = pair_groups(sizes)
+    keep = rng.random(int(sizes.sum())) < 0.4
+    first_rec = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    got = {}
+    for g in range(len(groups) - 1):
+        first, np_ = groups[g], groups[g + 1] - groups[g]
+        if np_ == 1:
+            continue                         # one-pair groups run the one-pair loop
+        size = np.zeros(32, dtype=int)
+        size[:np_] = sizes[first:first + np_]
+        off = np.cumsum(size) - size         # exclusive scan
+        total = off[31] + size[31]
+        assert total <= 32
+        ballot = 0
+        lanes = []
+        for lane in range(32):
+            j = max([q for q in range(np_) if off[q] <= lane] or [0])
+            if lane < total:
+                k = lane - off[j]
+                assert 0 <= k < size[j]
+                kp = keep[first_rec[first + j] + k]
+                if kp:
+                    ballot |= 1 << lane
+                lanes.append((lane, j, k, kp))
+        for lane, j, k, kp in lanes:
+            mask = ((1 << int(size[j])) - 1) << int(off[j])
+            if kp:
+                rank = bin(ballot & mask & ((1 << lane) - 1)).count("1")
+                got[(first + j, rank)] = k
+    # the one-pair-per-warp form: kept primitive pairs in increasing k
+    for p in range(len(sizes)):
+        g = np.searchsorted(groups, p, side="right") - 1
+        if groups[g + 1] - groups[g] == 1:
+            continue
+        ks = np.flatnonzero(keep[first_rec[p]:first_rec[p] + sizes[p]])
+        for rank, k in enumerate(ks):
+            assert got.pop((p, rank)) == k
+    assert not got
