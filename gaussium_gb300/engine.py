@@ -45,8 +45,8 @@ SPLIT_OFF = set()
 def heavy_threshold(cls):
     """Primitive quartets from which a quartet of class ``cls`` is run in the split form."""
     la, lb, lc, ld = cls
-    ne = sum(int(NCART[x]) for x in range(la, la + lb + 1))
-    nf = sum(int(NCART[x]) for x in range(lc, lc + ld + 1))
+    ne = sum((x + 1) * (x + 2) // 2 for x in range(la, la + lb + 1))
+    nf = sum((x + 1) * (x + 2) // 2 for x in range(lc, lc + ld + 1))
     return max(HEAVY_PRIM_QUARTETS, 2 * ne * nf)
 
 _pc_lut = np.full((3, 3), -1, dtype=np.int64)

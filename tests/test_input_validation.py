@@ -99,3 +99,25 @@ def test_device_comparison_is_exact(monkeypatch):
     with pytest.raises(_lib.GsError):
         engine._check_device_tensor(FakeCuda(), "cuda", "density matrix")
     engine._check_device_tensor(FakeCuda(), "cuda:1", "density matrix")
+
+
+def test_quartet_batch_host_planning(monkeypatch):
+    """QuartetBatch's host planning without a device (the pair records stubbed): class
+    segments in canonical order, tasks sorted by descending primitive work inside each,
+    and the heavy prefix counted with every class's threshold."""
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(3000, seed=2)
+
+    class StubPairs:
+        def __init__(self, ds, pairs, want32=True, max_exp=0.0):
+            self.nprim = (sb.nprim[pairs[:, 0]].astype(np.int64) * sb.nprim[pairs[:, 1]])
+
+    monkeypatch.setattr(engine, "PairSet", StubPairs)
+    monkeypatch.setattr(engine.torch.Tensor, "to", lambda self, dev: self)
+    b = engine.QuartetBatch(_host_only(sb), q)
+    assert [s for _, s, _ in b.segments] == sorted(s for _, s, _ in b.segments)
+    work = b.sorted_bra_nprim * b.sorted_ket_nprim
+    for (cls, s, e), heavy in zip(b.segments, b.heavy):
+        assert np.all(np.diff(work[s:e]) <= 0)
+        assert heavy == np.count_nonzero(work[s:e] >= engine.heavy_threshold(cls))
+        assert np.all(work[s:s + heavy] >= engine.heavy_threshold(cls))

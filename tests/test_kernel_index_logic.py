@@ -190,3 +190,18 @@ def test_packed_pair_build_lane_mapping():
         for rank, k in enumerate(ks):
             assert got.pop((p, rank)) == k
     assert not got
+
+
+def test_heavy_threshold_every_class():
+    """The split-form threshold is defined for every built class: at least 32 primitive
+    quartets and twice the class's contraction accumulators (its generated NACC)."""
+    import os
+    import sys
+    from gaussium_gb300 import engine
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                    "gaussium_gb300", "csrc"))
+    import gen_eri
+    for cls in gen_eri.canonical_classes(2):
+        v = gen_eri.VrrGen(cls)
+        nacc = len(v.e_targets) * len(v.f_targets)
+        assert engine.heavy_threshold(cls) == max(engine.HEAVY_PRIM_QUARTETS, 2 * nacc)
