@@ -231,10 +231,13 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
         const double gam = w * (0.5 * Pm[pa * nbf + pb] * Pm[pc * nbf + pd] -
                                 0.125 * (Pm[pa * nbf + pc] * Pm[pb * nbf + pd] +
                                          Pm[pa * nbf + pd] * Pm[pb * nbf + pc]));
+        // the HRR blocks are unscaled: the element carries the component scales of all four
+        // functions (not 1 for the xy, xz, yz components of a d shell)
+        const double s = gam * a.comp_scale[6 * sh[0] + idx[0]] * a.comp_scale[6 * sh[1] + idx[1]] *
+                         a.comp_scale[6 * sh[2] + idx[2]] * a.comp_scale[6 * sh[3] + idx[3]];
         for (int cen = 0; cen < 3; ++cen) {
             int ex[3];
             g_comp(ls[cen], idx[cen], ex[0], ex[1], ex[2]);
-            const double s = gam * a.comp_scale[6 * sh[cen] + idx[cen]];
             for (int x = 0; x < 3; ++x) {
                 int up[3] = {ex[0], ex[1], ex[2]};
                 up[x] += 1;
@@ -334,13 +337,15 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
         for (int i = 0; i < NC; ++i)
 #pragma unroll
             for (int j = 0; j < ND; ++j) pcd[i * ND + j] = Pm[(fc + i) * nbf + fd + j];
-        double cs0[NA], cs1[NB], cs2[NC];
+        double cs0[NA], cs1[NB], cs2[NC], cs3[ND];
 #pragma unroll
         for (int i = 0; i < NA; ++i) cs0[i] = a.comp_scale[6 * B.sa + i];
 #pragma unroll
         for (int i = 0; i < NB; ++i) cs1[i] = a.comp_scale[6 * B.sb + i];
 #pragma unroll
         for (int i = 0; i < NC; ++i) cs2[i] = a.comp_scale[6 * K.sa + i];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) cs3[i] = a.comp_scale[6 * K.sb + i];
         double w = 8.0;
         if (B.sa == B.sb) w *= 0.5;
         if (K.sa == K.sb) w *= 0.5;
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
         double g[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) g[k] = 0.0;
-        W::contract(H, w, pab, pcd, pac, pbd, pad, pbc, cs0, cs1, cs2, g);
+        W::contract(H, w, pab, pcd, pac, pbd, pad, pbc, cs0, cs1, cs2, cs3, g);
         const int at[4] = {a.shell_atom[B.sa], a.shell_atom[B.sb], a.shell_atom[K.sa],
                            a.shell_atom[K.sb]};
         double* dst = shared_sum ? sg : a.grad;

@@ -293,9 +293,10 @@ def emit_grad_thread(cls, p=None):
                     con.append(f"    gam = w * (0.5 * pab[{ia * n[1] + ib}] * pcd[{ic * n[3] + idd}] - "
                                f"0.125 * (pac[{ia * n[2] + ic}] * pbd[{ib * n[3] + idd}] + "
                                f"pad[{ia * n[3] + idd}] * pbc[{ib * n[2] + ic}]));")
+                    # unscaled HRR blocks: the element carries all four component scales
+                    con.append(f"    s = gam * cs0[{ia}] * cs1[{ib}] * cs2[{ic}] * cs3[{idd}];")
                     for cen in range(3):
                         ex = cart(ls[cen])[idx[cen]]
-                        con.append(f"    s = gam * cs{cen}[{idx[cen]}];")
                         for x in range(3):
                             up = list(ex)
                             up[x] += 1
@@ -327,7 +328,8 @@ def emit_grad_thread(cls, p=None):
              *hrr, "  }",
              "  static __device__ __forceinline__ void contract(const double* H, double w, const double* pab,",
              "      const double* pcd, const double* pac, const double* pbd, const double* pad,",
-             "      const double* pbc, const double* cs0, const double* cs1, const double* cs2, double* g) {",
+             "      const double* pbc, const double* cs0, const double* cs1, const double* cs2,",
+             "      const double* cs3, double* g) {",
              "    double gam, s;", *con, "  }", "};", "}  // namespace gs", ""]
     return "\n".join(lines)
 

@@ -200,9 +200,10 @@ def test_thread_gradient_code_matches_program(cls):
     nc = [gen_eri.ncart(x) for x in cls]
     dens = {k: rng.standard_normal(nc[a] * nc[b]) for k, (a, b) in
             {"pab": (0, 1), "pcd": (2, 3), "pac": (0, 2), "pbd": (1, 3), "pad": (0, 3), "pbc": (1, 2)}.items()}
-    cs = [rng.uniform(0.5, 2.0, nc[k]) for k in range(3)]
+    cs = [rng.uniform(0.5, 2.0, nc[k]) for k in range(4)]
     g = np.zeros(9)
-    exec(contract, {"fma": _fma, "H": H, "w": 0.5, **dens, "cs0": cs[0], "cs1": cs[1], "cs2": cs[2], "g": g})
+    exec(contract, {"fma": _fma, "H": H, "w": 0.5, **dens, "cs0": cs[0], "cs1": cs[1], "cs2": cs[2],
+                    "cs3": cs[3], "g": g})
     ref = np.zeros(9)
     for ia in range(nc[0]):
         for ib in range(nc[1]):
@@ -224,5 +225,6 @@ def test_thread_gradient_code_matches_program(cls):
                                 jj = list(idx); mm = list(nc)
                                 jj[cen] = gen_eri.cart(cls[cen] - 1).index(tuple(dn)); mm[cen] = gen_eri.ncart(cls[cen] - 1)
                                 v -= ex[x] * outs[3 + cen][((jj[0] * mm[1] + jj[1]) * mm[2] + jj[2]) * mm[3] + jj[3]]
-                            ref[3 * cen + x] += gam * cs[cen][idx[cen]] * v
+                            scale = cs[0][ia] * cs[1][ib] * cs[2][ic] * cs[3][idd]
+                            ref[3 * cen + x] += gam * scale * v
     assert np.max(np.abs(g - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref)))
