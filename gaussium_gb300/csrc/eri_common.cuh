@@ -139,24 +139,58 @@ GS_HD GS_INLINE void boys_small(double t, double pref, double* __restrict__ F) {
     }
 }
 
-// F[m] = pref * F_m(t), m = 0..M.  Below BOYS_TMAX (80): boys_small in FP64 for either T
-// (in FP32 quartets the FP64 values are rounded to float once, so neither the series nor
-// the downward recursion accumulates FP32 rounding).  Above it: F_0 = sqrt(pi/t)/2
-// (erf(sqrt t) = 1 to 1e-36) and the upward recursion F_{m+1} = (2m+1) F_m / (2t), whose
-// dropped exp(-t) term changes F_m (m <= 10) by less than 1e-23 relative at t >= 80.  The
-// wide table keeps the large-T branch free of an exponential: lanes of one warp that take
-// different branches cost the sum of both.
+// Boys function below the asymptotic threshold for an FP32 quartet: the same grid, the
+// Taylor expansion cut after the d^4 term (its remainder, at most d^5/5! < 3e-10 of F_M
+// for |d| <= 1/32, is far below FP32 rounding) and the downward recursion, all in FP64;
+// each F_m is rounded to float once and then scaled by pref in float.  t - t_k is exact in
+// float (both are multiples of t's ulp and |t - t_k| <= 1/32).
+template <int M>
+GS_HD GS_INLINE void boys_small32(float t, float pref, float* __restrict__ F) {
+    static_assert(M + 4 <= BOYS_NCOL - 2, "Taylor terms beyond the tabulated orders");
+    const int k = (int)(t * float(BOYS_INV_H) + 0.5f);
+    const double d = (double)((float)k * (1.0f / BOYS_INV_H) - t);
+    const double* row = boys_table() + k * BOYS_NCOL;
+    const double d2 = d * (1.0 / 2), d3 = d * (1.0 / 3), d4 = d * (1.0 / 4);
+    double Fd[M + 1];
+    double f = ldg(row + M + 4);
+    f = f * d4 + ldg(row + M + 3);
+    f = f * d3 + ldg(row + M + 2);
+    f = f * d2 + ldg(row + M + 1);
+    Fd[M] = f * d + ldg(row + M);
+    if (M > 0) {
+        double e = d4 + 1.0;
+        e = e * d3 + 1.0;
+        e = e * d2 + 1.0;
+        e = e * d + 1.0;
+        const double et = e * ldg(row + BOYS_NCOL - 1);
+        const double t2 = 2.0 * (double)t;
+        GS_UNROLL for (int m = M; m >= 1; --m) Fd[m - 1] = (t2 * Fd[m] + et) * (1.0 / (2 * m - 1));
+    }
+    GS_UNROLL for (int m = 0; m <= M; ++m) F[m] = (float)Fd[m] * pref;
+}
+
+// Start of the asymptotic branch for orders 0..M: the smallest T (rounded up) at which
+// F_m(T) ~ (2m-1)!! / (2T)^m * sqrt(pi/T) / 2 is within 2^-54 (FP64) or 2^-26 (FP32) of
+// F_m for every m <= M.  Its relative error is the regularised upper incomplete gamma
+// function Q(m + 1/2, T), which grows with m, so the threshold depends on M only.
+constexpr double kBoysAsym64[17] = {36, 40, 43, 46, 49, 52, 54, 57, 59, 61, 64, 66, 68, 70, 72, 74, 76};
+constexpr float kBoysAsym32[17] = {17, 20, 23, 25, 28, 30, 32, 34, 36, 38, 40, 42, 43, 45, 47, 48, 50};
+
+// F[m] = pref * F_m(t), m = 0..M.  Below the threshold: the grid expansion and the
+// downward recursion in FP64 (boys_small, or boys_small32 for an FP32 quartet, which
+// rounds the FP64 values to float once).  Above it: F_0 = sqrt(pi/t)/2 and the upward
+// recursion F_{m+1} = (2m+1) F_m / (2t) in the quartet's precision, exact to its rounding
+// there.  Neither branch needs an exponential: lanes of one warp that take different
+// branches cost the sum of both.
 template <int M, typename T>
 GS_HD GS_INLINE void boys(T t, T pref, T* __restrict__ F) {
+    static_assert(M <= 16, "Boys orders beyond the table");
     constexpr bool dbl = sizeof(T) == 8;
-    if (t < T(BOYS_TMAX)) {
-        if constexpr (dbl) {
-            boys_small<M>(t, pref, F);
-        } else {
-            double Fd[M + 1];
-            boys_small<M>((double)t, (double)pref, Fd);
-            GS_UNROLL for (int m = 0; m <= M; ++m) F[m] = (T)Fd[m];
-        }
+    constexpr T thr = dbl ? T(kBoysAsym64[M]) : T(kBoysAsym32[M]);
+    static_assert(thr <= T(BOYS_TMAX), "asymptotic threshold beyond the grid");
+    if (t < thr) {
+        if constexpr (dbl) boys_small<M>(t, pref, F);
+        else boys_small32<M>(t, pref, F);
     } else {
         const T rs = gs_rsqrt(t);
         F[0] = pref * T(0.88622692545275801365) * rs;   // sqrt(pi)/2

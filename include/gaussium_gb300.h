@@ -240,13 +240,15 @@ int gs_eri_grad_contract(int nq, const int* quartets, const long long* block_off
                          const double* comp_scale, const int* shell_atom, int nbf,
                          const double* density, double* grad, void* stream);
 
-/* K6 fused ERI adjoint for s/p classes (la lb | lc ld) (l <= 1): for the ntask unique
- * quartets tasks[2*t] = (bra pair, ket pair) it evaluates the derivative integrals of
- * centres A, B, C in one pass (VRR per primitive quartet into four weighted contraction
- * sets 1, 2 alpha, 2 beta, 2 gamma; six HRR blocks in shared memory), contracts them with
- * the same RHF weights as gs_eri_grad_contract and adds dE/dR to grad[natom*3] through
- * shell_atom[] (every entry in [0, natom)).  prim64 records must carry the first shell's exponent in their pad field
- * (gs_pairs_build writes it).  No reference counterpart (see gs_eri_grad_contract). */
+/* K6 fused ERI adjoint for the s/p/d classes (la lb | lc ld) (l <= 2, la >= lb, lc >= ld,
+ * (la,lb) >= (lc,ld)): for the ntask unique quartets tasks[2*t] = (bra pair, ket pair) it
+ * evaluates the derivative integrals of centres A, B, C in one pass (VRR per primitive
+ * quartet into four weighted contraction sets 1, 2 alpha, 2 beta, 2 gamma, up to l + 1 on
+ * the differentiated centre; six HRR blocks in shared memory), contracts them, times the
+ * component scales of all four functions, with the same RHF weights as
+ * gs_eri_grad_contract and adds dE/dR to grad[natom*3] through shell_atom[] (every entry
+ * in [0, natom)).  prim64 records must carry the first shell's exponent in their pad
+ * field (gs_pairs_build writes it).  No reference counterpart (see gs_eri_grad_contract). */
 int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
                 const double* comp_scale, const int* func_off, const int* shell_atom, int ntask,
                 const int* tasks, int nbf, int natom, const double* density, double* grad,

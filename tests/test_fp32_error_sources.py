@@ -1,10 +1,10 @@
 """Where the FP32 quartets' error comes from, on the CPU build of the generated recursions.
 
-The FP32 path evaluates the Boys function below BOYS_TMAX (series and downward recursion)
-in FP64 and every other stage in FP32.  Over a seeded sample of the microbench's shell
-quartets (l uniform over s/p/d, K 1-6, exponents 0.05-1e4, centres in a 10 A cube), the
-errors against the FP64 blocks, scaled by the sample's largest integral, are compared
-across variants that change one stage at a time:
+The FP32 path evaluates the Boys function below its asymptotic threshold (series and
+downward recursion) in FP64 and every other stage in FP32.  Over a seeded sample of the
+microbench's shell quartets (l uniform over s/p/d, K 1-6, exponents 0.05-1e4, centres in a
+10 A cube), the errors against the FP64 blocks, scaled by the sample's largest integral,
+are compared across variants that change one stage at a time:
   * the library's FP32 path;
   * the same with the horizontal recursion in FP64 (HRR's share);
   * the same with the Boys function in FP32 as well (the FP64 Boys' gain);

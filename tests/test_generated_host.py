@@ -38,3 +38,18 @@ def test_boys_host_matches_exact():
             h.hc_boys(M, 64, float(x), F.ctypes.data)
             ex = np.array([oracle.boys_exact(m, x) for m in range(M + 1)])
             assert np.max(np.abs(F - ex) / ex) < 5e-14, (M, x)
+
+
+def test_boys_host_fp32_matches_exact():
+    """The FP32 quartets' Boys function: FP64 grid expansion and downward recursion below
+    the order's asymptotic threshold, FP32 asymptotic form above it; every order within
+    2e-6 relative (1e-30 absolute, for values below float range) of the exact value at the
+    double argument, as the device test asks."""
+    g = golden("boys")
+    h = hostcheck.hc()
+    for M in range(11):
+        F = np.zeros(M + 1)
+        for x in g["x"]:
+            h.hc_boys(M, 32, float(x), F.ctypes.data)
+            ex = np.array([oracle.boys_exact(m, x) for m in range(M + 1)])
+            assert np.all(np.abs(F - ex) <= 1e-30 + 2e-6 * np.abs(ex)), (M, x)
