@@ -16,7 +16,7 @@ import torch
 from . import _lib
 from .basis import ShellBasis
 from .engine import (PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut, heavy_threshold,
-                     split_forms)
+                     mixed_prefix, split_forms)
 from .hamiltonian import one_electron
 from .molecules import shell_basis
 
@@ -86,6 +86,7 @@ class BatchedRHF:
             fs = np.repeat(np.arange(sb.nshell), sb.nfunc)
             blk[self.base[m]:self.base[m + 1]] = sbase[m] + (fs[:, None] * ns[m] + fs[None, :]).ravel()
         self.block_of = torch.as_tensor(blk).to(self.dev)
+        self.block_mol = torch.as_tensor(np.repeat(np.arange(len(sbs)), ns * ns)).to(self.dev)
         # one-electron matrices, orthogonalisers, padded index maps
         self.S, self.H = [], []
         for m, (mol, sb) in enumerate(zip(molecules, sbs)):
@@ -188,16 +189,37 @@ class BatchedRHF:
             need = max(L.gs_fock_jk_mixed_workspace(e - s) for _, s, e in self.segments)
             if getattr(self, "_ws", None) is None or self._ws.numel() < need:
                 self._ws = torch.empty(int(need), dtype=torch.uint8, device=self.dev)
-            for cls, s, e in self.segments:
+            mol_dmax = None
+            for (cls, s, e), heavy in zip(self.segments, self.heavy):
                 if classes is not None and cls not in classes:
                     continue
+                # the heavy prefix in the split form, one banded launch per precision; the
+                # bound there takes each molecule's largest |P| (at least the block value the
+                # partition uses, so no quartet is screened or demoted that the partition
+                # would keep)
+                h = 0
+                for prec, (form, _, count), lo, hi in mixed_prefix(cls, heavy, cut):
+                    if mol_dmax is None:
+                        mol_dmax = torch.zeros(len(self.mol_n), dtype=torch.float64,
+                                               device=self.dev)
+                        mol_dmax.scatter_reduce_(0, self.block_mol, dmax, "amax",
+                                                 include_self=True)
+                    h = count
+                    rc = L.gs_fock_jk_batched(
+                        *cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
+                        _lib.ptr(self.pairs.prims(prec)), _lib.ptr(self.ds.comp_scale),
+                        _lib.ptr(self.local_fo), _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base),
+                        _lib.ptr(self.mol_n), _lib.ptr(mol_dmax), self.mat_stride, count,
+                        base + s * 8, _lib.ptr(P), _lib.ptr(J), 1, _lib.ptr(P), _lib.ptr(K), thr,
+                        lo, hi, st)
+                    _lib.check(rc, f"gs_fock_jk_batched{cls}")
                 rc = L.gs_fock_jk_batched_mixed(
                     *cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
                     _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
                     _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
                     _lib.ptr(dmax), _lib.ptr(self.mol_shell0), _lib.ptr(self.mol_nshell),
-                    _lib.ptr(self.mol_sbase), self.mat_stride, e - s, base + s * 8, _lib.ptr(P),
-                    _lib.ptr(J), 1,
+                    _lib.ptr(self.mol_sbase), self.mat_stride, e - s - h, base + (s + h) * 8,
+                    _lib.ptr(P), _lib.ptr(J), 1,
                     _lib.ptr(P), _lib.ptr(K), thr, cut, _lib.ptr(self._ws), self._ws.numel(), st)
                 _lib.check(rc, f"gs_fock_jk_batched_mixed{cls}")
             return

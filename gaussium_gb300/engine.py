@@ -66,6 +66,20 @@ def split_forms(cls, precision, heavy):
     return [(SPLIT_FORM, 0, heavy), (THREAD_FORM, heavy, None)]
 
 
+def mixed_prefix(cls, heavy, mixed_cut):
+    """Launches for the heavy prefix of a class segment in a mixed-precision build, whose
+    partitioned launch (gs_fock_jk_mixed) evaluates every quartet in the class's configured
+    form: [(precision, (form, 0, heavy), prec_lo, prec_hi)], FP64 for density-weighted
+    bounds at or above ``mixed_cut``, FP32 below, each in the split form where
+    split_forms puts it (else the configured form).  Empty when neither precision splits:
+    the partitioned launch then takes the whole segment."""
+    parts = {p: split_forms(cls, p, heavy)[0] for p in (64, 32)}
+    if all(f != SPLIT_FORM for f, _, _ in parts.values()):
+        return []
+    return [(64, (parts[64][0], 0, heavy), mixed_cut, float("inf")),
+            (32, (parts[32][0], 0, heavy), 0.0, mixed_cut)]
+
+
 def _check_sizes():
     sizes = np.zeros(4, dtype=np.int32)
     _lib.check(_lib.lib().gs_record_sizes(sizes.ctypes.data), "gs_record_sizes")
@@ -438,13 +452,25 @@ class JKEngine:
             need = max(L.gs_fock_jk_mixed_workspace(e - s) for _, s, e in self.segments)
             if getattr(self, "_ws", None) is None or self._ws.numel() < need:
                 self._ws = torch.empty(int(need), dtype=torch.uint8, device=dev)
-            for cls, s, e in self.segments:
+            for (cls, s, e), heavy in zip(self.segments, self.heavy):
                 if classes is not None and cls not in classes:
                     continue
+                # the heavy prefix in the split form: one banded launch per precision (the
+                # same density-weighted bound and cut as the partition)
+                h = 0
+                for prec, (form, _, count), lo, hi in mixed_prefix(cls, heavy, mixed_cut):
+                    h = count
+                    rc = L.gs_fock_jk(*cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
+                                      _lib.ptr(self.pairs.prims(prec)),
+                                      _lib.ptr(self.ds.comp_scale), _lib.ptr(self.ds.func_off),
+                                      self.sb.nshell, n, count, base + s * 8, _lib.ptr(pj_c),
+                                      _lib.ptr(jbuf), nk, _lib.ptr(pk_c), _lib.ptr(kbuf),
+                                      _lib.ptr(dmax), thr, lo, hi, st)
+                    _lib.check(rc, f"gs_fock_jk{cls}")
                 rc = L.gs_fock_jk_mixed(*cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
                                         _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale),
-                                        _lib.ptr(self.ds.func_off), self.sb.nshell, n, e - s,
-                                        base + s * 8, _lib.ptr(pj_c), _lib.ptr(jbuf), nk,
+                                        _lib.ptr(self.ds.func_off), self.sb.nshell, n, e - s - h,
+                                        base + (s + h) * 8, _lib.ptr(pj_c), _lib.ptr(jbuf), nk,
                                         _lib.ptr(pk_c), _lib.ptr(kbuf), _lib.ptr(dmax), thr,
                                         mixed_cut, _lib.ptr(self._ws), self._ws.numel(), st)
                 _lib.check(rc, f"gs_fock_jk_mixed{cls}")

@@ -121,3 +121,27 @@ def test_quartet_batch_host_planning(monkeypatch):
         assert np.all(np.diff(work[s:e]) <= 0)
         assert heavy == np.count_nonzero(work[s:e] >= engine.heavy_threshold(cls))
         assert np.all(work[s:s + heavy] >= engine.heavy_threshold(cls))
+
+
+def test_mixed_prefix_bands(monkeypatch):
+    """The heavy prefix of a mixed-precision build: two banded launches whose bands tile
+    the density-weighted bound at the cut exactly as the partition does (FP64 at or above
+    it, FP32 below), each in the split form unless that precision's split is off or the
+    class does not run one thread per quartet; nothing when neither precision splits."""
+    forms = {64: engine.THREAD_FORM, 32: engine.THREAD_FORM}
+
+    class StubLib:
+        def gs_class_form(self, la, lb, lc, ld, precision):
+            return forms[precision]
+
+    monkeypatch.setattr(engine._lib, "lib", lambda: StubLib())
+    cls, inf = (1, 0, 0, 0), float("inf")
+    assert engine.mixed_prefix(cls, 0, 1e-2) == []
+    assert engine.mixed_prefix(cls, 7, 1e-2) == [
+        (64, (engine.SPLIT_FORM, 0, 7), 1e-2, inf), (32, (engine.SPLIT_FORM, 0, 7), 0.0, 1e-2)]
+    monkeypatch.setattr(engine, "SPLIT_OFF", {(cls, 64)})
+    assert engine.mixed_prefix(cls, 7, 1e-2) == [
+        (64, (0, 0, 7), 1e-2, inf), (32, (engine.SPLIT_FORM, 0, 7), 0.0, 1e-2)]
+    monkeypatch.setattr(engine, "SPLIT_OFF", set())
+    forms[64] = forms[32] = engine.WARP_FORM
+    assert engine.mixed_prefix(cls, 7, 1e-2) == []
