@@ -264,7 +264,7 @@ def run_gpu(args, rank, world):
         from gaussium_gb300 import autotune
         batch.pairs.build()
         chosen = autotune.tune_blocks(batch, out, reps=2)
-        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
+        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.describe(r)
                  for (c, p), r in chosen.items()}
 
     def step(precision, timing=None):
@@ -488,7 +488,7 @@ def fock_arms(n_waters, seed, mixed_cut, tune=True):
         rng = np.random.default_rng(0)
         a = rng.standard_normal((eng.sb.nbf, eng.sb.nbf)) * 0.1
         chosen = autotune.tune_jk(eng, torch.tensor(a + a.T, device="cuda"), reps=2)
-        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
+        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.describe(r)
                  for (c, p), r in chosen.items()}
     # warm-up: one build of each kind
     driver.rhf(mol, engine=eng, threshold=1e-10, max_iter=2)
@@ -576,7 +576,7 @@ def run_batch(args, rank, world):
     if not args.no_tune:
         from gaussium_gb300 import autotune
         chosen = other.tune(reps=2)
-        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.NAMES[r["form"]]
+        forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.describe(r)
                  for (c, p), r in chosen.items()}
     other.run(max_iter=2, **opts)
     del other
@@ -695,7 +695,7 @@ def run_gradient(args, rank, world):
         from gaussium_gb300 import autotune
         chosen = autotune.tune_jk(eng, torch.tensor(res.density, device="cuda"), precisions=(64,),
                                   reps=2)
-        fock_forms = {"%d%d%d%d" % c: autotune.NAMES[r["form"]] for (c, p), r in chosen.items()}
+        fock_forms = {"%d%d%d%d" % c: autotune.describe(r) for (c, p), r in chosen.items()}
     fb = TimedFock(np.zeros((sb.nbf, sb.nbf)), eng)
     for _ in range(5):
         fb.create(res.density)

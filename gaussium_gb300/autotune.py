@@ -8,7 +8,9 @@ depends on the workload, chiefly on the primitive counts of the quartets and on 
 shared memory the grouped buffers take from occupancy.  The
 tuner times both forms of every such class on the caller's own task lists (CUDA events on
 the launching stream, after a warm-up launch, median of ``reps``) and selects the faster
-with ``gs_set_class_variant``.  The choice is process-wide and stays until changed.
+with ``gs_set_class_variant``; then, for every class, it times the class with and without
+its heavy form (split or cooperative, for the quartets with many primitive quartets) and
+keeps the faster.  The choices are process-wide and stay until changed.
 """
 import json
 
@@ -16,8 +18,9 @@ import torch
 
 from . import _lib
 
-THREAD, WARP, GROUPED, SPLIT = 1, 2, 3, 4
-NAMES = {THREAD: "thread", WARP: "warp", GROUPED: "warp-grouped", SPLIT: "thread-split"}
+THREAD, WARP, GROUPED, SPLIT, COOP = 1, 2, 3, 4, 5
+NAMES = {THREAD: "thread", WARP: "warp", GROUPED: "warp-grouped", SPLIT: "thread-split",
+         COOP: "warp-cooperative"}
 
 
 def forms(cls, precision):
@@ -25,9 +28,19 @@ def forms(cls, precision):
     m = _lib.lib().gs_class_variants(*cls, precision)
     if m < 0:
         _lib.check(-m, f"gs_class_variants{cls}")
-    # the split form serves the heavy quartets of a thread-form class (engine.split_forms);
-    # as a whole-class form it would leave most lanes idle on light quartets
+    # the split and cooperative forms serve the heavy quartets of a thread-form or warp-form
+    # class (engine.split_forms); as whole-class forms they would leave most lanes idle on
+    # light quartets
     return [v for v in (THREAD, WARP, GROUPED) if m & (1 << (v - 1))]
+
+
+def describe(row):
+    """Name of a tuned class's forms: its form, with the heavy form where the tuner kept
+    its heavy quartets in the split or cooperative form."""
+    name = NAMES[row["form"]]
+    if row.get("heavy_form"):
+        name += "+split" if row["form"] == THREAD else "+cooperative"
+    return name
 
 
 def set_form(cls, precision, variant):
@@ -61,25 +74,28 @@ def tune(segments, run_class, precisions=(64, 32), reps=3, min_tasks=1):
             if e - s < min_tasks:
                 continue
             fs = forms(cls, prec)
-            if len(fs) < 2:
-                continue
             times = {}
-            for v in fs:
-                set_form(cls, prec, v)
-                times[v] = _time(lambda: run_class(cls, prec), reps)
-            best = min(times, key=times.get)
-            set_form(cls, prec, best)
+            if len(fs) >= 2:
+                for v in fs:
+                    set_form(cls, prec, v)
+                    times[v] = _time(lambda: run_class(cls, prec), reps)
+                best = min(times, key=times.get)
+                set_form(cls, prec, best)
+                t_best = times[best]
+            else:
+                best = fs[0]
+                t_best = _time(lambda: run_class(cls, prec), reps)
             row = {"form": best, "ms": times}
-            if best == THREAD:
-                # the thread form runs its heavy quartets in the split form; keep that only
-                # where it measures faster than leaving them on threads
+            # the class's heavy quartets run in the split form (thread form) or the
+            # cooperative form (warp forms); keep that only where it measures faster than
+            # leaving them on the class's own form
+            engine.SPLIT_OFF.add((cls, prec))
+            off = _time(lambda: run_class(cls, prec), reps)
+            engine.SPLIT_OFF.discard((cls, prec))
+            row["heavy_form"] = off >= t_best
+            row["ms_without_heavy_form"] = off
+            if not row["heavy_form"]:
                 engine.SPLIT_OFF.add((cls, prec))
-                off = _time(lambda: run_class(cls, prec), reps)
-                engine.SPLIT_OFF.discard((cls, prec))
-                row["heavy_split"] = off >= times[THREAD]
-                row["ms_without_split"] = off
-                if not row["heavy_split"]:
-                    engine.SPLIT_OFF.add((cls, prec))
             chosen[(cls, prec)] = row
     return chosen
 
@@ -129,7 +145,7 @@ def tune_gradient(segments, run_class, reps=3):
 
 def reset(segments, precisions=(64, 32)):
     """Back to the built-in default form for every class of ``segments`` (heavy quartets
-    of thread-form classes in the split form again)."""
+    in the split or cooperative form again)."""
     from . import engine
     for prec in precisions:
         for cls, _, _ in segments:

@@ -15,8 +15,8 @@ import torch
 
 from . import _lib
 from .basis import ShellBasis
-from .engine import (PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut, heavy_threshold,
-                     mixed_prefix, split_forms)
+from .engine import (COOP_PRIM_QUARTETS, PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut,
+                     heavy_threshold, mixed_prefix, split_forms)
 from .hamiltonian import one_electron
 from .molecules import shell_basis
 
@@ -103,11 +103,13 @@ class BatchedRHF:
         self.segments, self.tasks = batched_task_list(q, pc_d, pm_d, nprim, thr, len(PAIR_ORDER),
                                                       len(self.sbs))
         self.ntasks = int(self.tasks.shape[0])
-        # tasks of each segment with many primitive quartets (a prefix: the segments are
-        # sorted by descending primitive work); they run in the split form (engine.split_forms)
+        # tasks of each segment with many primitive quartets (prefixes: the segments are
+        # sorted by descending primitive work); they run in the split or cooperative form
+        # (engine.split_forms)
         work = nprim[self.tasks[:, 0].long()] * nprim[self.tasks[:, 1].long()] \
             if self.ntasks else torch.zeros(0, dtype=torch.int64, device=self.dev)
-        self.heavy = [int((work[s:e] >= heavy_threshold(cls)).sum()) for cls, s, e in self.segments]
+        self.heavy = [(int((work[s:e] >= heavy_threshold(cls)).sum()),
+                       int((work[s:e] >= COOP_PRIM_QUARTETS).sum())) for cls, s, e in self.segments]
 
     def _padded_setup(self):
         B, N = len(self.sbs), self.nmax
@@ -197,21 +199,20 @@ class BatchedRHF:
                 # bound there takes each molecule's largest |P| (at least the block value the
                 # partition uses, so no quartet is screened or demoted that the partition
                 # would keep)
-                h = 0
-                for prec, (form, _, count), lo, hi in mixed_prefix(cls, heavy, cut):
+                h, launches = mixed_prefix(cls, heavy, cut)
+                for prec, form, first, count, lo, hi in launches:
                     if mol_dmax is None:
                         mol_dmax = torch.zeros(len(self.mol_n), dtype=torch.float64,
                                                device=self.dev)
                         mol_dmax.scatter_reduce_(0, self.block_mol, dmax, "amax",
                                                  include_self=True)
-                    h = count
                     rc = L.gs_fock_jk_batched(
                         *cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
                         _lib.ptr(self.pairs.prims(prec)), _lib.ptr(self.ds.comp_scale),
                         _lib.ptr(self.local_fo), _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base),
                         _lib.ptr(self.mol_n), _lib.ptr(mol_dmax), self.mat_stride, count,
-                        base + s * 8, _lib.ptr(P), _lib.ptr(J), 1, _lib.ptr(P), _lib.ptr(K), thr,
-                        lo, hi, st)
+                        base + (s + first) * 8, _lib.ptr(P), _lib.ptr(J), 1, _lib.ptr(P),
+                        _lib.ptr(K), thr, lo, hi, st)
                     _lib.check(rc, f"gs_fock_jk_batched{cls}")
                 rc = L.gs_fock_jk_batched_mixed(
                     *cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),

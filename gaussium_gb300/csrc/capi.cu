@@ -37,7 +37,8 @@ int find_variants(int la, int lb, int lc, int ld, int prec) {
 // total angular momentum, 1 = one thread per quartet, 2 = one warp per quartet, 3 = one warp
 // per quartet with several primitive quartets per VRR pass.  It rides in bits 8.. of the
 // precision argument of the class launchers; 4 = the thread form's code with one warp per
-// quartet over its primitive quartets (split form).
+// quartet over its primitive quartets (split form); 5 = the warp form's code with several
+// warps per quartet (cooperative form, per call only).
 int g_variant[3][3][3][3][2] = {};
 
 inline int pv(int la, int lb, int lc, int ld, int prec) {
@@ -45,11 +46,11 @@ inline int pv(int la, int lb, int lc, int ld, int prec) {
 }
 
 // The precision argument of the launch entry points: 64 or 32, optionally with an explicit
-// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp, 4 split; 0 = the class's
-// configured form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
+// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp, 4 split, 5 cooperative; 0 =
+// the class's configured form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
 int decode_precision(int la, int lb, int lc, int ld, int precision) {
     const int prec = precision & 0xff, form = precision >> 8;
-    if ((prec != 64 && prec != 32) || form < 0 || form > 4) return -1;
+    if ((prec != 64 && prec != 32) || form < 0 || form > 5) return -1;
     if (form == 0) return pv(la, lb, lc, ld, prec);
     if (!(find_variants(la, lb, lc, ld, prec) & (1 << (form - 1)))) return -1;
     return prec | (form << 8);

@@ -5,7 +5,8 @@
 //   FP32 thread kernel for L <= GS_THREAD32_MAX, FP32 warp kernel for L >= GS_WIDE32_FROM,
 //   grouped form wherever the warp kernel is built and the class's group is above 1.
 // Where several exist the caller's choice (bits 8.. of the precision argument: 1 = thread,
-// 2 = warp, 3 = grouped warp, 4 = split: thread code, one warp per quartet) wins, else the default: the warp kernel from L = GS_WIDE64_MIN
+// 2 = warp, 3 = grouped warp, 4 = split: thread code, one warp per quartet, 5 = cooperative:
+// warp code, up to eight warps per quartet) wins, else the default: the warp kernel from L = GS_WIDE64_MIN
 // (FP64) or GS_WIDE32_MIN (FP32) up, grouped when its group is at least 4.  On GB300 a
 // warp-wide FP64 instruction holds the pipe for the same time whatever its active lanes, so
 // narrow recursion levels are filled with several primitive quartets.
@@ -49,13 +50,14 @@ struct ClassForms {
 
 // bit 0: thread kernel built, bit 1: warp kernel built, bit 2: grouped warp kernel built,
 // bit 3: split form built (the thread kernel's code, one warp per quartet over its
-// primitive quartets; wherever the thread kernel is)
+// primitive quartets; wherever the thread kernel is), bit 4: cooperative form built (the
+// warp kernel's code, several warps per quartet; wherever the warp kernel is)
 template <int LA, int LB, int LC, int LD>
 int variants(int prec) {
     using F = ClassForms<LA, LB, LC, LD>;
     if (prec == 64)
-        return (F::thread64 ? 9 : 0) | (F::wide64 ? 2 : 0) | (F::grouped64 ? 4 : 0);
-    return (F::thread32 ? 9 : 0) | (F::wide32 ? 2 : 0) | (F::grouped32 ? 4 : 0);
+        return (F::thread64 ? 9 : 0) | (F::wide64 ? 18 : 0) | (F::grouped64 ? 4 : 0);
+    return (F::thread32 ? 9 : 0) | (F::wide32 ? 18 : 0) | (F::grouped32 ? 4 : 0);
 }
 
 template <int LA, int LB, int LC, int LD, int PREC>
@@ -71,6 +73,7 @@ int launch_prec(int kind, int variant, const void* args, cudaStream_t st) {
     if (kind == GS_KIND_FORM) {
         // the form a launch with this variant resolves to
         if (v == 4 && thread) return 4;
+        if (v == 5 && wide) return 5;
         if (v == 3 && grouped) return 3;
         if (v >= 2 && v <= 3 && wide) return 2;
         return thread ? 1 : (wide ? 2 : 0);
@@ -84,6 +87,10 @@ int launch_prec(int kind, int variant, const void* args, cudaStream_t st) {
         }
     }
     if (v == 4) v = 1;
+    if constexpr (wide) {
+        if (v == 5 && kind != GS_KIND_SCHWARZ) return launch_wide_coop<LA, LB, LC, LD, PREC>(kind, args, st);
+    }
+    if (v == 5) v = 2;
     if constexpr (grouped) {
         if (v == 3) return launch_wide<LA, LB, LC, LD, PREC, F::VG>(kind, args, st);
     }

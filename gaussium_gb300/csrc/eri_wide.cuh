@@ -13,6 +13,7 @@
 #pragma once
 #include <type_traits>
 #include "eri_common.cuh"
+#include "eri_kernels.cuh"
 #include "gs_args.h"
 
 namespace gs {
@@ -158,21 +159,19 @@ __device__ __forceinline__ void vrr_step(const uint4* __restrict__ vrec, int nof
     }
 }
 
-// Evaluate one contracted quartet; on return sm[0 .. HSIZE) holds the HRR buffer whose
-// output slots are W::outslot().
+// Contracted [e0|f0] targets of primitive-quartet setup rounds first, first + stride, ...
+// (a round is Lay::SB primitive quartets): target lane + 32 k is added to acc[k].
 template <int LA, int LB, int LC, int LD, typename T, int VG>
-__device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
-                                             const PrimRec<T>* __restrict__ prims,
-                                             T* __restrict__ sm, int lane) {
+__device__ __forceinline__ void wide_contract(const PairRec& B, const PairRec& K,
+                                              const PrimRec<T>* __restrict__ prims,
+                                              T* __restrict__ sm, int lane, int first, int stride,
+                                              T* __restrict__ acc) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
     using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
     constexpr int L = G::L;
     constexpr int NACC = G::NACC;
     constexpr int NACCW = (NACC + 31) / 32;
-    T acc[NACCW];
-#pragma unroll
-    for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
     T* sC = sm;
     T* sF = sm + Lay::SC;
     T* node = sm + Lay::SC + Lay::SF;
@@ -185,7 +184,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     const uint4* __restrict__ vrec = VG == 1 ? W::vrec() : W::vrec_g();
     const int* __restrict__ vseg = VG == 1 ? W::vseg() : W::vseg_g();
     const unsigned short* __restrict__ vtgt = VG == 1 ? W::vtgt() : W::vtgt_g();
-    for (int base = 0; base < ntot; base += Lay::SB) {
+    for (int base = first * Lay::SB; base < ntot; base += stride * Lay::SB) {
         const int i = base + lane;
         if (lane < Lay::SB && i < ntot) {
             const PrimRec<T> P = prims[B.prim_off + i / nK];
@@ -259,14 +258,15 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
         }
         }
     }
-    // horizontal recursion in shared memory
+}
+
+// Horizontal recursion in shared memory from the contracted targets in sm[0 .. NACC); on
+// return sm[0 .. HSIZE) holds the HRR buffer whose output slots are W::outslot().
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void wide_hrr(const PairRec& B, const PairRec& K, T* __restrict__ sm,
+                                         int lane) {
+    using W = WideProg<LA, LB, LC, LD>;
     T* H = sm;
-#pragma unroll
-    for (int k = 0; k < NACCW; ++k) {
-        const int t = lane + 32 * k;
-        if (t < NACC) H[t] = acc[k];
-    }
-    __syncwarp();
     const unsigned int* __restrict__ hop = W::hop();
     const int* __restrict__ hlev = W::hlev();
     const T dv0 = T(B.ABx), dv1 = T(B.ABy), dv2 = T(B.ABz);
@@ -314,20 +314,34 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     }
 }
 
+// Evaluate one contracted quartet with one warp; on return sm[0 .. HSIZE) holds the HRR
+// buffer whose output slots are W::outslot().
 template <int LA, int LB, int LC, int LD, typename T, int VG>
-__global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_write(const WriteArgs a) {
+__device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
+                                             const PrimRec<T>* __restrict__ prims,
+                                             T* __restrict__ sm, int lane) {
+    constexpr int NACC = ClassGen<LA, LB, LC, LD>::NACC;
+    constexpr int NACCW = (NACC + 31) / 32;
+    T acc[NACCW];
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
+    wide_contract<LA, LB, LC, LD, T, VG>(B, K, prims, sm, lane, 0, 1, acc);
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) {
+        const int t = lane + 32 * k;
+        if (t < NACC) sm[t] = acc[k];
+    }
+    __syncwarp();
+    wide_hrr<LA, LB, LC, LD, T>(B, K, sm, lane);
+}
+
+// Block write of an evaluated quartet (HRR buffer in sm).
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void wide_write_out(const WriteArgs& a, const WriteTask& task,
+                                               const PairRec& B, const PairRec& K,
+                                               T* __restrict__ sm, int lane) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_W;
-    const int t = blockIdx.x * kWideWarps + warp;
-    if (t >= a.ntask) return;
-    const WriteTask task = a.tasks[t];
-    const PairRec B = a.pairs[task.bra];
-    const PairRec K = a.pairs[task.ket];
-    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     long long s[4];
     block_strides(task.code, G::NA, G::NB, G::NC, G::ND, s);
     T* sab = sm + W::HSIZE;
@@ -349,14 +363,29 @@ __global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_write(co
 }
 
 template <int LA, int LB, int LC, int LD, typename T, int VG>
-__device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restrict__ sm, int lane) {
+__global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_write(const WriteArgs a) {
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_W;
+    const int t = blockIdx.x * kWideWarps + warp;
+    if (t >= a.ntask) return;
+    const WriteTask task = a.tasks[t];
+    const PairRec B = a.pairs[task.bra];
+    const PairRec K = a.pairs[task.ket];
+    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_write_out<LA, LB, LC, LD, T>(a, task, B, K, sm, lane);
+}
+
+// J/K digestion of an evaluated quartet (HRR buffer in sm).
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void wide_jk_digest(const JKArgs& a, const int2& task,
+                                               const PairRec& B, const PairRec& K,
+                                               T* __restrict__ sm, int lane) {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
     constexpr int NA = G::NA, NB = G::NB, NC = G::NC, ND = G::ND;
     constexpr int NAB = NA * NB, NCD = NC * ND;
-    const int2 task = a.tasks[t];
-    const PairRec B = a.pairs[task.x];
-    const PairRec K = a.pairs[task.y];
     int n = a.nbf;
     long long mbase = 0;
     if (a.shell_mol) {
@@ -364,24 +393,6 @@ __device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restri
         n = a.mol_n[m];
         mbase = a.mol_base[m];
     }
-    if (a.screen_thr > 0.0) {
-        const double bound = (double)B.qmax * (double)K.qmax;
-        double dm;
-        if (a.shell_mol) {
-            dm = a.mol_dmax[a.shell_mol[B.sa]];
-        } else {
-            const int ns = a.nshell;
-            dm = a.shell_dmax[B.sa * ns + B.sb];
-            dm = fmax(dm, a.shell_dmax[K.sa * ns + K.sb]);
-            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sa]);
-            dm = fmax(dm, a.shell_dmax[B.sa * ns + K.sb]);
-            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sa]);
-            dm = fmax(dm, a.shell_dmax[B.sb * ns + K.sb]);
-        }
-        const double est = bound * dm;
-        if (est < a.screen_thr || est < a.prec_lo || est >= a.prec_hi) return;
-    }
-    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     const double deg = (B.sa == B.sb ? 0.5 : 1.0) * (K.sa == K.sb ? 0.5 : 1.0) *
                        (task.x == task.y ? 0.5 : 1.0);
     T* V = sm + W::HSIZE;
@@ -452,6 +463,16 @@ __device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restri
     }
 }
 
+template <int LA, int LB, int LC, int LD, typename T, int VG>
+__device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restrict__ sm, int lane) {
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    if (!jk_keep(a, B, K)) return;                 // warp-uniform
+    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_jk_digest<LA, LB, LC, LD, T>(a, task, B, K, sm, lane);
+}
+
 // One warp per task; with a task count on the device (after a partition) the grid is
 // capped and each warp strides over the tasks.
 template <int LA, int LB, int LC, int LD, typename T, int VG>
@@ -493,6 +514,94 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0) a.q[p] = sqrt(m);
+}
+
+// Cooperative form for the heavy quartets of a warp-form class: one block of several warps
+// per quartet.  Warp w contracts setup rounds w, w + warps, ... of the quartet's primitive
+// quartets into its own accumulators; the partial sums meet in shared memory, added in
+// warp order (the result does not depend on timing), and warp 0 runs the HRR and the
+// epilogue.  A class's tasks are sorted by descending primitive work, so its heavy prefix
+// is a contiguous range with a host count; this form takes that range and leaves the rest
+// of the segment to the one-warp form.
+//
+// Shared memory: warp 0 has a full one-warp region (VRR buffers, then the HRR buffer and
+// the epilogue's arrays), warps 1.. only the VRR buffers (which also take their partial
+// sums).  Eight warps where that fits in 227 KB, else six, four or two.
+template <int LA, int LB, int LC, int LD, typename T, bool JK> struct CoopLayout {
+    using Lay = WideLayout<LA, LB, LC, LD, T, 1>;
+    static constexpr int NACC = ClassGen<LA, LB, LC, LD>::NACC;
+    static constexpr int FIRST = JK ? Lay::WARP_JK : Lay::WARP_W;
+    static constexpr int REST = Lay::VRR > NACC ? Lay::VRR : NACC;
+    static constexpr bool fits(int w) {
+        return (size_t)(FIRST + (size_t)(w - 1) * REST) * sizeof(T) <= 227 * 1024;
+    }
+    static constexpr int WARPS = fits(8) ? 8 : fits(6) ? 6 : fits(4) ? 4 : 2;
+    static_assert(fits(WARPS), "cooperative block beyond 227 KB");
+    static constexpr size_t BYTES = (size_t)(FIRST + (size_t)(WARPS - 1) * REST) * sizeof(T);
+    __device__ static T* region(T* base, int w) {
+        return w == 0 ? base : base + FIRST + (size_t)(w - 1) * REST;
+    }
+};
+constexpr int kCoopMaxWarps = 8;
+
+// Contract the quartet over the block's warps; true in warp 0, whose region then holds
+// the HRR buffer.
+template <int LA, int LB, int LC, int LD, typename T, bool JK>
+__device__ __forceinline__ bool coop_quartet(const PairRec& B, const PairRec& K,
+                                             const PrimRec<T>* __restrict__ prims,
+                                             T* __restrict__ base, int lane, int warp) {
+    using CL = CoopLayout<LA, LB, LC, LD, T, JK>;
+    constexpr int NACC = CL::NACC;
+    constexpr int NACCW = (NACC + 31) / 32;
+    T* sm = CL::region(base, warp);
+    T acc[NACCW];
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
+    wide_contract<LA, LB, LC, LD, T, 1>(B, K, prims, sm, lane, warp, CL::WARPS, acc);
+#pragma unroll
+    for (int k = 0; k < NACCW; ++k) {
+        const int t = lane + 32 * k;
+        if (t < NACC) sm[t] = acc[k];
+    }
+    __syncthreads();
+    if (warp != 0) return false;
+    for (int t = lane; t < NACC; t += 32) {
+        T v = base[t];
+        for (int w = 1; w < CL::WARPS; ++w) v += CL::region(base, w)[t];
+        base[t] = v;
+    }
+    __syncwarp();
+    wide_hrr<LA, LB, LC, LD, T>(B, K, base, lane);
+    return true;
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(32 * kCoopMaxWarps) k_wide_write_coop(const WriteArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* base = reinterpret_cast<T*>(smem_raw);
+    const int t = blockIdx.x;
+    if (t >= a.ntask) return;                      // block-uniform
+    const WriteTask task = a.tasks[t];
+    const PairRec B = a.pairs[task.bra];
+    const PairRec K = a.pairs[task.ket];
+    if (coop_quartet<LA, LB, LC, LD, T, false>(B, K, (const PrimRec<T>*)a.prims, base, lane, warp))
+        wide_write_out<LA, LB, LC, LD, T>(a, task, B, K, base, lane);
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(32 * kCoopMaxWarps) k_wide_jk_coop(const JKArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* base = reinterpret_cast<T*>(smem_raw);
+    const int t = blockIdx.x;
+    if (t >= a.ntask) return;                      // block-uniform
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    if (!jk_keep(a, B, K)) return;                 // block-uniform
+    if (coop_quartet<LA, LB, LC, LD, T, true>(B, K, (const PrimRec<T>*)a.prims, base, lane, warp))
+        wide_jk_digest<LA, LB, LC, LD, T>(a, task, B, K, base, lane);
 }
 
 // Raise a kernel's dynamic shared-memory limit once (the first launch happens before any
@@ -537,6 +646,29 @@ int launch_wide(int kind, const void* args, cudaStream_t st) {
         } else {
             return GS_ERR_CLASS;
         }
+    } else {
+        return GS_ERR_ARG;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+}
+
+// The cooperative form (host task counts only: the heavy prefix of a class segment).
+template <int LA, int LB, int LC, int LD, int PREC>
+int launch_wide_coop(int kind, const void* args, cudaStream_t st) {
+    using T = typename std::conditional<PREC == 64, double, float>::type;
+    if (kind == GS_KIND_WRITE) {
+        using CL = CoopLayout<LA, LB, LC, LD, T, false>;
+        const WriteArgs& a = *(const WriteArgs*)args;
+        if (a.ntask <= 0) return 0;
+        if (set_smem<k_wide_write_coop<LA, LB, LC, LD, T>>(CL::BYTES)) return GS_ERR_CUDA;
+        k_wide_write_coop<LA, LB, LC, LD, T><<<a.ntask, 32 * CL::WARPS, CL::BYTES, st>>>(a);
+    } else if (kind == GS_KIND_JK) {
+        using CL = CoopLayout<LA, LB, LC, LD, T, true>;
+        const JKArgs& a = *(const JKArgs*)args;
+        if (a.ntask <= 0) return 0;
+        if (a.ntask_dev) return GS_ERR_ARG;
+        if (set_smem<k_wide_jk_coop<LA, LB, LC, LD, T>>(CL::BYTES)) return GS_ERR_CUDA;
+        k_wide_jk_coop<LA, LB, LC, LD, T><<<a.ntask, 32 * CL::WARPS, CL::BYTES, st>>>(a);
     } else {
         return GS_ERR_ARG;
     }

@@ -36,8 +36,14 @@ WRITE_TASK_DTYPE = np.dtype([("bra", "<i4"), ("ket", "<i4"), ("code", "<i4"), ("
 # few long-running warps.  "Many" is at least HEAVY_PRIM_QUARTETS and twice the class's
 # accumulator count (the warp's final sum costs five additions per accumulator).
 HEAVY_PRIM_QUARTETS = 32
-THREAD_FORM, WARP_FORM, GROUPED_FORM, SPLIT_FORM = 1, 2, 3, 4
-# (class, precision) pairs whose heavy quartets stay on the thread form (set by the
+# Quartets with at least COOP_PRIM_QUARTETS primitive quartets of a class that runs one
+# warp per quartet run in the cooperative form: up to eight warps per quartet (as many as
+# fit the shared memory), warp w taking setup rounds w, w + warps, ... of its primitive
+# quartets, the partial sums added in shared memory before one HRR.  The class's time would otherwise have a floor at its heaviest quartet,
+# walked by one warp while the other warps of the launch have finished.
+COOP_PRIM_QUARTETS = 128
+THREAD_FORM, WARP_FORM, GROUPED_FORM, SPLIT_FORM, COOP_FORM = 1, 2, 3, 4, 5
+# (class, precision) pairs whose heavy quartets stay on the class's own form (set by the
 # autotuner where that measured faster)
 SPLIT_OFF = set()
 
@@ -54,30 +60,56 @@ for _i, (_a, _b) in enumerate(PAIR_ORDER):
     _pc_lut[_a, _b] = _i
 
 
+def heavy_counts(cls, work_desc):
+    """(split, cooperative): how many tasks of a segment whose primitive-quartet counts
+    ``work_desc`` are sorted in descending order reach heavy_threshold(cls), and how many
+    reach COOP_PRIM_QUARTETS -- both prefixes of the segment."""
+    w = -np.asarray(work_desc, dtype=np.int64)
+    return (int(np.searchsorted(w, -heavy_threshold(cls), side="right")),
+            int(np.searchsorted(w, -COOP_PRIM_QUARTETS, side="right")))
+
+
 def split_forms(cls, precision, heavy):
     """[(form, first, count)] for a class segment whose tasks are sorted by descending
-    primitive-quartet count, ``heavy`` of them at or above heavy_threshold(cls): the heavy
-    prefix in the split form when the class otherwise runs one thread per quartet.
-    form 0 = the class's configured form; count None = to the end of the segment."""
-    L = _lib.lib()
-    if heavy <= 0 or (cls, precision) in SPLIT_OFF or \
-            L.gs_class_form(*cls, precision) != THREAD_FORM:
+    primitive-quartet count, with heavy = heavy_counts(cls, ...): the heavy prefix in the
+    split form when the class runs one thread per quartet, in the cooperative form when it
+    runs one warp per quartet, the rest in the class's form.  form 0 = the class's
+    configured form; count None = to the end of the segment."""
+    if (cls, precision) in SPLIT_OFF:
         return [(0, 0, None)]
-    return [(SPLIT_FORM, 0, heavy), (THREAD_FORM, heavy, None)]
+    form = _lib.lib().gs_class_form(*cls, precision)
+    if form == THREAD_FORM:
+        h, hform = heavy[0], SPLIT_FORM
+    elif form in (WARP_FORM, GROUPED_FORM):
+        h, hform = heavy[1], COOP_FORM
+    else:
+        h, hform = 0, 0
+    if h <= 0:
+        return [(0, 0, None)]
+    return [(hform, 0, h), (form, h, None)]
 
 
 def mixed_prefix(cls, heavy, mixed_cut):
-    """Launches for the heavy prefix of a class segment in a mixed-precision build, whose
-    partitioned launch (gs_fock_jk_mixed) evaluates every quartet in the class's configured
-    form: [(precision, (form, 0, heavy), prec_lo, prec_hi)], FP64 for density-weighted
-    bounds at or above ``mixed_cut``, FP32 below, each in the split form where
-    split_forms puts it (else the configured form).  Empty when neither precision splits:
-    the partitioned launch then takes the whole segment."""
-    parts = {p: split_forms(cls, p, heavy)[0] for p in (64, 32)}
-    if all(f != SPLIT_FORM for f, _, _ in parts.values()):
-        return []
-    return [(64, (parts[64][0], 0, heavy), mixed_cut, float("inf")),
-            (32, (parts[32][0], 0, heavy), 0.0, mixed_cut)]
+    """The heavy prefix of a class segment in a mixed-precision build, whose partitioned
+    launch (gs_fock_jk_mixed) evaluates every quartet in the class's configured form.
+    Returns (h, [(precision, form, first, count, prec_lo, prec_hi)]): tasks [0, h) run as
+    banded launches -- FP64 for density-weighted bounds at or above ``mixed_cut``, FP32
+    below, the same bands as the partition -- each precision's heavy tasks in its heavy
+    form (split_forms) and the rest of the prefix in its configured form; the partitioned
+    launch takes [h, end).  (0, []) when neither precision has a heavy form here."""
+    parts = {p: split_forms(cls, p, heavy) for p in (64, 32)}
+    h = max((pp[0][2] for pp in parts.values() if len(pp) > 1), default=0)
+    if h == 0:
+        return 0, []
+    out = []
+    for p, lo, hi in ((64, mixed_cut, float("inf")), (32, 0.0, mixed_cut)):
+        pp = parts[p]
+        c = pp[0][2] if len(pp) > 1 else 0
+        if c > 0:
+            out.append((p, pp[0][0], 0, c, lo, hi))
+        if c < h:
+            out.append((p, 0, c, h - c, lo, hi))
+    return h, out
 
 
 def _check_sizes():
@@ -282,8 +314,7 @@ class QuartetBatch:
         self.sorted_bra_nprim = nb[order]
         self.sorted_ket_nprim = nk[order]
         work = self.sorted_bra_nprim * self.sorted_ket_nprim
-        self.heavy = [int(np.count_nonzero(work[s:e] >= heavy_threshold(cls)))
-                      for cls, s, e in self.segments]
+        self.heavy = [heavy_counts(cls, work[s:e]) for cls, s, e in self.segments]
 
     def class_counts(self):
         return {cls: e - s for cls, s, e in self.segments}
@@ -356,7 +387,7 @@ class JKEngine:
         q = self.q
         nprim = torch.as_tensor(self.pairs.nprim).to(dev)
         self.segments = []
-        self.heavy = []           # tasks of each segment with >= HEAVY_PRIM_QUARTETS
+        self.heavy = []           # heavy_counts of each segment
         chunks = []
         ntot = 0
         thr = self.schwarz_thr
@@ -397,7 +428,8 @@ class JKEngine:
                 t = torch.stack([bra[o], ket[o]], dim=1).to(torch.int32)
                 (la, lb), (lc, ld) = PAIR_ORDER[cb], PAIR_ORDER[ck]
                 self.segments.append(((la, lb, lc, ld), ntot, ntot + total))
-                self.heavy.append(int((key >= heavy_threshold((la, lb, lc, ld)) * 4096).sum()))
+                self.heavy.append((int((key >= heavy_threshold((la, lb, lc, ld)) * 4096).sum()),
+                                   int((key >= COOP_PRIM_QUARTETS * 4096).sum())))
                 chunks.append(t)
                 ntot += total
         self.tasks = torch.cat(chunks, 0).contiguous() if chunks else \
@@ -455,17 +487,16 @@ class JKEngine:
             for (cls, s, e), heavy in zip(self.segments, self.heavy):
                 if classes is not None and cls not in classes:
                     continue
-                # the heavy prefix in the split form: one banded launch per precision (the
+                # the heavy prefix in the heavy forms: banded launches per precision (the
                 # same density-weighted bound and cut as the partition)
-                h = 0
-                for prec, (form, _, count), lo, hi in mixed_prefix(cls, heavy, mixed_cut):
-                    h = count
+                h, launches = mixed_prefix(cls, heavy, mixed_cut)
+                for prec, form, first, count, lo, hi in launches:
                     rc = L.gs_fock_jk(*cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
                                       _lib.ptr(self.pairs.prims(prec)),
                                       _lib.ptr(self.ds.comp_scale), _lib.ptr(self.ds.func_off),
-                                      self.sb.nshell, n, count, base + s * 8, _lib.ptr(pj_c),
-                                      _lib.ptr(jbuf), nk, _lib.ptr(pk_c), _lib.ptr(kbuf),
-                                      _lib.ptr(dmax), thr, lo, hi, st)
+                                      self.sb.nshell, n, count, base + (s + first) * 8,
+                                      _lib.ptr(pj_c), _lib.ptr(jbuf), nk, _lib.ptr(pk_c),
+                                      _lib.ptr(kbuf), _lib.ptr(dmax), thr, lo, hi, st)
                     _lib.check(rc, f"gs_fock_jk{cls}")
                 rc = L.gs_fock_jk_mixed(*cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
                                         _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale),

@@ -53,7 +53,9 @@ int gs_class_available(int la, int lb, int lc, int ld);
 
 /* Kernel forms built for class (la lb|lc ld) in the given precision (64 or 32): bit 0 the
  * one-thread-per-quartet kernel, bit 1 the warp-per-quartet kernel, bit 2 the warp kernel
- * that runs several primitive quartets through each recursion pass; negative status on a
+ * that runs several primitive quartets through each recursion pass, bit 3 the split form
+ * (the thread kernel's code, one warp per quartet over its primitive quartets), bit 4 the
+ * cooperative form (the warp kernel's code, up to eight warps per quartet); negative status on a
  * bad class or precision.  No reference counterpart (the reference has one code path). */
 int gs_class_variants(int la, int lb, int lc, int ld, int precision);
 
@@ -67,10 +69,12 @@ int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int vari
 /* The kernel form (1 thread, 2 warp, 3 grouped warp) a launch of (la lb|lc ld) in that
  * precision uses with no explicit form: the configured variant, or the built-in default.
  * The precision argument of gs_eri_blocks, gs_fock_jk and gs_fock_jk_batched may carry an
- * explicit form in its bits 8.. (precision | form << 8) for that call only; the engine uses
- * it to run the quartets of a thread-form class that have many primitive quartets in the
- * warp form, whose lanes share a quartet's primitive quartets.  Negative status on a bad
- * class or precision.  No reference counterpart. */
+ * explicit form in its bits 8.. (precision | form << 8, forms 1-5 as gs_class_variants'
+ * bits 0-4) for that call only; the engine uses it to run the quartets with many primitive
+ * quartets (the heavy prefix of a class's task list, sorted by descending primitive work)
+ * in the split form where the class runs one thread per quartet, and in the cooperative
+ * form where it runs one warp per quartet.  The cooperative form takes host task counts
+ * only.  Negative status on a bad class or precision.  No reference counterpart. */
 int gs_class_form(int la, int lb, int lc, int ld, int precision);
 
 /* K0 shell-pair builder.  Replaces the per-primitive-quartet prologue of

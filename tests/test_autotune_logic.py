@@ -1,29 +1,43 @@
 """The autotuner's choice logic with the library calls replaced by fakes (no GPU): every
-class with several forms is timed in each and left on its fastest; single-form classes
-and empty segments are skipped."""
+class with several forms is timed in each and left on its fastest; every class is then
+timed with and without its heavy form (split or cooperative) and keeps the faster; empty
+segments are skipped."""
 import pytest
 
 from gaussium_gb300 import autotune
 
 
 def test_tune_picks_fastest_form(monkeypatch):
+    from gaussium_gb300 import engine
     built = {(2, 1, 0, 0): [1, 2, 3], (1, 0, 0, 0): [1], (2, 2, 2, 2): [2, 3]}
     cost = {((2, 1, 0, 0), 1): 3.0, ((2, 1, 0, 0), 2): 2.0, ((2, 1, 0, 0), 3): 1.0,
-            ((2, 2, 2, 2), 2): 1.0, ((2, 2, 2, 2), 3): 5.0}
+            ((1, 0, 0, 0), 1): 1.0, ((2, 2, 2, 2), 2): 1.0, ((2, 2, 2, 2), 3): 5.0}
+    # time without the heavy form: slower for (2,1,0,0), faster for (1,0,0,0)
+    off_cost = {(2, 1, 0, 0): 1.5, (1, 0, 0, 0): 0.5}
     state = {}
     monkeypatch.setattr(autotune, "forms", lambda cls, prec: built[cls])
     monkeypatch.setattr(autotune, "set_form", lambda cls, prec, v: state.__setitem__((cls, prec), v))
+    monkeypatch.setattr(engine, "SPLIT_OFF", set())
     current = {}
 
     def run_class(cls, prec):
-        current["c"] = (cls, state[(cls, prec)])
+        if (cls, prec) in engine.SPLIT_OFF:
+            current["t"] = off_cost[cls]
+        else:
+            current["t"] = cost[(cls, state.get((cls, prec), built[cls][0]))]
 
-    monkeypatch.setattr(autotune, "_time", lambda fn, reps: (fn(), cost[current["c"]])[1])
+    monkeypatch.setattr(autotune, "_time", lambda fn, reps: (fn(), current["t"])[1])
     segs = [((2, 1, 0, 0), 0, 10), ((1, 0, 0, 0), 10, 20), ((2, 2, 2, 2), 20, 20)]
     chosen = autotune.tune(segs, run_class, precisions=(64,), reps=1)
     assert chosen[((2, 1, 0, 0), 64)]["form"] == 3
     assert state[((2, 1, 0, 0), 64)] == 3
-    assert ((1, 0, 0, 0), 64) not in chosen          # one form only
+    assert chosen[((2, 1, 0, 0), 64)]["heavy_form"] is True
+    assert ((2, 1, 0, 0), 64) not in engine.SPLIT_OFF
+    assert chosen[((1, 0, 0, 0), 64)]["form"] == 1           # one form: heavy choice only
+    assert chosen[((1, 0, 0, 0), 64)]["heavy_form"] is False
+    assert ((1, 0, 0, 0), 64) in engine.SPLIT_OFF
+    assert autotune.describe(chosen[((2, 1, 0, 0), 64)]) == "warp-grouped+cooperative"
+    assert autotune.describe(chosen[((1, 0, 0, 0), 64)]) == "thread"
     assert ((2, 2, 2, 2), 64) not in chosen          # empty segment (min_tasks)
 
 

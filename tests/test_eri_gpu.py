@@ -154,25 +154,73 @@ def test_primitive_screening_changes_nothing_measurable(gpu_lib):
     assert kept < 0.8      # the screen does drop work on this distribution
 
 
-def test_heavy_quartets_split_matches_single_form(gpu_lib):
-    """A thread-form class runs its quartets with many primitive quartets in the warp
-    form; the blocks agree with every class on one form."""
+@pytest.mark.parametrize("precision", [64, 32])
+def test_heavy_quartet_forms_match_plain_forms(gpu_lib, precision):
+    """Quartets with many primitive quartets run in the split form (thread-form classes)
+    or the cooperative form (warp-form classes); with the default forms and with every
+    class on the warp form, the blocks agree with the same forms run without the heavy
+    forms (the sums differ in order only)."""
     import torch
     from gaussium_gb300 import autotune, engine
     from gaussium_gb300.workloads import random_shell_quartets
     sb, q, _ = random_shell_quartets(6000, seed=21)
     ds = engine.DeviceShells(sb)
-    b = engine.QuartetBatch(ds, q, want32=False, max_exp=engine.PRIM_SCREEN)
-    assert sum(b.heavy) > 0
-    split = torch.zeros(b.total, dtype=torch.float64, device="cuda")
-    b.run(split, 64)
+    b = engine.QuartetBatch(ds, q, want32=precision == 32, max_exp=engine.PRIM_SCREEN)
+    assert sum(h[0] for h in b.heavy) > 0 and sum(h[1] for h in b.heavy) > 0
     classes = [c for c, _, _ in b.segments]
+    tol = 1e-12 if precision == 64 else 1e-5
     try:
-        for c in classes:
-            autotune.set_form(c, 64, autotune.WARP)
-        warp = torch.zeros_like(split)
-        b.run(warp, 64)
+        for warp_all in (False, True):
+            if warp_all:
+                for c in classes:
+                    autotune.set_form(c, precision, autotune.WARP)
+            heavy = torch.zeros(b.total, dtype=torch.float64, device="cuda")
+            b.run(heavy, precision)
+            engine.SPLIT_OFF.update((c, precision) for c in classes)
+            plain = torch.zeros_like(heavy)
+            b.run(plain, precision)
+            engine.SPLIT_OFF.clear()
+            scale = float(plain.abs().max())
+            assert float((heavy - plain).abs().max()) <= tol * scale, warp_all
     finally:
-        autotune.reset([(c, 0, 0) for c in classes], (64,))
-    scale = float(split.abs().max())
-    assert float((split - warp).abs().max()) <= 1e-12 * scale
+        engine.SPLIT_OFF.clear()
+        autotune.reset([(c, 0, 0) for c in classes], (precision,))
+
+
+def test_cooperative_jk_matches_plain_forms(gpu_lib):
+    """J/K of six seeded centres with one s, p and d shell of six primitives each, every
+    class on the warp form: the heavy quartets in the cooperative form agree with the
+    plain warp form, in FP64 and in a mixed build (banded heavy prefix ahead of the
+    partitioned launch)."""
+    import torch
+    from gaussium_gb300 import autotune, engine
+    from gaussium_gb300.basis import ShellBasis
+    rng = np.random.default_rng(7)
+    shells = []
+    for _ in range(6):
+        centre = rng.uniform(-1.5, 1.5, 3)
+        for l in (0, 1, 2):
+            shells.append({"l": l, "centre": centre.tolist(),
+                           "expo": np.sort(10 ** rng.uniform(-1, 1.5, 6))[::-1].tolist(),
+                           "coef": rng.uniform(0.2, 1.0, 6).tolist()})
+    sb = ShellBasis.from_shell_dicts(shells)
+    eng = engine.JKEngine(sb, schwarz_thr=1e-12)
+    assert sum(h[1] for h in eng.heavy) > 0
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((sb.nbf, sb.nbf))
+    P = torch.tensor(a + a.T, device="cuda")
+    try:
+        for c, _, _ in eng.segments:
+            for prec in (64, 32):
+                autotune.set_form(c, prec, autotune.WARP)
+        for kw in (dict(), dict(mixed_cut=1e-2, screen_thr=1e-14)):
+            J1, K1 = eng.jk(P, [P], **kw)
+            engine.SPLIT_OFF.update((c, p) for c, _, _ in eng.segments for p in (64, 32))
+            J0, K0 = eng.jk(P, [P], **kw)
+            engine.SPLIT_OFF.clear()
+            tol = 1e-11 if not kw else 1e-7      # FP32 quartets: sums in another order
+            for x, y in ((J1, J0), (K1[0], K0[0])):
+                assert float((x - y).abs().max()) <= tol * float(y.abs().max()), kw
+    finally:
+        engine.SPLIT_OFF.clear()
+        autotune.reset(eng.segments)

@@ -117,17 +117,22 @@ def test_quartet_batch_host_planning(monkeypatch):
     b = engine.QuartetBatch(_host_only(sb), q)
     assert [s for _, s, _ in b.segments] == sorted(s for _, s, _ in b.segments)
     work = b.sorted_bra_nprim * b.sorted_ket_nprim
-    for (cls, s, e), heavy in zip(b.segments, b.heavy):
+    for (cls, s, e), (split, coop) in zip(b.segments, b.heavy):
         assert np.all(np.diff(work[s:e]) <= 0)
-        assert heavy == np.count_nonzero(work[s:e] >= engine.heavy_threshold(cls))
-        assert np.all(work[s:s + heavy] >= engine.heavy_threshold(cls))
+        assert split == np.count_nonzero(work[s:e] >= engine.heavy_threshold(cls))
+        assert np.all(work[s:s + split] >= engine.heavy_threshold(cls))
+        assert coop == np.count_nonzero(work[s:e] >= engine.COOP_PRIM_QUARTETS)
+        assert np.all(work[s:s + coop] >= engine.COOP_PRIM_QUARTETS)
+    assert sum(c for _, c in b.heavy) > 0
 
 
 def test_mixed_prefix_bands(monkeypatch):
-    """The heavy prefix of a mixed-precision build: two banded launches whose bands tile
-    the density-weighted bound at the cut exactly as the partition does (FP64 at or above
-    it, FP32 below), each in the split form unless that precision's split is off or the
-    class does not run one thread per quartet; nothing when neither precision splits."""
+    """The heavy prefix of a mixed-precision build: banded launches whose bands tile the
+    density-weighted bound at the cut exactly as the partition does (FP64 at or above it,
+    FP32 below), over the same prefix in both precisions -- each precision's heavy tasks
+    in its heavy form (split for a thread-form class, cooperative for a warp-form one) and
+    the rest of the prefix in its configured form; nothing when neither precision has a
+    heavy form."""
     forms = {64: engine.THREAD_FORM, 32: engine.THREAD_FORM}
 
     class StubLib:
@@ -136,12 +141,36 @@ def test_mixed_prefix_bands(monkeypatch):
 
     monkeypatch.setattr(engine._lib, "lib", lambda: StubLib())
     cls, inf = (1, 0, 0, 0), float("inf")
-    assert engine.mixed_prefix(cls, 0, 1e-2) == []
-    assert engine.mixed_prefix(cls, 7, 1e-2) == [
-        (64, (engine.SPLIT_FORM, 0, 7), 1e-2, inf), (32, (engine.SPLIT_FORM, 0, 7), 0.0, 1e-2)]
+    S, C = engine.SPLIT_FORM, engine.COOP_FORM
+    assert engine.mixed_prefix(cls, (0, 0), 1e-2) == (0, [])
+    assert engine.mixed_prefix(cls, (7, 2), 1e-2) == (7, [
+        (64, S, 0, 7, 1e-2, inf), (32, S, 0, 7, 0.0, 1e-2)])
     monkeypatch.setattr(engine, "SPLIT_OFF", {(cls, 64)})
-    assert engine.mixed_prefix(cls, 7, 1e-2) == [
-        (64, (0, 0, 7), 1e-2, inf), (32, (engine.SPLIT_FORM, 0, 7), 0.0, 1e-2)]
+    assert engine.mixed_prefix(cls, (7, 2), 1e-2) == (7, [
+        (64, 0, 0, 7, 1e-2, inf), (32, S, 0, 7, 0.0, 1e-2)])
     monkeypatch.setattr(engine, "SPLIT_OFF", set())
-    forms[64] = forms[32] = engine.WARP_FORM
-    assert engine.mixed_prefix(cls, 7, 1e-2) == []
+    forms[32] = engine.WARP_FORM             # FP64 splits 7, FP32 runs 2 cooperatively
+    assert engine.mixed_prefix(cls, (7, 2), 1e-2) == (7, [
+        (64, S, 0, 7, 1e-2, inf), (32, C, 0, 2, 0.0, 1e-2), (32, 0, 2, 5, 0.0, 1e-2)])
+    forms[64] = engine.GROUPED_FORM
+    assert engine.mixed_prefix(cls, (7, 2), 1e-2) == (2, [
+        (64, C, 0, 2, 1e-2, inf), (32, C, 0, 2, 0.0, 1e-2)])
+    assert engine.mixed_prefix(cls, (7, 0), 1e-2) == (0, [])
+
+
+def test_split_forms_by_class_form(monkeypatch):
+    """split_forms picks the heavy count and form that match the class's form."""
+    form = [engine.THREAD_FORM]
+
+    class StubLib:
+        def gs_class_form(self, la, lb, lc, ld, precision):
+            return form[0]
+
+    monkeypatch.setattr(engine._lib, "lib", lambda: StubLib())
+    cls = (2, 2, 2, 2)
+    assert engine.split_forms(cls, 64, (5, 3)) == [(engine.SPLIT_FORM, 0, 5), (engine.THREAD_FORM, 5, None)]
+    form[0] = engine.WARP_FORM
+    assert engine.split_forms(cls, 64, (5, 3)) == [(engine.COOP_FORM, 0, 3), (engine.WARP_FORM, 3, None)]
+    assert engine.split_forms(cls, 64, (5, 0)) == [(0, 0, None)]
+    w = np.array([600, 300, 200, 128, 127, 40, 1])
+    assert engine.heavy_counts(cls, w) == (int(np.count_nonzero(w >= engine.heavy_threshold(cls))), 4)
