@@ -70,6 +70,9 @@ def parse():
                     help="water molecules of the XC workload (19 6-31G* functions each)")
     ap.add_argument("--mo-waters", type=int, default=6,
                     help="water molecules of the AO->MO workload (13 6-31G functions each)")
+    ap.add_argument("--opt-basis", default="6-31G",
+                    help="basis of the optimize workload (6-31G, or 6-31G* with d shells)")
+    ap.add_argument("--opt-waters", type=int, default=4, help="waters of the optimize workload")
     ap.add_argument("--optimizer", default="L-BFGS-B", choices=["L-BFGS-B", "BFGS"],
                     help="quasi-Newton method of the geometry-optimisation workload")
     ap.add_argument("--guess", default="sad", choices=["core", "sad"],
@@ -769,21 +772,23 @@ def run_gradient(args, rank, world):
 
 # ---------------------------------------------------------------------- geometry optimisation
 def run_optimize(args, rank, world):
-    """Seeded (H2O)4 / 6-31G, each nucleus moved 0.1 A: BFGS on the analytic gradient
-    against the reference's Nelder-Mead restated over the same GPU energy."""
+    """Seeded (H2O)n (default 4) / 6-31G (or --opt-basis), each nucleus moved 0.1 A: BFGS
+    on the analytic gradient against the reference's Nelder-Mead restated over the same GPU
+    energy."""
     import torch
     from gaussium_gb300 import build, molecules, optimize
     from gaussium_gb300.gradient import rhf_energy_gradient
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     build.build()
-    mol = molecules.perturbed(molecules.water_cluster(4, seed=4), 0.1, seed=4)
-    rhf_energy_gradient(molecules.water_cluster(1, seed=1))             # warm-up
-    e0 = rhf_energy_gradient(mol, "6-31G", want_gradient=False)[0]
+    basis, nw = args.opt_basis, args.opt_waters
+    mol = molecules.perturbed(molecules.water_cluster(nw, seed=nw), 0.1, seed=nw)
+    rhf_energy_gradient(molecules.water_cluster(1, seed=1), basis)      # warm-up
+    e0 = rhf_energy_gradient(mol, basis, want_gradient=False)[0]
     t0 = time.perf_counter()
-    e_b, x_b, n_b, gmax_b = optimize.optimize_bfgs(mol, "6-31G", gtol=1e-5, method=args.optimizer)
+    e_b, x_b, n_b, gmax_b = optimize.optimize_bfgs(mol, basis, gtol=1e-5, method=args.optimizer)
     t_b = time.perf_counter() - t0
     nm = optimize.NelderMead(mol.symbols, mol.coords,
-                             lambda m: rhf_energy_gradient(m, "6-31G", want_gradient=False)[0],
+                             lambda m: rhf_energy_gradient(m, basis, want_gradient=False)[0],
                              threshold=1e-6, max_evals=args.nm_evals)
     t0 = time.perf_counter()
     e_n, x_n = nm.optimize()
@@ -792,8 +797,8 @@ def run_optimize(args, rank, world):
         "metric": METRIC, "value": t_b, "unit": "s (gradient-driven geometry optimisation)",
         "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": t_b * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded (H2O)4, 0.1 A perturbation)",
-        "config": {"workload": "geometry optimisation (H2O)4/6-31G", "gtol": 1e-5,
+        "data": f"synthetic (seeded (H2O){nw}, 0.1 A perturbation)",
+        "config": {"workload": f"geometry optimisation (H2O){nw}/{basis}", "gtol": 1e-5,
                    "optimizer": args.optimizer + " on the analytic gradient, internal frame",
                    "nelder_mead_threshold": 1e-6, "nelder_mead_max_evals": args.nm_evals},
         "start_energy": e0,

@@ -159,7 +159,10 @@ def test_heavy_quartet_forms_match_plain_forms(gpu_lib, precision):
     """Quartets with many primitive quartets run in the split form (thread-form classes)
     or the cooperative form (warp-form classes); with the default forms and with every
     class on the warp form, the blocks agree with the same forms run without the heavy
-    forms (the sums differ in order only)."""
+    forms (the sums differ in order only): within 1e-12 of the largest element in FP64;
+    in FP32 both within 1e-4 of it from the FP64 blocks (the tolerance of every FP32
+    class test: the FP32 recursions' own error, which a different summation order moves
+    by the same amount)."""
     import torch
     from gaussium_gb300 import autotune, engine
     from gaussium_gb300.workloads import random_shell_quartets
@@ -168,7 +171,9 @@ def test_heavy_quartet_forms_match_plain_forms(gpu_lib, precision):
     b = engine.QuartetBatch(ds, q, want32=precision == 32, max_exp=engine.PRIM_SCREEN)
     assert sum(h[0] for h in b.heavy) > 0 and sum(h[1] for h in b.heavy) > 0
     classes = [c for c, _, _ in b.segments]
-    tol = 1e-12 if precision == 64 else 1e-5
+    ref = torch.zeros(b.total, dtype=torch.float64, device="cuda")
+    b.run(ref, 64)
+    scale = float(ref.abs().max())
     try:
         for warp_all in (False, True):
             if warp_all:
@@ -180,8 +185,11 @@ def test_heavy_quartet_forms_match_plain_forms(gpu_lib, precision):
             plain = torch.zeros_like(heavy)
             b.run(plain, precision)
             engine.SPLIT_OFF.clear()
-            scale = float(plain.abs().max())
-            assert float((heavy - plain).abs().max()) <= tol * scale, warp_all
+            if precision == 64:
+                assert float((heavy - plain).abs().max()) <= 1e-12 * scale, warp_all
+            else:
+                for x in (heavy, plain):
+                    assert float((x - ref).abs().max()) <= 1e-4 * scale, warp_all
     finally:
         engine.SPLIT_OFF.clear()
         autotune.reset([(c, 0, 0) for c in classes], (precision,))
