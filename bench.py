@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fock", action="store_true",
                     help="leave out the (H2O)n / 6-31G* Fock-build arms of the default line")
+    ap.add_argument("--forms", default=None,
+                    help="path prefix for the tuned kernel forms: loaded from <prefix>.<workload>"
+                         ".json when present, else tuned and saved there (a profiled run then "
+                         "uses the forms its plain run chose)")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the built-in kernel form of every class (no autotuning)")
     ap.add_argument("--cpu-sample", type=int, default=1024)
@@ -266,7 +270,8 @@ def run_gpu(args, rank, world):
         # on this batch by the autotuner before the timed region
         from gaussium_gb300 import autotune
         batch.pairs.build()
-        chosen = autotune.tune_blocks(batch, out, reps=2)
+        chosen = autotune.tune_or_load(forms_file(args, "microbench"),
+                                       lambda: autotune.tune_blocks(batch, out, reps=2))
         forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.describe(r)
                  for (c, p), r in chosen.items()}
 
@@ -398,7 +403,8 @@ def run_gpu(args, rank, world):
     if not args.no_fock:
         # the metric's Fock-build half: (H2O)16 / 6-31G*, plain FP64 vs screened incremental
         # FP64 vs mixed, on the same engine
-        fock = fock_arms(args.waters, args.waters + rank, args.mixed_cut, tune=not args.no_tune)
+        fock = fock_arms(args.waters, args.waters + rank, args.mixed_cut, tune=not args.no_tune,
+                         forms_path=forms_file(args, "fock"))
 
     n_all = args.quartets * world
     ms64, ms32 = res[64]["ms"], res[32]["ms"]
@@ -469,7 +475,12 @@ def run_gpu(args, rank, world):
 
 
 # ---------------------------------------------------------------------- Fock-build workload
-def fock_arms(n_waters, seed, mixed_cut, tune=True):
+def forms_file(args, label):
+    """Where ``--forms`` keeps the tuned kernel forms of one workload (None without it)."""
+    return f"{args.forms}.{label}.json" if getattr(args, "forms", None) else None
+
+
+def fock_arms(n_waters, seed, mixed_cut, tune=True, forms_path=None):
     """RHF of a seeded (H2O)n / 6-31G* cluster three times on one engine (Schwarz 1e-12):
       fp64                       plain FP64 integral-direct builds;
       fp64_screened_incremental  FP64 with density screening at 1e-12 and incremental
@@ -490,7 +501,8 @@ def fock_arms(n_waters, seed, mixed_cut, tune=True):
         from gaussium_gb300 import autotune
         rng = np.random.default_rng(0)
         a = rng.standard_normal((eng.sb.nbf, eng.sb.nbf)) * 0.1
-        chosen = autotune.tune_jk(eng, torch.tensor(a + a.T, device="cuda"), reps=2)
+        chosen = autotune.tune_or_load(
+            forms_path, lambda: autotune.tune_jk(eng, torch.tensor(a + a.T, device="cuda"), reps=2))
         forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.describe(r)
                  for (c, p), r in chosen.items()}
     # warm-up: one build of each kind
@@ -544,7 +556,8 @@ def run_water(args, rank, world):
     from gaussium_gb300 import build
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     build.build()
-    f = fock_arms(args.waters, args.waters + rank, args.mixed_cut, tune=not args.no_tune)
+    f = fock_arms(args.waters, args.waters + rank, args.mixed_cut, tune=not args.no_tune,
+                  forms_path=forms_file(args, "fock"))
     mx = f["arms"]["mixed"]
     line = {
         "metric": METRIC, "value": mx["ms_per_build"], "unit": "ms per Fock build (mixed)",
@@ -578,7 +591,7 @@ def run_batch(args, rank, world):
     forms = {}
     if not args.no_tune:
         from gaussium_gb300 import autotune
-        chosen = other.tune(reps=2)
+        chosen = autotune.tune_or_load(forms_file(args, "batch"), lambda: other.tune(reps=2))
         forms = {"%d%d%d%d/fp%d" % (*c, p): autotune.describe(r)
                  for (c, p), r in chosen.items()}
     other.run(max_iter=2, **opts)

@@ -155,18 +155,40 @@ def reset(segments, precisions=(64, 32)):
 
 def save(chosen, path):
     rows = [{"class": list(cls), "precision": prec, "form": r["form"],
+             "heavy_form": r.get("heavy_form", True),
              "ms": {str(k): v for k, v in r["ms"].items()}} for (cls, prec), r in chosen.items()]
     with open(path, "w") as f:
         json.dump(rows, f, indent=1)
 
 
 def load(path):
-    """Apply a saved choice; returns it in the form ``tune`` returns."""
+    """Apply a saved choice (form and heavy form of every class); returns it in the form
+    ``tune`` returns."""
+    from . import engine
     with open(path) as f:
         rows = json.load(f)
     chosen = {}
     for r in rows:
         cls, prec = tuple(r["class"]), r["precision"]
         set_form(cls, prec, r["form"])
-        chosen[(cls, prec)] = {"form": r["form"], "ms": {int(k): v for k, v in r["ms"].items()}}
+        heavy = r.get("heavy_form", True)
+        if heavy:
+            engine.SPLIT_OFF.discard((cls, prec))
+        else:
+            engine.SPLIT_OFF.add((cls, prec))
+        chosen[(cls, prec)] = {"form": r["form"], "heavy_form": heavy,
+                               "ms": {int(k): v for k, v in r["ms"].items()}}
+    return chosen
+
+
+def tune_or_load(path, tune_fn):
+    """The saved choice at ``path`` if the file exists, else ``tune_fn()`` saved there
+    (None: always tune).  A run under a profiler, whose per-launch overheads would change
+    the choices, loads what a plain run of the same command chose."""
+    import os
+    if path and os.path.exists(path):
+        return load(path)
+    chosen = tune_fn()
+    if path:
+        save(chosen, path)
     return chosen

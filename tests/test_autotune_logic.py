@@ -66,3 +66,31 @@ def test_vrr_group_choice():
         assert vg * prog["nvslot"] <= gen_eri.VGROUP_SLOT_BUDGET
     base = gen_eri.wide_program((2, 2, 2, 2))
     assert gen_eri.wave_efficiency(base["vrec"], base["vseg"]) > 0.94
+
+
+def test_tune_or_load_round_trip(monkeypatch, tmp_path):
+    """A saved choice (form and heavy form per class) is re-applied by tune_or_load without
+    tuning again; without a path it always tunes."""
+    from gaussium_gb300 import engine
+    state = {}
+    monkeypatch.setattr(autotune, "set_form", lambda cls, prec, v: state.__setitem__((cls, prec), v))
+    monkeypatch.setattr(engine, "SPLIT_OFF", set())
+    chosen = {((2, 1, 0, 0), 64): {"form": 3, "heavy_form": True, "ms": {3: 1.0}},
+              ((1, 0, 0, 0), 32): {"form": 1, "heavy_form": False, "ms": {}}}
+    calls = []
+
+    def tune():
+        calls.append(1)
+        return chosen
+
+    path = str(tmp_path / "forms.json")
+    assert autotune.tune_or_load(path, tune) == chosen and len(calls) == 1
+    state.clear()
+    engine.SPLIT_OFF.clear()
+    again = autotune.tune_or_load(path, tune)
+    assert len(calls) == 1                                   # loaded, not tuned
+    assert state == {((2, 1, 0, 0), 64): 3, ((1, 0, 0, 0), 32): 1}
+    assert engine.SPLIT_OFF == {((1, 0, 0, 0), 32)}
+    assert again[((2, 1, 0, 0), 64)]["heavy_form"] is True
+    autotune.tune_or_load(None, tune)
+    assert len(calls) == 2
