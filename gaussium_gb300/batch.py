@@ -15,8 +15,8 @@ import torch
 
 from . import _lib
 from .basis import ShellBasis
-from .engine import (COOP_PRIM_QUARTETS, PAIR_ORDER, PRIM_SCREEN, DeviceShells, PairSet, _pc_lut,
-                     heavy_threshold, mixed_prefix, split_forms)
+from .engine import (COOP_PRIM_QUARTETS, PAIR_ORDER, PRIM_SCREEN, DeviceShells, HeavyLane, PairSet,
+                     _pc_lut, heavy_threshold, mixed_prefix, split_forms)
 from .hamiltonian import one_electron
 from .molecules import shell_basis
 
@@ -182,6 +182,7 @@ class BatchedRHF:
                    classes=None):
         L = _lib.lib()
         st = _lib.stream()
+        lane = HeavyLane(self.dev)
         base = self.tasks.data_ptr()
         if mixed_cut is not None or screen_thr > 0:
             # partitioned path: screened tasks are dropped on the device before any class
@@ -212,7 +213,7 @@ class BatchedRHF:
                         _lib.ptr(self.local_fo), _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base),
                         _lib.ptr(self.mol_n), _lib.ptr(mol_dmax), self.mat_stride, count,
                         base + (s + first) * 8, _lib.ptr(P), _lib.ptr(J), 1, _lib.ptr(P),
-                        _lib.ptr(K), thr, lo, hi, st)
+                        _lib.ptr(K), thr, lo, hi, lane.stream())
                     _lib.check(rc, f"gs_fock_jk_batched{cls}")
                 rc = L.gs_fock_jk_batched_mixed(
                     *cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
@@ -223,6 +224,7 @@ class BatchedRHF:
                     _lib.ptr(P), _lib.ptr(J), 1,
                     _lib.ptr(P), _lib.ptr(K), thr, cut, _lib.ptr(self._ws), self._ws.numel(), st)
                 _lib.check(rc, f"gs_fock_jk_batched_mixed{cls}")
+            lane.join()
             return
         thr = 0.0
         runs = [(precision, 0.0, float("inf"))]
@@ -230,18 +232,25 @@ class BatchedRHF:
             runs = [(64, mixed_cut, float("inf")), (32, 0.0, mixed_cut)]
         for prec, lo, hi in runs:
             prims = self.pairs.prims(prec)
-            for (cls, s, e), heavy in zip(self.segments, self.heavy):
-                if classes is not None and cls not in classes:
-                    continue
-                for form, first, count in split_forms(cls, prec, heavy):
-                    m = (e - s - first) if count is None else count
-                    rc = L.gs_fock_jk_batched(
-                        *cls, prec | (form << 8), _lib.ptr(self.pairs.rec), _lib.ptr(prims),
-                        _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
-                        _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
-                        _lib.ptr(dmax), self.mat_stride, m, base + (s + first) * 8, _lib.ptr(P),
-                        _lib.ptr(J), 1, _lib.ptr(P), _lib.ptr(K), thr, lo, hi, st)
-                    _lib.check(rc, f"gs_fock_jk_batched{cls}")
+            plan = [(cls, s, e, split_forms(cls, prec, heavy))
+                    for (cls, s, e), heavy in zip(self.segments, self.heavy)
+                    if classes is None or cls in classes]
+            # heavy prefixes first, on the side stream; then every class's rest
+            for heavy_pass in (True, False):
+                for cls, s, e, parts in plan:
+                    for k, (form, first, count) in enumerate(parts):
+                        if (k == 0 and len(parts) > 1) != heavy_pass:
+                            continue
+                        m = (e - s - first) if count is None else count
+                        rc = L.gs_fock_jk_batched(
+                            *cls, prec | (form << 8), _lib.ptr(self.pairs.rec), _lib.ptr(prims),
+                            _lib.ptr(self.ds.comp_scale), _lib.ptr(self.local_fo),
+                            _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
+                            _lib.ptr(dmax), self.mat_stride, m, base + (s + first) * 8,
+                            _lib.ptr(P), _lib.ptr(J), 1, _lib.ptr(P), _lib.ptr(K), thr, lo, hi,
+                            lane.stream() if heavy_pass else st)
+                        _lib.check(rc, f"gs_fock_jk_batched{cls}")
+        lane.join()
 
     def tune(self, precisions=(64, 32), reps=3):
         """Choose the kernel form of every class with two on this batch's task lists."""

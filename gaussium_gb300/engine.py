@@ -112,6 +112,36 @@ def mixed_prefix(cls, heavy, mixed_cut):
     return h, out
 
 
+_SIDE = {}
+
+
+class HeavyLane:
+    """The heavy prefixes of a build's classes go to a second stream of the device, forked
+    from the caller's stream before their first launch and joined back by ``join``: their
+    few long blocks then run beside the class launches of the caller's stream instead of
+    leaving most SMs idle while they finish."""
+
+    def __init__(self, device, stream=None):
+        d = indexed_device(device)
+        self.main = stream or torch.cuda.current_stream(d)
+        if d not in _SIDE:
+            _SIDE[d] = torch.cuda.Stream(device=d)
+        self.side = _SIDE[d]
+        self.forked = False
+
+    def stream(self):
+        """The side stream (as the C ABI takes it), forked on first use."""
+        if not self.forked:
+            self.side.wait_stream(self.main)
+            self.forked = True
+        return _lib.stream(self.side)
+
+    def join(self):
+        if self.forked:
+            self.main.wait_stream(self.side)
+            self.forked = False
+
+
 def _check_sizes():
     sizes = np.zeros(4, dtype=np.int32)
     _lib.check(_lib.lib().gs_record_sizes(sizes.ctypes.data), "gs_record_sizes")
@@ -325,17 +355,25 @@ class QuartetBatch:
             raise ValueError(f"output buffer holds {out.numel()} doubles, the blocks need {self.total}")
         L = _lib.lib()
         st = _lib.stream(stream)
+        lane = HeavyLane(self.ds.device, stream)
         base = self.tasks.data_ptr()
         prims = self.pairs.prims(precision)
-        for (cls, s, e), heavy in zip(self.segments, self.heavy):
-            if classes is not None and cls not in classes:
-                continue
-            for form, first, count in split_forms(cls, precision, heavy):
-                n = (e - s - first) if count is None else count
-                rc = L.gs_eri_blocks(*cls, precision | (form << 8), _lib.ptr(self.pairs.rec),
-                                     _lib.ptr(prims), _lib.ptr(self.ds.comp_scale), n,
-                                     base + (s + first) * WRITE_TASK, _lib.ptr(out), st)
-                _lib.check(rc, f"gs_eri_blocks{cls}")
+        plan = [(cls, s, e, split_forms(cls, precision, heavy))
+                for (cls, s, e), heavy in zip(self.segments, self.heavy)
+                if classes is None or cls in classes]
+        # heavy prefixes first, on the side stream; then every class's rest on the caller's
+        for heavy_pass in (True, False):
+            for cls, s, e, parts in plan:
+                for k, (form, first, count) in enumerate(parts):
+                    if (k == 0 and len(parts) > 1) != heavy_pass:
+                        continue
+                    n = (e - s - first) if count is None else count
+                    rc = L.gs_eri_blocks(*cls, precision | (form << 8), _lib.ptr(self.pairs.rec),
+                                         _lib.ptr(prims), _lib.ptr(self.ds.comp_scale), n,
+                                         base + (s + first) * WRITE_TASK, _lib.ptr(out),
+                                         lane.stream() if heavy_pass else st)
+                    _lib.check(rc, f"gs_eri_blocks{cls}")
+        lane.join()
         return out
 
 
@@ -479,6 +517,7 @@ class JKEngine:
             thr = 0.0
         L = _lib.lib()
         st = _lib.stream(stream)
+        lane = HeavyLane(dev, stream)
         base = self.tasks.data_ptr()
         if mixed_cut is not None:
             need = max(L.gs_fock_jk_mixed_workspace(e - s) for _, s, e in self.segments)
@@ -496,7 +535,7 @@ class JKEngine:
                                       _lib.ptr(self.ds.comp_scale), _lib.ptr(self.ds.func_off),
                                       self.sb.nshell, n, count, base + (s + first) * 8,
                                       _lib.ptr(pj_c), _lib.ptr(jbuf), nk, _lib.ptr(pk_c),
-                                      _lib.ptr(kbuf), _lib.ptr(dmax), thr, lo, hi, st)
+                                      _lib.ptr(kbuf), _lib.ptr(dmax), thr, lo, hi, lane.stream())
                     _lib.check(rc, f"gs_fock_jk{cls}")
                 rc = L.gs_fock_jk_mixed(*cls, _lib.ptr(self.pairs.rec), _lib.ptr(self.pairs.p64),
                                         _lib.ptr(self.pairs.p32), _lib.ptr(self.ds.comp_scale),
@@ -508,18 +547,24 @@ class JKEngine:
             runs = []
         for prec, lo, hi in runs:
             prims = self.pairs.prims(prec)
-            for (cls, s, e), heavy in zip(self.segments, self.heavy):
-                if classes is not None and cls not in classes:
-                    continue
-                for form, first, count in split_forms(cls, prec, heavy):
-                    m = (e - s - first) if count is None else count
-                    rc = L.gs_fock_jk(*cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
-                                      _lib.ptr(prims), _lib.ptr(self.ds.comp_scale),
-                                      _lib.ptr(self.ds.func_off), self.sb.nshell, n, m,
-                                      base + (s + first) * 8, _lib.ptr(pj_c), _lib.ptr(jbuf), nk,
-                                      _lib.ptr(pk_c), _lib.ptr(kbuf), _lib.ptr(dmax), thr, lo,
-                                      hi, st)
-                    _lib.check(rc, f"gs_fock_jk{cls}")
+            plan = [(cls, s, e, split_forms(cls, prec, heavy))
+                    for (cls, s, e), heavy in zip(self.segments, self.heavy)
+                    if classes is None or cls in classes]
+            # heavy prefixes first, on the side stream; then every class's rest
+            for heavy_pass in (True, False):
+                for cls, s, e, parts in plan:
+                    for k, (form, first, count) in enumerate(parts):
+                        if (k == 0 and len(parts) > 1) != heavy_pass:
+                            continue
+                        m = (e - s - first) if count is None else count
+                        rc = L.gs_fock_jk(*cls, prec | (form << 8), _lib.ptr(self.pairs.rec),
+                                          _lib.ptr(prims), _lib.ptr(self.ds.comp_scale),
+                                          _lib.ptr(self.ds.func_off), self.sb.nshell, n, m,
+                                          base + (s + first) * 8, _lib.ptr(pj_c), _lib.ptr(jbuf),
+                                          nk, _lib.ptr(pk_c), _lib.ptr(kbuf), _lib.ptr(dmax), thr,
+                                          lo, hi, lane.stream() if heavy_pass else st)
+                        _lib.check(rc, f"gs_fock_jk{cls}")
+        lane.join()
         J = (jbuf + jbuf.T) if jbuf is not None else None
         K = [kbuf[s] + kbuf[s].T for s in range(nk)]
         return J, K
