@@ -159,8 +159,8 @@ __device__ __forceinline__ void vrr_step(const uint4* __restrict__ vrec, int nof
     }
 }
 
-// Contracted [e0|f0] targets of primitive-quartet setup rounds first, first + stride, ...
-// (a round is Lay::SB primitive quartets): target lane + 32 k is added to acc[k].
+// Contracted [e0|f0] targets of primitive quartets first, first + stride, ... of the
+// quartet (set up Lay::SB at a time): target lane + 32 k is added to acc[k].
 template <int LA, int LB, int LC, int LD, typename T, int VG>
 __device__ __forceinline__ void wide_contract(const PairRec& B, const PairRec& K,
                                               const PrimRec<T>* __restrict__ prims,
@@ -176,7 +176,7 @@ __device__ __forceinline__ void wide_contract(const PairRec& B, const PairRec& K
     T* sF = sm + Lay::SC;
     T* node = sm + Lay::SC + Lay::SF;
     const int nK = K.nprim;
-    const int ntot = B.nprim * nK;
+    const int nmine = first < B.nprim * nK ? (B.nprim * nK - first + stride - 1) / stride : 0;
     // the node program: waves of at most 32 nodes (one per lane), or of 32/VG nodes for the
     // grouped form (one per lane group of VG primitive quartets)
     constexpr int NVS = Lay::NVS;
@@ -184,16 +184,16 @@ __device__ __forceinline__ void wide_contract(const PairRec& B, const PairRec& K
     const uint4* __restrict__ vrec = VG == 1 ? W::vrec() : W::vrec_g();
     const int* __restrict__ vseg = VG == 1 ? W::vseg() : W::vseg_g();
     const unsigned short* __restrict__ vtgt = VG == 1 ? W::vtgt() : W::vtgt_g();
-    for (int base = first * Lay::SB; base < ntot; base += stride * Lay::SB) {
-        const int i = base + lane;
-        if (lane < Lay::SB && i < ntot) {
+    for (int base = 0; base < nmine; base += Lay::SB) {
+        const int i = first + (base + lane) * stride;
+        if (lane < Lay::SB && base + lane < nmine) {
             const PrimRec<T> P = prims[B.prim_off + i / nK];
             const PrimRec<T> Q = prims[K.prim_off + i % nK];
             wide_setup_m<L, T>(P, Q, sC + lane * kNCoef, sF + lane * (L + 1));
             sC[lane * kNCoef + kZeroCoef] = T(0);
         }
         __syncwarp();
-        const int nb = min(Lay::SB, ntot - base);
+        const int nb = min(Lay::SB, nmine - base);
         if constexpr (VG == 1) {
         for (int j = 0; j < nb; ++j) {
             const T* __restrict__ c = sC + j * kNCoef;
@@ -517,12 +517,15 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_wide_schwarz(const SchwarzA
 }
 
 // Cooperative form for the heavy quartets of a warp-form class: one block of several warps
-// per quartet.  Warp w contracts setup rounds w, w + warps, ... of the quartet's primitive
-// quartets into its own accumulators; the partial sums meet in shared memory, added in
+// per quartet.  Each warp contracts its share of the quartet's primitive quartets into its
+// own accumulators; the partial sums meet in shared memory, added in
 // warp order (the result does not depend on timing), and warp 0 runs the HRR and the
 // epilogue.  A class's tasks are sorted by descending primitive work, so its heavy prefix
 // is a contiguous range with a host count; this form takes that range and leaves the rest
 // of the segment to the one-warp form.
+//
+// Warp w takes primitive quartets w, w + warps, ..., so the warps' shares differ by one at
+// most and none waits long at the reduction.
 //
 // Shared memory: warp 0 has a full one-warp region (VRR buffers, then the HRR buffer and
 // the epilogue's arrays), warps 1.. only the VRR buffers (which also take their partial

@@ -38,8 +38,8 @@ WRITE_TASK_DTYPE = np.dtype([("bra", "<i4"), ("ket", "<i4"), ("code", "<i4"), ("
 HEAVY_PRIM_QUARTETS = 32
 # Quartets with at least COOP_PRIM_QUARTETS primitive quartets of a class that runs one
 # warp per quartet run in the cooperative form: up to eight warps per quartet (as many as
-# fit the shared memory), warp w taking setup rounds w, w + warps, ... of its primitive
-# quartets, the partial sums added in shared memory before one HRR.  The class's time would otherwise have a floor at its heaviest quartet,
+# fit the shared memory), warp w taking primitive quartets w, w + warps, ..., the partial
+# sums added in shared memory before one HRR.  The class's time would otherwise have a floor at its heaviest quartet,
 # walked by one warp while the other warps of the launch have finished.
 COOP_PRIM_QUARTETS = 128
 THREAD_FORM, WARP_FORM, GROUPED_FORM, SPLIT_FORM, COOP_FORM = 1, 2, 3, 4, 5
