@@ -74,6 +74,8 @@ def parse():
                     help="water molecules of the XC workload (19 6-31G* functions each)")
     ap.add_argument("--mo-waters", type=int, default=6,
                     help="water molecules of the AO->MO workload (13 6-31G functions each)")
+    ap.add_argument("--grad-basis", default="6-31G",
+                    help="basis of the gradient workload (6-31G, or 6-31G* with d shells)")
     ap.add_argument("--opt-basis", default="6-31G",
                     help="basis of the optimize workload (6-31G, or 6-31G* with d shells)")
     ap.add_argument("--opt-waters", type=int, default=4, help="waters of the optimize workload")
@@ -687,22 +689,23 @@ def run_batch(args, rank, world):
 
 # ---------------------------------------------------------------------- gradient workload
 def run_gradient(args, rank, world):
-    """Analytic RHF gradient of a seeded (H2O)8 / 6-31G: time against one Fock build, and
-    central finite differences (h = 1e-4 bohr) on --fd-coords coordinates."""
+    """Analytic RHF gradient of a seeded (H2O)8 / 6-31G (or --grad-basis): time against one
+    Fock build, and central finite differences (h = 1e-4 bohr) on --fd-coords coordinates."""
     import torch
     from gaussium_gb300 import build, gradient, molecules
     from gaussium_gb300.driver import TimedFock
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     build.build()
+    basis = args.grad_basis
     mol = molecules.water_cluster(8, seed=8)
-    gradient.rhf_energy_gradient(molecules.water_cluster(1, seed=1))      # warm-up
+    gradient.rhf_energy_gradient(molecules.water_cluster(1, seed=1), basis)      # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e, g, res = gradient.rhf_energy_gradient(mol, "6-31G")
+    e, g, res = gradient.rhf_energy_gradient(mol, basis)
     torch.cuda.synchronize()
     t_total = time.perf_counter() - t0
     # gradient part alone, and one full Fock build, on the converged state
-    sb = molecules.shell_basis(mol, "6-31G")
+    sb = molecules.shell_basis(mol, basis)
     from gaussium_gb300.engine import JKEngine
     eng = JKEngine(sb, schwarz_thr=1e-14)
     fock_forms = {}
@@ -763,15 +766,15 @@ def run_gradient(args, rank, world):
         cp, cm = mol.coords.copy(), mol.coords.copy()
         cp[a, x] += h
         cm[a, x] -= h
-        ep = gradient.rhf_energy_gradient(molecules.Molecule(mol.symbols, cp), "6-31G", want_gradient=False)[0]
-        em = gradient.rhf_energy_gradient(molecules.Molecule(mol.symbols, cm), "6-31G", want_gradient=False)[0]
+        ep = gradient.rhf_energy_gradient(molecules.Molecule(mol.symbols, cp), basis, want_gradient=False)[0]
+        em = gradient.rhf_energy_gradient(molecules.Molecule(mol.symbols, cm), basis, want_gradient=False)[0]
         err = max(err, abs((ep - em) / (2 * h) - g[a, x]))
     line = {
         "metric": METRIC, "value": (t_eri_grad + t_one_grad) / t_fock,
         "unit": "gradient time / one Fock build", "n_gpus": world, "steps": 1, "warmup": 1,
         "ms_per_step": (t_eri_grad + t_one_grad) * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": f"RHF gradient (H2O)8/6-31G, {sb.nbf} functions",
+        "config": {"workload": f"RHF gradient (H2O)8/{basis}, {sb.nbf} functions",
                    "fd_coordinates_checked": int(ncoord), "fd_step_bohr": h},
         "energy": e, "max_abs_grad_minus_fd": err,
         "eri_gradient_ms": t_eri_grad * 1e3, "one_electron_gradient_ms": t_one_grad * 1e3,
