@@ -235,9 +235,9 @@ class BatchedRHF:
             plan = [(cls, s, e, split_forms(cls, prec, heavy))
                     for (cls, s, e), heavy in zip(self.segments, self.heavy)
                     if classes is None or cls in classes]
-            # heavy prefixes first, on the side stream; then every class's rest
+            # heavy prefixes first, on side 0; then every class's rest, alternating streams
             for heavy_pass in (True, False):
-                for cls, s, e, parts in plan:
+                for i, (cls, s, e, parts) in enumerate(plan):
                     for k, (form, first, count) in enumerate(parts):
                         if (k == 0 and len(parts) > 1) != heavy_pass:
                             continue
@@ -248,7 +248,7 @@ class BatchedRHF:
                             _lib.ptr(self.shell_mol), _lib.ptr(self.mol_base), _lib.ptr(self.mol_n),
                             _lib.ptr(dmax), self.mat_stride, m, base + (s + first) * 8,
                             _lib.ptr(P), _lib.ptr(J), 1, _lib.ptr(P), _lib.ptr(K), thr, lo, hi,
-                            lane.stream() if heavy_pass else st)
+                            lane.stream() if heavy_pass else lane.alternate(i))
                         _lib.check(rc, f"gs_fock_jk_batched{cls}")
         lane.join()
 

@@ -116,30 +116,36 @@ _SIDE = {}
 
 
 class HeavyLane:
-    """The heavy prefixes of a build's classes go to a second stream of the device, forked
-    from the caller's stream before their first launch and joined back by ``join``: their
-    few long blocks then run beside the class launches of the caller's stream instead of
-    leaving most SMs idle while they finish."""
+    """Side streams of a build, forked from the caller's stream before their first launch
+    and joined back by ``join``.  Side 0 takes the heavy prefixes of the classes: their few
+    long blocks then run beside the class launches instead of leaving most SMs idle while
+    they finish.  Side 1 takes every other class's launch of a plain (unpartitioned)
+    build, so that one class's last partial wave overlaps the next class's first."""
 
     def __init__(self, device, stream=None):
         d = indexed_device(device)
         self.main = stream or torch.cuda.current_stream(d)
         if d not in _SIDE:
-            _SIDE[d] = torch.cuda.Stream(device=d)
-        self.side = _SIDE[d]
-        self.forked = False
+            _SIDE[d] = (torch.cuda.Stream(device=d), torch.cuda.Stream(device=d))
+        self.sides = _SIDE[d]
+        self.forked = [False, False]
 
-    def stream(self):
-        """The side stream (as the C ABI takes it), forked on first use."""
-        if not self.forked:
-            self.side.wait_stream(self.main)
-            self.forked = True
-        return _lib.stream(self.side)
+    def stream(self, k=0):
+        """Side stream k (as the C ABI takes it), forked on first use."""
+        if not self.forked[k]:
+            self.sides[k].wait_stream(self.main)
+            self.forked[k] = True
+        return _lib.stream(self.sides[k])
+
+    def alternate(self, i):
+        """The stream of the i-th class launch of a plain build: the caller's or side 1."""
+        return _lib.stream(self.main) if i % 2 == 0 else self.stream(1)
 
     def join(self):
-        if self.forked:
-            self.main.wait_stream(self.side)
-            self.forked = False
+        for k in (0, 1):
+            if self.forked[k]:
+                self.main.wait_stream(self.sides[k])
+                self.forked[k] = False
 
 
 def _check_sizes():
@@ -361,9 +367,9 @@ class QuartetBatch:
         plan = [(cls, s, e, split_forms(cls, precision, heavy))
                 for (cls, s, e), heavy in zip(self.segments, self.heavy)
                 if classes is None or cls in classes]
-        # heavy prefixes first, on the side stream; then every class's rest on the caller's
+        # heavy prefixes first, on side 0; then every class's rest, alternating streams
         for heavy_pass in (True, False):
-            for cls, s, e, parts in plan:
+            for i, (cls, s, e, parts) in enumerate(plan):
                 for k, (form, first, count) in enumerate(parts):
                     if (k == 0 and len(parts) > 1) != heavy_pass:
                         continue
@@ -371,7 +377,7 @@ class QuartetBatch:
                     rc = L.gs_eri_blocks(*cls, precision | (form << 8), _lib.ptr(self.pairs.rec),
                                          _lib.ptr(prims), _lib.ptr(self.ds.comp_scale), n,
                                          base + (s + first) * WRITE_TASK, _lib.ptr(out),
-                                         lane.stream() if heavy_pass else st)
+                                         lane.stream() if heavy_pass else lane.alternate(i))
                     _lib.check(rc, f"gs_eri_blocks{cls}")
         lane.join()
         return out
@@ -550,9 +556,9 @@ class JKEngine:
             plan = [(cls, s, e, split_forms(cls, prec, heavy))
                     for (cls, s, e), heavy in zip(self.segments, self.heavy)
                     if classes is None or cls in classes]
-            # heavy prefixes first, on the side stream; then every class's rest
+            # heavy prefixes first, on side 0; then every class's rest, alternating streams
             for heavy_pass in (True, False):
-                for cls, s, e, parts in plan:
+                for i, (cls, s, e, parts) in enumerate(plan):
                     for k, (form, first, count) in enumerate(parts):
                         if (k == 0 and len(parts) > 1) != heavy_pass:
                             continue
@@ -562,7 +568,7 @@ class JKEngine:
                                           _lib.ptr(self.ds.func_off), self.sb.nshell, n, m,
                                           base + (s + first) * 8, _lib.ptr(pj_c), _lib.ptr(jbuf),
                                           nk, _lib.ptr(pk_c), _lib.ptr(kbuf), _lib.ptr(dmax), thr,
-                                          lo, hi, lane.stream() if heavy_pass else st)
+                                          lo, hi, lane.stream() if heavy_pass else lane.alternate(i))
                         _lib.check(rc, f"gs_fock_jk{cls}")
         lane.join()
         J = (jbuf + jbuf.T) if jbuf is not None else None
