@@ -1,9 +1,10 @@
 """Per-class kernel-form autotuner.
 
 A class (la lb|lc ld) whose total angular momentum lies in the overlap of the kernel
-families is built as the one-thread-per-quartet kernel, as the warp-per-quartet kernel
-and, where its narrow recursion levels leave lanes idle, as the warp kernel that pushes
-several primitive quartets through each pass (``gs_class_variants``).  Which is faster
+families is built as the one-thread-per-quartet kernel, as the warp-per-quartet kernel,
+where its narrow recursion levels leave lanes idle as the warp kernel that pushes several
+primitive quartets through each pass, and as the stacked warp kernel whose lanes each run
+their node record on several primitive quartets (``gs_class_variants``).  Which is faster
 depends on the workload, chiefly on the primitive counts of the quartets and on how much
 shared memory the grouped buffers take from occupancy.  The
 tuner times both forms of every such class on the caller's own task lists (CUDA events on
@@ -18,20 +19,20 @@ import torch
 
 from . import _lib
 
-THREAD, WARP, GROUPED, SPLIT, COOP = 1, 2, 3, 4, 5
+THREAD, WARP, GROUPED, SPLIT, COOP, STACKED = 1, 2, 3, 4, 5, 6
 NAMES = {THREAD: "thread", WARP: "warp", GROUPED: "warp-grouped", SPLIT: "thread-split",
-         COOP: "warp-cooperative"}
+         COOP: "warp-cooperative", STACKED: "warp-stacked"}
 
 
 def forms(cls, precision):
-    """Kernel forms built for a class: a subset of {THREAD, WARP, GROUPED}."""
+    """Kernel forms built for a class: a subset of {THREAD, WARP, GROUPED, STACKED}."""
     m = _lib.lib().gs_class_variants(*cls, precision)
     if m < 0:
         _lib.check(-m, f"gs_class_variants{cls}")
     # the split and cooperative forms serve the heavy quartets of a thread-form or warp-form
     # class (engine.split_forms); as whole-class forms they would leave most lanes idle on
     # light quartets
-    return [v for v in (THREAD, WARP, GROUPED) if m & (1 << (v - 1))]
+    return [v for v in (THREAD, WARP, GROUPED, STACKED) if m & (1 << (v - 1))]
 
 
 def describe(row):

@@ -38,7 +38,8 @@ int find_variants(int la, int lb, int lc, int ld, int prec) {
 // per quartet with several primitive quartets per VRR pass.  It rides in bits 8.. of the
 // precision argument of the class launchers; 4 = the thread form's code with one warp per
 // quartet over its primitive quartets (split form); 5 = the warp form's code with several
-// warps per quartet (cooperative form, per call only).
+// warps per quartet (cooperative form, per call only); 6 = the warp form with several
+// primitive quartets per lane (stacked form).
 int g_variant[3][3][3][3][2] = {};
 
 inline int pv(int la, int lb, int lc, int ld, int prec) {
@@ -46,11 +47,11 @@ inline int pv(int la, int lb, int lc, int ld, int prec) {
 }
 
 // The precision argument of the launch entry points: 64 or 32, optionally with an explicit
-// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp, 4 split, 5 cooperative; 0 =
-// the class's configured form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
+// kernel form in bits 8.. (1 thread, 2 warp, 3 grouped warp, 4 split, 5 cooperative, 6
+// stacked; 0 = the class's configured form).  Returns the launcher's precision-and-form word, or -1 if invalid or not built.
 int decode_precision(int la, int lb, int lc, int ld, int precision) {
     const int prec = precision & 0xff, form = precision >> 8;
-    if ((prec != 64 && prec != 32) || form < 0 || form > 5) return -1;
+    if ((prec != 64 && prec != 32) || form < 0 || form > 6) return -1;
     if (form == 0) return pv(la, lb, lc, ld, prec);
     if (!(find_variants(la, lb, lc, ld, prec) & (1 << (form - 1)))) return -1;
     return prec | (form << 8);
@@ -347,7 +348,9 @@ int gs_class_form(int la, int lb, int lc, int ld, int precision) {
 
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant) {
     if (!find_class(la, lb, lc, ld)) return GS_ERR_CLASS;
-    if ((precision != 64 && precision != 32) || variant < 0 || variant > 4) return GS_ERR_ARG;
+    // the cooperative form (5) takes host task counts only, so it is per call, not per class
+    if ((precision != 64 && precision != 32) || variant < 0 || variant > 6 || variant == 5)
+        return GS_ERR_ARG;
     if (variant && !(find_variants(la, lb, lc, ld, precision) & (1 << (variant - 1))))
         return GS_ERR_ARG;
     g_variant[la][lb][lc][ld][precision == 64 ? 0 : 1] = variant;

@@ -35,11 +35,17 @@ constexpr int kNCoef = 32;                    // coefficient slots per primitive
 // nodes with more terms (gen_eri.py ZERO_COEF; the i2p_4 slot, unused up to (dd|dd))
 constexpr int kZeroCoef = 15;
 constexpr int kSetupBatch = GS_SETUP_BATCH;   // primitive quartets prepared per setup round
+// primitive quartets per lane in the stacked form: FP32 nodes are cheap beside their record
+// decode and operand loads, so four share one decode; FP64 stacks two, for the independent
+// FMA chains
+template <typename T> constexpr int kStack = sizeof(T) == 8 ? 2 : 4;
 static_assert(kSetupBatch >= 1 && kSetupBatch <= 32, "one primitive quartet per lane at most");
 static_assert(kWideWarps >= 1 && kWideWarps <= 32, "warps per block");
 // VG: primitive quartets a warp pushes through the VRR node program at once (1, or the
-// class's WideProg::VGROUP for the grouped form).
-template <int LA, int LB, int LC, int LD, typename T, int VG = 1> struct WideLayout {
+// class's WideProg::VGROUP for the grouped form).  RQ: primitive quartets each lane runs its
+// node record on (1, or kStack for the stacked form): the ungrouped program, one record
+// decode for RQ quartets with RQ node buffers.
+template <int LA, int LB, int LC, int LD, typename T, int VG = 1, int RQ = 1> struct WideLayout {
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
     // primitive quartets set up per round: a grouped form with large node buffers prepares
@@ -50,14 +56,15 @@ template <int LA, int LB, int LC, int LD, typename T, int VG = 1> struct WideLay
     // large -- grouped with more than 1024 slots, or an ungrouped class of total angular
     // momentum 7 or more whose VRR buffers would outgrow the HRR's (measured: (dd|dp)
     // 17.7 -> 16.0 ms at 2,000,000 quartets; the smaller classes lose setup parallelism)
-    static constexpr int VRR32 = 32 * kNCoef + 32 * (G::L + 1) + VG * NVS;
+    static constexpr int VRR32 = 32 * kNCoef + 32 * (G::L + 1) + VG * RQ * NVS;
     static constexpr int HRR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
-    static constexpr int SB = kSetupBatch > 16 && ((VG > 1 && VG * NVS > 1024) ||
-                                                   (VG == 1 && G::L >= 7 && VRR32 > HRR_W))
+    static constexpr int SB = kSetupBatch > 16 && ((VG * RQ > 1 && VG * RQ * NVS > 1024) ||
+                                                   (VG * RQ == 1 && G::L >= 7 && VRR32 > HRR_W))
                                   ? 16 : kSetupBatch;
+    static_assert(SB % RQ == 0, "setup rounds hold whole stacks");
     static constexpr int SC = SB * kNCoef;                       // coefficients
     static constexpr int SF = SB * (G::L + 1);                   // Boys values
-    static constexpr int VRR = SC + SF + VG * NVS;
+    static constexpr int VRR = SC + SF + VG * RQ * NVS;
     // write/Schwarz epilogues need the HRR buffer and the scale vectors; the J/K epilogue
     // also a scaled copy of the block
     static constexpr int HR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
@@ -159,16 +166,67 @@ __device__ __forceinline__ void vrr_step(const uint4* __restrict__ vrec, int nof
     }
 }
 
+// One synchronisation step of the ungrouped node program for a stack of ng <= RQ primitive
+// quartets: lane j takes record j of every wave of 32, decodes it once and runs it on each
+// quartet of the stack (coefficients c + r kNCoef, node buffer nd + r NVS).  The quartets
+// are independent FMA chains, so the record's operand loads overlap without prefetching.
+// Nodes of one step never read one another, so each wave's results are stored before the
+// next wave's operands are read.
+template <int RQ, int NVS, typename T>
+__device__ __forceinline__ void vrr_step_rq(const uint4* __restrict__ vrec, int noff, int cnt,
+                                            int ng, const T* __restrict__ c, T* nd, int j) {
+    uint4 a = make_uint4(0, 0, 0, 0), b = a, na = a, nb = a;
+    int n = j;
+    bool act = n < cnt;
+    if (act) {
+        a = __ldg(vrec + 2 * (noff + n));
+        b = __ldg(vrec + 2 * (noff + n) + 1);
+    }
+    while (act) {
+        const bool nact = n + 32 < cnt;
+        if (nact) {                                  // record of the next wave
+            na = __ldg(vrec + 2 * (noff + n + 32));
+            nb = __ldg(vrec + 2 * (noff + n + 32) + 1);
+        }
+        const int nt = a.x >> 16, out = a.x & 0xffff;
+        const int k0 = a.y >> 16, s0 = a.y & 0xffff, k1 = a.z >> 16, s1 = a.z & 0xffff;
+        const int k2 = a.w >> 16, s2 = a.w & 0xffff, k3 = b.x >> 16, s3 = b.x & 0xffff;
+        const int k4 = b.y >> 16, s4 = b.y & 0xffff;
+        T r[RQ];
+#pragma unroll
+        for (int q = 0; q < RQ; ++q) {
+            if (q < ng) {
+                const T* __restrict__ cq = c + q * kNCoef;
+                const T* vq = nd + q * NVS;
+                T v = cq[k0] * vq[s0];
+                v = fma(cq[k1], vq[s1], v);
+                if (nt > 2) v = fma(cq[k2], vq[s2], v);
+                if (nt > 3) v = fma(cq[k3], vq[s3], v);
+                if (nt > 4) v = fma(cq[k4], vq[s4], v);
+                r[q] = v;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < RQ; ++q)
+            if (q < ng) nd[q * NVS + out] = r[q];
+        a = na;
+        b = nb;
+        act = nact;
+        n += 32;
+    }
+}
+
 // Contracted [e0|f0] targets of primitive quartets first, first + stride, ... of the
 // quartet (set up Lay::SB at a time): target lane + 32 k is added to acc[k].
-template <int LA, int LB, int LC, int LD, typename T, int VG>
+template <int LA, int LB, int LC, int LD, typename T, int VG, int RQ = 1>
 __device__ __forceinline__ void wide_contract(const PairRec& B, const PairRec& K,
                                               const PrimRec<T>* __restrict__ prims,
                                               T* __restrict__ sm, int lane, int first, int stride,
                                               T* __restrict__ acc) {
+    static_assert(VG == 1 || RQ == 1, "grouped and stacked forms are separate");
     using G = ClassGen<LA, LB, LC, LD>;
     using W = WideProg<LA, LB, LC, LD>;
-    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG, RQ>;
     constexpr int L = G::L;
     constexpr int NACC = G::NACC;
     constexpr int NACCW = (NACC + 31) / 32;
@@ -194,7 +252,41 @@ __device__ __forceinline__ void wide_contract(const PairRec& B, const PairRec& K
         }
         __syncwarp();
         const int nb = min(Lay::SB, nmine - base);
-        if constexpr (VG == 1) {
+        if constexpr (RQ > 1) {
+        // RQ primitive quartets at a time, each with its own node buffer; lane j runs record
+        // j of every wave on all of them.  The accumulators add the quartets in order, so
+        // the sums match the one-at-a-time form.
+        for (int j0 = 0; j0 < nb; j0 += RQ) {
+            const int ng = min(RQ, nb - j0);
+            for (int x = lane; x < ng * (L + 1); x += 32) {
+                const int q = x / (L + 1), m = x - q * (L + 1);
+                node[q * NVS + m] = sF[(j0 + q) * (L + 1) + m];
+            }
+            __syncwarp();
+            int noff = __ldg(vseg), cnt = __ldg(vseg + 1);
+            for (int s = 0; s < NVSEG; ++s) {
+                int noff_n = 0, cnt_n = 0;
+                if (s + 1 < NVSEG) {
+                    noff_n = __ldg(vseg + 4 * (s + 1));
+                    cnt_n = __ldg(vseg + 4 * (s + 1) + 1);
+                }
+                if (s > 0) __syncwarp();
+                vrr_step_rq<RQ, NVS, T>(vrec, noff, cnt, ng, sC + j0 * kNCoef, node, lane);
+                noff = noff_n;
+                cnt = cnt_n;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < NACCW; ++k) {
+                const int t = lane + 32 * k;
+                if (t < NACC) {
+                    const int v = __ldg(vtgt + t);
+                    for (int q = 0; q < ng; ++q) acc[k] += node[q * NVS + v];
+                }
+            }
+            __syncwarp();
+        }
+        } else if constexpr (VG == 1) {
         for (int j = 0; j < nb; ++j) {
             const T* __restrict__ c = sC + j * kNCoef;
             if (lane <= L) node[lane] = sF[j * (L + 1) + lane];
@@ -316,7 +408,7 @@ __device__ __forceinline__ void wide_hrr(const PairRec& B, const PairRec& K, T* 
 
 // Evaluate one contracted quartet with one warp; on return sm[0 .. HSIZE) holds the HRR
 // buffer whose output slots are W::outslot().
-template <int LA, int LB, int LC, int LD, typename T, int VG>
+template <int LA, int LB, int LC, int LD, typename T, int VG, int RQ = 1>
 __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
                                              const PrimRec<T>* __restrict__ prims,
                                              T* __restrict__ sm, int lane) {
@@ -325,7 +417,7 @@ __device__ __forceinline__ void wide_quartet(const PairRec& B, const PairRec& K,
     T acc[NACCW];
 #pragma unroll
     for (int k = 0; k < NACCW; ++k) acc[k] = T(0);
-    wide_contract<LA, LB, LC, LD, T, VG>(B, K, prims, sm, lane, 0, 1, acc);
+    wide_contract<LA, LB, LC, LD, T, VG, RQ>(B, K, prims, sm, lane, 0, 1, acc);
 #pragma unroll
     for (int k = 0; k < NACCW; ++k) {
         const int t = lane + 32 * k;
@@ -362,9 +454,9 @@ __device__ __forceinline__ void wide_write_out(const WriteArgs& a, const WriteTa
     }
 }
 
-template <int LA, int LB, int LC, int LD, typename T, int VG>
+template <int LA, int LB, int LC, int LD, typename T, int VG, int RQ = 1>
 __global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_write(const WriteArgs a) {
-    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG, RQ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_W;
@@ -373,7 +465,7 @@ __global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_write(co
     const WriteTask task = a.tasks[t];
     const PairRec B = a.pairs[task.bra];
     const PairRec K = a.pairs[task.ket];
-    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_quartet<LA, LB, LC, LD, T, VG, RQ>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     wide_write_out<LA, LB, LC, LD, T>(a, task, B, K, sm, lane);
 }
 
@@ -463,27 +555,27 @@ __device__ __forceinline__ void wide_jk_digest(const JKArgs& a, const int2& task
     }
 }
 
-template <int LA, int LB, int LC, int LD, typename T, int VG>
+template <int LA, int LB, int LC, int LD, typename T, int VG, int RQ = 1>
 __device__ __forceinline__ void wide_jk_task(const JKArgs& a, int t, T* __restrict__ sm, int lane) {
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
     if (!jk_keep(a, B, K)) return;                 // warp-uniform
-    wide_quartet<LA, LB, LC, LD, T, VG>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
+    wide_quartet<LA, LB, LC, LD, T, VG, RQ>(B, K, (const PrimRec<T>*)a.prims, sm, lane);
     wide_jk_digest<LA, LB, LC, LD, T>(a, task, B, K, sm, lane);
 }
 
 // One warp per task; with a task count on the device (after a partition) the grid is
 // capped and each warp strides over the tasks.
-template <int LA, int LB, int LC, int LD, typename T, int VG>
+template <int LA, int LB, int LC, int LD, typename T, int VG, int RQ = 1>
 __global__ void __launch_bounds__(32 * kWideWarps, GS_WIDE_MINB) k_wide_jk(const JKArgs a) {
-    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG, RQ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     T* sm = reinterpret_cast<T*>(smem_raw) + (size_t)warp * Lay::WARP_JK;
     const int ntask = a.ntask_dev ? *a.ntask_dev : a.ntask;
     for (int t = blockIdx.x * kWideWarps + warp; t < ntask; t += gridDim.x * kWideWarps) {
-        wide_jk_task<LA, LB, LC, LD, T, VG>(a, t, sm, lane);
+        wide_jk_task<LA, LB, LC, LD, T, VG, RQ>(a, t, sm, lane);
         __syncwarp();
     }
 }
@@ -619,28 +711,28 @@ int set_smem(size_t sh) {
     return 0;
 }
 
-template <int LA, int LB, int LC, int LD, int PREC, int VG = 1>
+template <int LA, int LB, int LC, int LD, int PREC, int VG = 1, int RQ = 1>
 int launch_wide(int kind, const void* args, cudaStream_t st) {
     using T = typename std::conditional<PREC == 64, double, float>::type;
-    using Lay = WideLayout<LA, LB, LC, LD, T, VG>;
+    using Lay = WideLayout<LA, LB, LC, LD, T, VG, RQ>;
     constexpr int TPB = 32 * kWideWarps;
     if (kind == GS_KIND_WRITE) {
         const WriteArgs& a = *(const WriteArgs*)args;
         if (a.ntask <= 0) return 0;
-        auto k = k_wide_write<LA, LB, LC, LD, T, VG>;
-        if (set_smem<k_wide_write<LA, LB, LC, LD, T, VG>>(Lay::BYTES_W)) return GS_ERR_CUDA;
+        auto k = k_wide_write<LA, LB, LC, LD, T, VG, RQ>;
+        if (set_smem<k_wide_write<LA, LB, LC, LD, T, VG, RQ>>(Lay::BYTES_W)) return GS_ERR_CUDA;
         k<<<(a.ntask + kWideWarps - 1) / kWideWarps, TPB, Lay::BYTES_W, st>>>(a);
     } else if (kind == GS_KIND_JK) {
         const JKArgs& a = *(const JKArgs*)args;
         if (a.ntask <= 0) return 0;
-        auto k = k_wide_jk<LA, LB, LC, LD, T, VG>;
-        if (set_smem<k_wide_jk<LA, LB, LC, LD, T, VG>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
+        auto k = k_wide_jk<LA, LB, LC, LD, T, VG, RQ>;
+        if (set_smem<k_wide_jk<LA, LB, LC, LD, T, VG, RQ>>(Lay::BYTES_JK)) return GS_ERR_CUDA;
         int grid = (a.ntask + kWideWarps - 1) / kWideWarps;
         if (a.ntask_dev && grid > kWideDeviceCountBlocksPerSM * sm_count())
             grid = kWideDeviceCountBlocksPerSM * sm_count();
         k<<<grid, TPB, Lay::BYTES_JK, st>>>(a);
     } else if (kind == GS_KIND_SCHWARZ) {
-        if constexpr (LA == LC && LB == LD && PREC == 64 && VG == 1) {
+        if constexpr (LA == LC && LB == LD && PREC == 64 && VG == 1 && RQ == 1) {
             const SchwarzArgs& a = *(const SchwarzArgs*)args;
             if (a.npair <= 0) return 0;
             auto k = k_wide_schwarz<LA, LB, double>;

@@ -42,7 +42,7 @@ HEAVY_PRIM_QUARTETS = 32
 # sums added in shared memory before one HRR.  The class's time would otherwise have a floor at its heaviest quartet,
 # walked by one warp while the other warps of the launch have finished.
 COOP_PRIM_QUARTETS = 128
-THREAD_FORM, WARP_FORM, GROUPED_FORM, SPLIT_FORM, COOP_FORM = 1, 2, 3, 4, 5
+THREAD_FORM, WARP_FORM, GROUPED_FORM, SPLIT_FORM, COOP_FORM, STACKED_FORM = 1, 2, 3, 4, 5, 6
 # (class, precision) pairs whose heavy quartets stay on the class's own form (set by the
 # autotuner where that measured faster)
 SPLIT_OFF = set()
@@ -80,7 +80,7 @@ def split_forms(cls, precision, heavy):
     form = _lib.lib().gs_class_form(*cls, precision)
     if form == THREAD_FORM:
         h, hform = heavy[0], SPLIT_FORM
-    elif form in (WARP_FORM, GROUPED_FORM):
+    elif form in (WARP_FORM, GROUPED_FORM, STACKED_FORM):
         h, hform = heavy[1], COOP_FORM
     else:
         h, hform = 0, 0

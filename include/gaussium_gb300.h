@@ -55,26 +55,30 @@ int gs_class_available(int la, int lb, int lc, int ld);
  * one-thread-per-quartet kernel, bit 1 the warp-per-quartet kernel, bit 2 the warp kernel
  * that runs several primitive quartets through each recursion pass, bit 3 the split form
  * (the thread kernel's code, one warp per quartet over its primitive quartets), bit 4 the
- * cooperative form (the warp kernel's code, up to eight warps per quartet); negative status on a
- * bad class or precision.  No reference counterpart (the reference has one code path). */
+ * cooperative form (the warp kernel's code, up to eight warps per quartet), bit 5 the
+ * stacked form (the warp kernel with each lane's node record run on several primitive
+ * quartets: 2 in FP64, 4 in FP32); negative status on a bad class or precision.  No
+ * reference counterpart (the reference has one code path). */
 int gs_class_variants(int la, int lb, int lc, int ld, int precision);
 
 /* Chooses the kernel form later calls use for (la lb|lc ld) in that precision, process-wide:
  * 0 = the built-in default by total angular momentum, 1 = thread per quartet, 2 = warp per
- * quartet, 3 = grouped warp per quartet (a form the class was not built with is
- * GS_ERR_ARG).  Results do not depend on the form beyond rounding; the autotuner times the
- * forms on the caller's task lists.  No reference counterpart. */
+ * quartet, 3 = grouped warp per quartet, 4 = split, 6 = stacked warp per quartet (a form
+ * the class was not built with, or the per-call cooperative form 5, is GS_ERR_ARG).
+ * Results do not depend on the form beyond rounding; the autotuner times the forms on the
+ * caller's task lists.  No reference counterpart. */
 int gs_set_class_variant(int la, int lb, int lc, int ld, int precision, int variant);
 
-/* The kernel form (1 thread, 2 warp, 3 grouped warp) a launch of (la lb|lc ld) in that
- * precision uses with no explicit form: the configured variant, or the built-in default.
+/* The kernel form (1 thread, 2 warp, 3 grouped warp, 4 split, 6 stacked) a launch of
+ * (la lb|lc ld) in that precision uses with no explicit form: the configured variant, or
+ * the built-in default.
  * The precision argument of gs_eri_blocks, gs_fock_jk and gs_fock_jk_batched may carry an
- * explicit form in its bits 8.. (precision | form << 8, forms 1-5 as gs_class_variants'
- * bits 0-4) for that call only; the engine uses it to run the quartets with many primitive
+ * explicit form in its bits 8.. (precision | form << 8, forms 1-6 as gs_class_variants'
+ * bits 0-5) for that call only; the engine uses it to run the quartets with many primitive
  * quartets (the heavy prefix of a class's task list, sorted by descending primitive work)
  * in the split form where the class runs one thread per quartet, and in the cooperative
- * form where it runs one warp per quartet.  The cooperative form takes host task counts
- * only.  Negative status on a bad class or precision.  No reference counterpart. */
+ * form where it runs one warp per quartet (warp, grouped or stacked).  The cooperative form
+ * takes host task counts only.  Negative status on a bad class or precision.  No reference counterpart. */
 int gs_class_form(int la, int lb, int lc, int ld, int precision);
 
 /* K0 shell-pair builder.  Replaces the per-primitive-quartet prologue of
