@@ -210,11 +210,10 @@ def pair_groups(sizes, lanes=32):
     m = -(-n // 4) * 4
     sz = np.zeros(m, dtype=np.int64)
     sz[:n] = sizes
-    quad = sz.reshape(-1, 4).sum(1) <= lanes
-    half = sz.reshape(-1, 2).sum(1) <= lanes
-    i = np.arange(m)
-    q, r = i // 4, i % 4
-    start = (r == 0) | ((r == 2) & ~quad[q]) | (((r == 1) | (r == 3)) & ~quad[q] & ~half[i // 2])
+    quad = np.repeat(sz.reshape(-1, 4).sum(1) <= lanes, 4)
+    half = np.repeat(sz.reshape(-1, 2).sum(1) <= lanes, 2)
+    r = np.tile(np.arange(4), m // 4)
+    start = (r == 0) | ((r == 2) & ~quad) | ((r & 1).astype(bool) & ~quad & ~half)
     out = np.flatnonzero(start[:n]).astype(np.int32)
     return np.concatenate([out, np.array([n], dtype=np.int32)])
 
@@ -281,9 +280,8 @@ class PairSet:
 
 
 # ---------------------------------------------------------------------- shell-quartet blocks
-def canonicalize(l4):
-    """Per quartet of angular momenta (n,4): canonical order (bra pair class >= ket pair
-    class, la >= lb, lc >= ld), the 3-bit permutation code, and index maps."""
+def _canonicalize_rows(l4):
+    """canonicalize, evaluated row by row from the rule (the table below is built from it)."""
     la, lb, lc, ld = l4[:, 0], l4[:, 1], l4[:, 2], l4[:, 3]
     s_ab = la < lb
     s_cd = lc < ld
@@ -299,6 +297,28 @@ def canonicalize(l4):
     return pos, code.astype(np.int32), np.where(s_bk, pc2, pc1), np.where(s_bk, pc1, pc2)
 
 
+# canonicalize's results and the block size for each of the 81 (la, lb, lc, ld) with l <= 2,
+# indexed by ((la*3 + lb)*3 + lc)*3 + ld: a gather per quartet instead of a dozen
+# elementwise passes over the batch
+_L4_ALL = np.array([[a, b, c, d] for a in range(3) for b in range(3) for c in range(3)
+                    for d in range(3)], dtype=np.int64)
+_CANON_LUT = _canonicalize_rows(_L4_ALL)
+_SIZE_LUT = np.prod(NCART[_L4_ALL], axis=1)
+
+
+def _l4_index(l4):
+    l4 = np.asarray(l4, dtype=np.int64)
+    return ((l4[:, 0] * 3 + l4[:, 1]) * 3 + l4[:, 2]) * 3 + l4[:, 3]
+
+
+def canonicalize(l4):
+    """Per quartet of angular momenta (n,4): canonical order (bra pair class >= ket pair
+    class, la >= lb, lc >= ld), the 3-bit permutation code, and index maps."""
+    i = _l4_index(l4)
+    pos, code, pcb, pck = _CANON_LUT
+    return pos[i], code[i], pcb[i], pck[i]
+
+
 class QuartetBatch:
     """A batch of shell quartets (n,4 shell indices, any order) evaluated into one flat f64
     buffer: quartet q's block occupies out[off[q] : off[q] + na*nb*nc*nd] in the caller's
@@ -311,9 +331,10 @@ class QuartetBatch:
         check_shell_indices(q, sb.nshell, "shell quartets")
         n = len(q)
         l4 = sb.l[q]
-        pos, code, pcb, pck = canonicalize(l4)
+        li = _l4_index(l4)
+        pos, code, pcb, pck = (x[li] for x in _CANON_LUT)
         qc = np.take_along_axis(q, pos, axis=1)          # canonical shells
-        size = np.prod(NCART[l4], axis=1)
+        size = _SIZE_LUT[li]
         off = np.zeros(n + 1, dtype=np.int64)
         off[1:] = np.cumsum(size)
         self.n = n
@@ -328,8 +349,22 @@ class QuartetBatch:
         cls = pcb * 6 + pck
         # within a class, most primitive quartets first (the longest blocks start first, so
         # the short ones fill the end of the launch), equal (K_bra, K_ket) kept together so
-        # that the lanes of a warp run the same loop trip counts
-        order = np.lexsort((-nk, -nb, -(nb * nk), cls))
+        # that the lanes of a warp run the same loop trip counts: one packed key (class,
+        # then descending nb*nk, nb, nk) and a stable sort, the order of a lexsort on the four
+        wb = int(nb.max()).bit_length() if n else 1
+        wk = int(nk.max()).bit_length() if n else 1
+        ww = int((nb * nk).max()).bit_length() if n else 1
+        key = cls.astype(np.int64)
+        key = (key << ww) | ((1 << ww) - 1 - nb * nk)
+        key = (key << wb) | ((1 << wb) - 1 - nb)
+        key = (key << wk) | ((1 << wk) - 1 - nk)
+        wi = int(n).bit_length()
+        if 6 + ww + wb + wk + wi <= 62:
+            # the index as the last key field makes every key distinct: a plain value sort
+            # gives the stable order (and is faster than a stable argsort)
+            order = np.sort((key << wi) | np.arange(n, dtype=np.int64)) & ((1 << wi) - 1)
+        else:
+            order = np.argsort(key, kind="stable")
         tasks = np.zeros(n, dtype=WRITE_TASK_DTYPE)
         tasks["bra"] = order
         tasks["ket"] = order + n
