@@ -141,10 +141,13 @@ def generate():
         tag = "".join(map(str, cls))
         thread = sum(cls) <= GRAD_THREAD_LMAX
         inc = '#include "eri_grad_%s.h"\n' % tag + ('#include "eri_gradt_%s.h"\n' % tag if thread else "")
-        body = ('    if (thread) return gs::launch_grad_thread<%d, %d, %d, %d>(a, st);\n' % cls
-                if thread else '    (void)thread;\n')
+        # form: 1 thread per quartet, 2 warp per quartet, 3 split (the thread code, one warp
+        # per quartet); the C entry checks that the thread forms exist for the class
+        body = ('    if (form == 1) return gs::launch_grad_thread<%d, %d, %d, %d>(a, st);\n'
+                '    if (form == 3) return gs::launch_grad_split<%d, %d, %d, %d>(a, st);\n'
+                % (cls + cls) if thread else '    (void)form;\n')
         code = ('#include "eri_grad.cuh"\n%s'
-                'int gs_grad_launch_%s(const gs::GradArgs& a, bool thread, cudaStream_t st) {\n%s'
+                'int gs_grad_launch_%s(const gs::GradArgs& a, int form, cudaStream_t st) {\n%s'
                 '    return gs::launch_grad<%d, %d, %d, %d>(a, st);\n}\n' % (inc, tag, body, *cls))
         path = os.path.join(GEN, f"eri_grad_k_{tag}.cu")
         if not os.path.exists(path) or open(path).read() != code:

@@ -6,7 +6,7 @@
 #include "eri_grad_list.h"
 
 #define GS_GDECL(A, B, C, D) \
-    int gs_grad_launch_##A##B##C##D(const gs::GradArgs&, bool, cudaStream_t);
+    int gs_grad_launch_##A##B##C##D(const gs::GradArgs&, int, cudaStream_t);
 GS_FOR_EACH_GRAD(GS_GDECL)
 #undef GS_GDECL
 
@@ -39,22 +39,39 @@ extern "C" int gs_set_eri_grad_variant(int la, int lb, int lc, int ld, int varia
     return GS_OK;
 }
 
+extern "C" int gs_eri_grad_form(int la, int lb, int lc, int ld, int form, const void* pair_rec,
+                                const void* prim64, const double* comp_scale, const int* func_off,
+                                const int* shell_atom, int ntask, const int* tasks, int nbf,
+                                int natom, const double* density, double* grad, void* stream) {
+    if (ntask < 0 || nbf <= 0 || natom <= 0 || !pair_rec || !prim64 || !comp_scale || !func_off ||
+        !shell_atom || (ntask > 0 && !tasks) || !density || !grad || form < 0 || form > 3)
+        return GS_ERR_ARG;
+    if (!valid_class(la, lb, lc, ld)) return GS_ERR_CLASS;
+    if ((form == 1 || form == 3) && !has_thread(la, lb, lc, ld)) return GS_ERR_ARG;
+    gs::GradArgs a{(const gs::PairRec*)pair_rec, (const gs::PrimRec<double>*)prim64, comp_scale,
+                   func_off, shell_atom, (const int2*)tasks, ntask, nbf, density, grad, natom};
+    cudaStream_t st = (cudaStream_t)stream;
+    if (form == 0) {
+        const int v = g_grad_variant[la][lb][lc][ld];
+        form = has_thread(la, lb, lc, ld) && (v ? v == 1 : la + lb + lc + ld <= 2) ? 1 : 2;
+    }
+#define GS_GL(A, B, C, D) \
+    if (la == A && lb == B && lc == C && ld == D) return gs_grad_launch_##A##B##C##D(a, form, st);
+    GS_FOR_EACH_GRAD(GS_GL)
+#undef GS_GL
+    return GS_ERR_CLASS;
+}
+
 extern "C" int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec, const void* prim64,
                            const double* comp_scale, const int* func_off, const int* shell_atom,
                            int ntask, const int* tasks, int nbf, int natom, const double* density,
                            double* grad, void* stream) {
-    if (ntask < 0 || nbf <= 0 || natom <= 0 || !pair_rec || !prim64 || !comp_scale || !func_off ||
-        !shell_atom || (ntask > 0 && !tasks) || !density || !grad)
-        return GS_ERR_ARG;
-    if (!valid_class(la, lb, lc, ld)) return GS_ERR_CLASS;
-    gs::GradArgs a{(const gs::PairRec*)pair_rec, (const gs::PrimRec<double>*)prim64, comp_scale,
-                   func_off, shell_atom, (const int2*)tasks, ntask, nbf, density, grad, natom};
-    cudaStream_t st = (cudaStream_t)stream;
+    return gs_eri_grad_form(la, lb, lc, ld, 0, pair_rec, prim64, comp_scale, func_off, shell_atom,
+                            ntask, tasks, nbf, natom, density, grad, stream);
+}
+
+extern "C" int gs_eri_grad_class_form(int la, int lb, int lc, int ld) {
+    if (!valid_class(la, lb, lc, ld)) return -GS_ERR_CLASS;
     const int v = g_grad_variant[la][lb][lc][ld];
-    const bool thread = has_thread(la, lb, lc, ld) && (v ? v == 1 : la + lb + lc + ld <= 2);
-#define GS_GL(A, B, C, D) \
-    if (la == A && lb == B && lc == C && ld == D) return gs_grad_launch_##A##B##C##D(a, thread, st);
-    GS_FOR_EACH_GRAD(GS_GL)
-#undef GS_GL
-    return GS_ERR_CLASS;
+    return has_thread(la, lb, lc, ld) && (v ? v == 1 : la + lb + lc + ld <= 2) ? 1 : 2;
 }

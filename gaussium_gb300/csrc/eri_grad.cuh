@@ -278,6 +278,95 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
 constexpr int kGradThreads = 128;
 constexpr int kGradSmemAtoms = 2048;
 
+// HRR, contraction with the RHF weights and the atomic adds of one quartet whose weighted
+// contraction sets are in H[0 .. NACC).  With warp_sum, lanes of a full warp whose quartets
+// share an atom at a centre sum first and one lane adds (every lane of the warp must call
+// it); without, each caller adds its own (a single lane may call it).
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void grad_finish(const GradArgs& a, const int2 task, const PairRec& B,
+                                            const PairRec& K, double* H, double* dst,
+                                            bool warp_sum) {
+    using W = GradThread<LA, LB, LC, LD>;
+    constexpr int NA = (LA + 1) * (LA + 2) / 2, NB = (LB + 1) * (LB + 2) / 2;
+    constexpr int NC = (LC + 1) * (LC + 2) / 2, ND = (LD + 1) * (LD + 2) / 2;
+    const double dv[6] = {B.ABx, B.ABy, B.ABz, K.ABx, K.ABy, K.ABz};
+    W::hrr(H, dv);
+    const int fa = a.func_off[B.sa], fb = a.func_off[B.sb];
+    const int fc = a.func_off[K.sa], fd = a.func_off[K.sb];
+    const int nbf = a.nbf;
+    const double* Pm = a.P;
+    double pab[NA * NB], pcd[NC * ND], pac[NA * NC], pbd[NB * ND], pad[NA * ND], pbc[NB * NC];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+#pragma unroll
+        for (int j = 0; j < NB; ++j) pab[i * NB + j] = Pm[(fa + i) * nbf + fb + j];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) pac[i * NC + j] = Pm[(fa + i) * nbf + fc + j];
+#pragma unroll
+        for (int j = 0; j < ND; ++j) pad[i * ND + j] = Pm[(fa + i) * nbf + fd + j];
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+#pragma unroll
+        for (int j = 0; j < ND; ++j) pbd[i * ND + j] = Pm[(fb + i) * nbf + fd + j];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) pbc[i * NC + j] = Pm[(fb + i) * nbf + fc + j];
+    }
+#pragma unroll
+    for (int i = 0; i < NC; ++i)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) pcd[i * ND + j] = Pm[(fc + i) * nbf + fd + j];
+    double cs0[NA], cs1[NB], cs2[NC], cs3[ND];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) cs0[i] = a.comp_scale[6 * B.sa + i];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) cs1[i] = a.comp_scale[6 * B.sb + i];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) cs2[i] = a.comp_scale[6 * K.sa + i];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) cs3[i] = a.comp_scale[6 * K.sb + i];
+    double w = 8.0;
+    if (B.sa == B.sb) w *= 0.5;
+    if (K.sa == K.sb) w *= 0.5;
+    if (task.x == task.y) w *= 0.5;
+    double g[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) g[k] = 0.0;
+    W::contract(H, w, pab, pcd, pac, pbd, pad, pbc, cs0, cs1, cs2, cs3, g);
+    const int at[4] = {a.shell_atom[B.sa], a.shell_atom[B.sb], a.shell_atom[K.sa],
+                       a.shell_atom[K.sb]};
+    // per-centre contributions (D by translational invariance); when the whole warp is
+    // active and every lane has the same atom at a centre (neighbouring tasks usually
+    // share their bra pair), the warp sums first and one lane adds
+    double gc[4][3];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        gc[0][x] = g[x];
+        gc[1][x] = g[3 + x];
+        gc[2][x] = g[6 + x];
+        gc[3][x] = -(g[x] + g[3 + x] + g[6 + x]);
+    }
+    const unsigned act = warp_sum ? __activemask() : 0u;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int cen = 0; cen < 4; ++cen) {
+        const bool uniform = warp_sum && act == 0xffffffffu &&
+                             __all_sync(act, at[cen] == __shfl_sync(act, at[cen], 0));
+        if (uniform) {
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                double v = gc[cen][x];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(act, v, o);
+                if (lane == 0) atomicAdd(dst + 3 * at[cen] + x, v);
+            }
+        } else {
+#pragma unroll
+            for (int x = 0; x < 3; ++x) atomicAdd(dst + 3 * at[cen] + x, gc[cen][x]);
+        }
+    }
+}
+
 template <int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs a) {
     using W = GradThread<LA, LB, LC, LD>;
@@ -310,83 +399,7 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
             c[35] = 5.0 * c[28];               // 5/(2(p+q)), raised (dd|..) classes
             W::prim(c, n, H);
         }
-        const double dv[6] = {B.ABx, B.ABy, B.ABz, K.ABx, K.ABy, K.ABz};
-        W::hrr(H, dv);
-        const int fa = a.func_off[B.sa], fb = a.func_off[B.sb];
-        const int fc = a.func_off[K.sa], fd = a.func_off[K.sb];
-        const int nbf = a.nbf;
-        const double* Pm = a.P;
-        double pab[NA * NB], pcd[NC * ND], pac[NA * NC], pbd[NB * ND], pad[NA * ND], pbc[NB * NC];
-#pragma unroll
-        for (int i = 0; i < NA; ++i) {
-#pragma unroll
-            for (int j = 0; j < NB; ++j) pab[i * NB + j] = Pm[(fa + i) * nbf + fb + j];
-#pragma unroll
-            for (int j = 0; j < NC; ++j) pac[i * NC + j] = Pm[(fa + i) * nbf + fc + j];
-#pragma unroll
-            for (int j = 0; j < ND; ++j) pad[i * ND + j] = Pm[(fa + i) * nbf + fd + j];
-        }
-#pragma unroll
-        for (int i = 0; i < NB; ++i) {
-#pragma unroll
-            for (int j = 0; j < ND; ++j) pbd[i * ND + j] = Pm[(fb + i) * nbf + fd + j];
-#pragma unroll
-            for (int j = 0; j < NC; ++j) pbc[i * NC + j] = Pm[(fb + i) * nbf + fc + j];
-        }
-#pragma unroll
-        for (int i = 0; i < NC; ++i)
-#pragma unroll
-            for (int j = 0; j < ND; ++j) pcd[i * ND + j] = Pm[(fc + i) * nbf + fd + j];
-        double cs0[NA], cs1[NB], cs2[NC], cs3[ND];
-#pragma unroll
-        for (int i = 0; i < NA; ++i) cs0[i] = a.comp_scale[6 * B.sa + i];
-#pragma unroll
-        for (int i = 0; i < NB; ++i) cs1[i] = a.comp_scale[6 * B.sb + i];
-#pragma unroll
-        for (int i = 0; i < NC; ++i) cs2[i] = a.comp_scale[6 * K.sa + i];
-#pragma unroll
-        for (int i = 0; i < ND; ++i) cs3[i] = a.comp_scale[6 * K.sb + i];
-        double w = 8.0;
-        if (B.sa == B.sb) w *= 0.5;
-        if (K.sa == K.sb) w *= 0.5;
-        if (task.x == task.y) w *= 0.5;
-        double g[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) g[k] = 0.0;
-        W::contract(H, w, pab, pcd, pac, pbd, pad, pbc, cs0, cs1, cs2, cs3, g);
-        const int at[4] = {a.shell_atom[B.sa], a.shell_atom[B.sb], a.shell_atom[K.sa],
-                           a.shell_atom[K.sb]};
-        double* dst = shared_sum ? sg : a.grad;
-        // per-centre contributions (D by translational invariance); when the whole warp is
-        // active and every lane has the same atom at a centre (neighbouring tasks usually
-        // share their bra pair), the warp sums first and one lane adds
-        double gc[4][3];
-#pragma unroll
-        for (int x = 0; x < 3; ++x) {
-            gc[0][x] = g[x];
-            gc[1][x] = g[3 + x];
-            gc[2][x] = g[6 + x];
-            gc[3][x] = -(g[x] + g[3 + x] + g[6 + x]);
-        }
-        const unsigned act = __activemask();
-        const int lane = threadIdx.x & 31;
-#pragma unroll
-        for (int cen = 0; cen < 4; ++cen) {
-            const bool uniform =
-                act == 0xffffffffu && __all_sync(act, at[cen] == __shfl_sync(act, at[cen], 0));
-            if (uniform) {
-#pragma unroll
-                for (int x = 0; x < 3; ++x) {
-                    double v = gc[cen][x];
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(act, v, o);
-                    if (lane == 0) atomicAdd(dst + 3 * at[cen] + x, v);
-                }
-            } else {
-#pragma unroll
-                for (int x = 0; x < 3; ++x) atomicAdd(dst + 3 * at[cen] + x, gc[cen][x]);
-            }
-        }
+        grad_finish<LA, LB, LC, LD>(a, task, B, K, H, shared_sum ? sg : a.grad, true);
     }
     if (shared_sum) {
         __syncthreads();
@@ -403,6 +416,52 @@ int launch_grad_thread(const GradArgs& a, cudaStream_t st) {
         return GS_ERR_CUDA;
     k_eri_grad_thread<LA, LB, LC, LD><<<(a.ntask + kGradThreads - 1) / kGradThreads, kGradThreads,
                                         sh, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+}
+
+// Split form of the thread kernel, for quartets with many primitive quartets (the heavy
+// prefix of a class's task list, sorted by descending primitive work): one warp per
+// quartet, its lanes taking the primitive quartets 32 apart with the same generated code,
+// a butterfly sum of the weighted contraction sets, then lane 0 finishes the quartet.
+constexpr int kGradSplitWarps = 4;
+
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(32 * kGradSplitWarps) k_eri_grad_split(const GradArgs a) {
+    using W = GradThread<LA, LB, LC, LD>;
+    constexpr int L = W::L;
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kGradSplitWarps + (threadIdx.x >> 5);
+    if (t >= a.ntask) return;                      // warp-uniform
+    const int2 task = a.tasks[t];
+    const PairRec B = a.pairs[task.x];
+    const PairRec K = a.pairs[task.y];
+    double H[W::HSIZE];
+#pragma unroll
+    for (int k = 0; k < W::NACC; ++k) H[k] = 0.0;
+    const int nK = K.nprim, ntot = B.nprim * nK;
+    for (int i = lane; i < ntot; i += 32) {
+        const PrimRec<double> P = a.prims[B.prim_off + i / nK];
+        const PrimRec<double> Q = a.prims[K.prim_off + i % nK];
+        double c[kNCoefG], n[W::NVSLOT];
+        wide_setup_m<L, double>(P, Q, c, n);
+        c[32] = 2.0 * P.pad;
+        c[33] = 2.0 * (P.p - P.pad);
+        c[34] = 2.0 * Q.pad;
+        c[35] = 5.0 * c[28];
+        W::prim(c, n, H);
+    }
+#pragma unroll
+    for (int k = 0; k < W::NACC; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) H[k] += __shfl_xor_sync(0xffffffffu, H[k], o);
+    if (lane == 0) grad_finish<LA, LB, LC, LD>(a, task, B, K, H, a.grad, false);
+}
+
+template <int LA, int LB, int LC, int LD>
+int launch_grad_split(const GradArgs& a, cudaStream_t st) {
+    if (a.ntask <= 0) return 0;
+    k_eri_grad_split<LA, LB, LC, LD><<<(a.ntask + kGradSplitWarps - 1) / kGradSplitWarps,
+                                       32 * kGradSplitWarps, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 

@@ -19,10 +19,14 @@ import torch
 
 from . import _lib, scf
 from .basis import ShellBasis
-from .engine import DeviceShells, JKEngine, QuartetBatch
+from .engine import DeviceShells, HeavyLane, JKEngine, QuartetBatch
 from .fock import FockMatrixRestrictedGPU
 from .hamiltonian import one_electron
 from .molecules import Molecule, shell_basis
+
+# quartets of a thread-form gradient class with many primitive quartets (the engine's heavy
+# prefix) run in the split form: one warp per quartet over its primitive quartets
+GRAD_SPLIT = True
 
 _COMP = {0: [(0, 0, 0)], 1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)],
          2: [(2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)]}
@@ -180,13 +184,25 @@ def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom, classes=None, host=
     sa = torch.as_tensor(np.ascontiguousarray(shell_atom, dtype=np.int32)).to(dev)
     L = _lib.lib()
     base = engine.tasks.data_ptr()
-    for cls, s, e in engine.segments:
+    lane = HeavyLane(dev)
+    for (cls, s, e), heavy in zip(engine.segments, engine.heavy):
         if classes is not None and cls not in classes:
             continue
-        _lib.check(L.gs_eri_grad(*cls, _lib.ptr(engine.pairs.rec), _lib.ptr(engine.pairs.p64),
-                                 _lib.ptr(engine.ds.comp_scale), _lib.ptr(engine.ds.func_off),
-                                 _lib.ptr(sa), e - s, base + s * 8, sb.nbf, natom, _lib.ptr(pt),
-                                 _lib.ptr(grad), _lib.stream()), f"gs_eri_grad{cls}")
+        # a thread-form class's quartets with many primitive quartets (the task list's
+        # prefix) in the split form, on the side stream beside the other launches
+        h = heavy[0] if GRAD_SPLIT and L.gs_eri_grad_class_form(*cls) == 1 else 0
+        for form, first, count, st in ((3, 0, h, "side"), (0, h, e - s - h, "main")):
+            if count <= 0:
+                continue
+            _lib.check(L.gs_eri_grad_form(*cls, form, _lib.ptr(engine.pairs.rec),
+                                          _lib.ptr(engine.pairs.p64),
+                                          _lib.ptr(engine.ds.comp_scale),
+                                          _lib.ptr(engine.ds.func_off), _lib.ptr(sa), count,
+                                          base + (s + first) * 8, sb.nbf, natom, _lib.ptr(pt),
+                                          _lib.ptr(grad),
+                                          lane.stream() if st == "side" else _lib.stream()),
+                       f"gs_eri_grad_form{cls}")
+    lane.join()
     return grad.view(natom, 3).cpu().numpy() if host else grad.view(natom, 3)
 
 

@@ -262,6 +262,21 @@ int gs_eri_grad(int la, int lb, int lc, int ld, const void* pair_rec, const void
                 const int* tasks, int nbf, int natom, const double* density, double* grad,
                 void* stream);
 
+/* gs_eri_grad with an explicit kernel form for this call: 0 = the class's configured form,
+ * 1 = one thread per quartet, 2 = one warp per quartet, 3 = split (the thread code with one
+ * warp per quartet over its primitive quartets, for quartets with many of them); forms 1
+ * and 3 exist for classes of total angular momentum <= 3 (else GS_ERR_ARG).  No reference
+ * counterpart (see gs_eri_grad_contract). */
+int gs_eri_grad_form(int la, int lb, int lc, int ld, int form, const void* pair_rec,
+                     const void* prim64, const double* comp_scale, const int* func_off,
+                     const int* shell_atom, int ntask, const int* tasks, int nbf, int natom,
+                     const double* density, double* grad, void* stream);
+
+/* The form (1 thread, 2 warp) a gs_eri_grad launch of that class uses: the configured
+ * variant or the default; negative status on a class without gradient kernels.  No
+ * reference counterpart. */
+int gs_eri_grad_class_form(int la, int lb, int lc, int ld);
+
 /* Kernel forms built for gradient class (la lb|lc ld): bit 0 one thread per quartet
  * (classes of total angular momentum <= 3), bit 1 one warp per quartet; negative status
  * for a class without gradient kernels.  No reference counterpart. */

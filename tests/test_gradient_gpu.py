@@ -171,3 +171,25 @@ def test_eri_gradient_per_class_against_differences(gpu_lib):
             if abs(g[a, x] - fd) > 1e-7:
                 bad.append((cls, a, x, float(g[a, x]), fd))
     assert not bad, bad
+
+
+def test_gradient_split_form_matches_thread_form(gpu_lib):
+    """(H2O)2 / 6-31G: the ERI gradient with the heavy quartets of thread-form classes in
+    the split form (one warp per quartet) equals the all-thread-form gradient."""
+    from gaussium_gb300 import gradient, molecules
+    from gaussium_gb300.engine import JKEngine
+    mol = molecules.water_cluster(2, seed=2)
+    _, _, res = gradient.rhf_energy_gradient(mol, "6-31G")
+    sb = molecules.shell_basis(mol, "6-31G")
+    eng = JKEngine(sb, schwarz_thr=1e-14)
+    assert sum(h[0] for h in eng.heavy) > 0
+    sa = gradient.shell_atoms(mol, sb)
+    n = len(mol.symbols)
+    try:
+        gradient.GRAD_SPLIT = True
+        g1 = gradient.eri_gradient(sb, eng, sa, res.density, n)
+        gradient.GRAD_SPLIT = False
+        g0 = gradient.eri_gradient(sb, eng, sa, res.density, n)
+    finally:
+        gradient.GRAD_SPLIT = True
+    assert np.max(np.abs(g1 - g0)) <= 1e-11 * max(1.0, np.max(np.abs(g0)))
