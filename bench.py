@@ -39,10 +39,10 @@ WORKLOAD = "synthetic ERI microbench: 2,000,000 seeded shell quartets, l uniform
 # ncu capture of the 1,000,000-quartet case of this workload (its output blocks, 256 MB for
 # (dd|dp), exceed the 129 MB L2, as at full size); empty until such a capture exists, and
 # the line then reports traffic null
-NCU_DRAM_BYTES_PER_QUARTET = {(2, 2, 2, 1): (61216512 + 202637312) / 49552}
+NCU_DRAM_BYTES_PER_QUARTET = {(2, 2, 2, 1): (56363520 + 195581952) / 48606}
 NCU_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_wide_write<2,2,2,1,"
-                      "double> on the 1,000,000-quartet case (49,552 quartets of the class, "
-                      "256.9 MB of output blocks > L2)")
+                      "double> on the 1,000,000-quartet case (the one-warp launch over 48,606 "
+                      "of the class's 49,552 quartets, 252.0 MB of output blocks > L2)")
 
 
 def parse():
