@@ -265,7 +265,6 @@ def run_gpu(args, rank, world):
     out = torch.empty(batch.total, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
     classes = [c for c, _, _ in batch.segments]
-    nlaunch = 1 + len(classes)
     forms = {}
     if not args.no_tune:
         # kernel form (thread / warp per quartet) of every class built with both, chosen
@@ -468,7 +467,9 @@ def run_gpu(args, rank, world):
         "per_class_gflop": {"".join(map(str, c)): round(v / 1e9, 3) for c, v in fl.items()},
         "clocks": res[64]["clocks"],
         "e2e": e2e,
-        "gpu_launches": nlaunch * args.steps,
+        # the FP64 timed steps: the pair build and each class's launches (a class whose heavy
+        # prefix runs in its own form launches twice)
+        "gpu_launches": (1 + batch.launch_count(64)) * args.steps,
         "cpu_baseline": cpu,
         "fock": fock,
     }

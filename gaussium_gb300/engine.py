@@ -390,6 +390,15 @@ class QuartetBatch:
     def class_counts(self):
         return {cls: e - s for cls, s, e in self.segments}
 
+    def launch_count(self, precision=64):
+        """Kernel launches one ``run`` makes with the current kernel forms: one per class,
+        and one more for a class whose heavy prefix runs in its own form."""
+        n = 0
+        for (cls, s, e), heavy in zip(self.segments, self.heavy):
+            for form, first, count in split_forms(cls, precision, heavy):
+                n += ((e - s - first) if count is None else count) > 0
+        return n
+
     def run(self, out, precision=64, stream=None, classes=None):
         _check_device_tensor(out, self.ds.device, "output buffer")
         if out.numel() < self.total:
