@@ -110,7 +110,10 @@ def generate():
                 with open(spath, "w") as f:
                     f.write(stub)
         inc = '#include "eri_class_%s.h"\n#include "eri_wide_%s.h"\n' % (tag, tag)
-        code = ('#define GS_WIDE64_MIN %d\n#define GS_WIDE32_MIN %d\n#define GS_THREAD64_MAX %d\n'
+        # GS_BOYS_ORDER: the Boys order of this class's kernels, whose Taylor rows the unit
+        # embeds (eri_common.cuh)
+        code = ('#define GS_BOYS_ORDER %d\n' % L +
+                '#define GS_WIDE64_MIN %d\n#define GS_WIDE32_MIN %d\n#define GS_THREAD64_MAX %d\n'
                 '#define GS_THREAD32_MAX %d\n#define GS_WIDE_FROM %d\n#define GS_WIDE32_FROM %d\n'
                 '#include "eri_launch.cuh"\n%s'
                 'int gs_launch_%s(int kind, int prec, const void* args, cudaStream_t st) {\n'
@@ -146,9 +149,11 @@ def generate():
         body = ('    if (form == 1) return gs::launch_grad_thread<%d, %d, %d, %d>(a, st);\n'
                 '    if (form == 3) return gs::launch_grad_split<%d, %d, %d, %d>(a, st);\n'
                 % (cls + cls) if thread else '    (void)form;\n')
-        code = ('#include "eri_grad.cuh"\n%s'
+        # the derivative integrals raise one centre: Boys order L + 1
+        code = ('#define GS_BOYS_ORDER %d\n#include "eri_grad.cuh"\n%s'
                 'int gs_grad_launch_%s(const gs::GradArgs& a, int form, cudaStream_t st) {\n%s'
-                '    return gs::launch_grad<%d, %d, %d, %d>(a, st);\n}\n' % (inc, tag, body, *cls))
+                '    return gs::launch_grad<%d, %d, %d, %d>(a, st);\n}\n'
+                % (sum(cls) + 1, inc, tag, body, *cls))
         path = os.path.join(GEN, f"eri_grad_k_{tag}.cu")
         if not os.path.exists(path) or open(path).read() != code:
             with open(path, "w") as f:

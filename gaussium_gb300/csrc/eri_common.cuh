@@ -98,6 +98,22 @@ GS_HD GS_INLINE const double* boys_table() {
 #endif
 }
 
+// Taylor rows of the one Boys order the kernels of a translation unit evaluate most
+// (GS_BOYS_ORDER, defined by the generated class and gradient units): row k holds
+// F_{M+j}(T_k) / j!, j = 0..6, and the exponential's row exp(-T_k) / j!, so that an
+// expansion about T_k is a Horner chain of FMAs in T_k - T.  Other orders use the grid.
+#if defined(__CUDACC__) && defined(GS_BOYS_ORDER)
+#define GS_BOYS_CAT2(a, b) a##b
+#define GS_BOYS_CAT(a, b) GS_BOYS_CAT2(a, b)
+__device__ __align__(16) const double g_boys_taylor[BOYS_ROWS * 8] = {
+    GS_BOYS_CAT(GS_BOYS_TAYLOR_, GS_BOYS_ORDER)};
+__device__ __align__(16) const double g_boys_expt[BOYS_ROWS * 8] = {GS_BOYS_EXPT};
+constexpr int kBoysOrder = GS_BOYS_ORDER;
+static_assert(kBoysOrder >= 0 && kBoysOrder <= BOYS_TAYLOR_MMAX, "Boys order without rows");
+#else
+constexpr int kBoysOrder = -1;
+#endif
+
 template <typename T> GS_HD GS_INLINE T ldg(const T* p) {
 #if defined(__CUDA_ARCH__)
     return __ldg(p);
@@ -113,6 +129,34 @@ template <typename T> GS_HD GS_INLINE T ldg(const T* p) {
 // e^{-(t - t_k)}.  F[m] = pref * F_m(t).
 template <int M>
 GS_HD GS_INLINE void boys_small(double t, double pref, double* __restrict__ F) {
+#if defined(__CUDA_ARCH__) && defined(GS_BOYS_ORDER)
+    if constexpr (M == kBoysOrder) {
+        // the same expansion and recursion from this order's Taylor rows
+        const int k = __double2int_rn(t * BOYS_INV_H);
+        const double d = fma((double)k, 1.0 / BOYS_INV_H, -t);     // t_k - t, exact
+        const double2* g = reinterpret_cast<const double2*>(g_boys_taylor) + 4 * k;
+        const double2 g01 = __ldg(g), g23 = __ldg(g + 1), g45 = __ldg(g + 2), g67 = __ldg(g + 3);
+        double f = fma(g67.x, d, g45.y);
+        f = fma(f, d, g45.x);
+        f = fma(f, d, g23.y);
+        f = fma(f, d, g23.x);
+        f = fma(f, d, g01.y);
+        F[M] = fma(f, d, g01.x) * pref;
+        if (M > 0) {
+            const double2* x = reinterpret_cast<const double2*>(g_boys_expt) + 4 * k;
+            const double2 x01 = __ldg(x), x23 = __ldg(x + 1), x45 = __ldg(x + 2), x67 = __ldg(x + 3);
+            double e = fma(x67.x, d, x45.y);
+            e = fma(e, d, x45.x);
+            e = fma(e, d, x23.y);
+            e = fma(e, d, x23.x);
+            e = fma(e, d, x01.y);
+            const double et = fma(e, d, x01.x) * pref;
+            const double t2 = t + t;
+            GS_UNROLL for (int m = M; m >= 1; --m) F[m - 1] = (t2 * F[m] + et) * (1.0 / (2 * m - 1));
+        }
+        return;
+    }
+#endif
     const int k = (int)(t * BOYS_INV_H + 0.5);
     const double d = k * (1.0 / BOYS_INV_H) - t;
     const double* row = boys_table() + k * BOYS_NCOL;
@@ -147,6 +191,32 @@ GS_HD GS_INLINE void boys_small(double t, double pref, double* __restrict__ F) {
 template <int M>
 GS_HD GS_INLINE void boys_small32(float t, float pref, float* __restrict__ F) {
     static_assert(M + 4 <= BOYS_NCOL - 2, "Taylor terms beyond the tabulated orders");
+#if defined(__CUDA_ARCH__) && defined(GS_BOYS_ORDER)
+    if constexpr (M == kBoysOrder) {
+        // this order's Taylor rows, cut after the d^4 term as below
+        const int k = __float2int_rn(t * float(BOYS_INV_H));
+        const double d = (double)((float)k * (1.0f / BOYS_INV_H) - t);
+        const double2* g = reinterpret_cast<const double2*>(g_boys_taylor) + 4 * k;
+        const double2 g01 = __ldg(g), g23 = __ldg(g + 1), g45 = __ldg(g + 2);
+        double Fd[M + 1];
+        double f = fma(g45.x, d, g23.y);
+        f = fma(f, d, g23.x);
+        f = fma(f, d, g01.y);
+        Fd[M] = fma(f, d, g01.x);
+        if (M > 0) {
+            const double2* x = reinterpret_cast<const double2*>(g_boys_expt) + 4 * k;
+            const double2 x01 = __ldg(x), x23 = __ldg(x + 1), x45 = __ldg(x + 2);
+            double e = fma(x45.x, d, x23.y);
+            e = fma(e, d, x23.x);
+            e = fma(e, d, x01.y);
+            const double et = fma(e, d, x01.x);
+            const double t2 = 2.0 * (double)t;
+            GS_UNROLL for (int m = M; m >= 1; --m) Fd[m - 1] = (t2 * Fd[m] + et) * (1.0 / (2 * m - 1));
+        }
+        GS_UNROLL for (int m = 0; m <= M; ++m) F[m] = (float)Fd[m] * pref;
+        return;
+    }
+#endif
     const int k = (int)(t * float(BOYS_INV_H) + 0.5f);
     const double d = (double)((float)k * (1.0f / BOYS_INV_H) - t);
     const double* row = boys_table() + k * BOYS_NCOL;
