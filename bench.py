@@ -74,6 +74,9 @@ def parse():
                     help="water molecules of the XC workload (19 6-31G* functions each)")
     ap.add_argument("--mo-waters", type=int, default=6,
                     help="water molecules of the AO->MO workload (13 6-31G functions each)")
+    ap.add_argument("--grad-mixed-cut", type=float, default=1e-3,
+                    help="gradient workload: density-weighted bound below which the adjoint's "
+                         "recursion runs in FP32")
     ap.add_argument("--grad-basis", default="6-31G",
                     help="basis of the gradient workload (6-31G, or 6-31G* with d shells)")
     ap.add_argument("--opt-basis", default="6-31G",
@@ -740,6 +743,15 @@ def run_gradient(args, rank, world):
     ge = gradient.eri_gradient(sb, eng, sa, P, natom)
     torch.cuda.synchronize()
     t_eri_grad = time.perf_counter() - t0
+    # the same with density screening (1e-12) and FP32 recursions below the mixed cut
+    mx = dict(screen_thr=1e-12, mixed_cut=args.grad_mixed_cut)
+    gradient.eri_gradient(sb, eng, sa, P, natom, **mx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ge_mx = gradient.eri_gradient(sb, eng, sa, P, natom, **mx)
+    torch.cuda.synchronize()
+    t_eri_grad_mx = time.perf_counter() - t0
+    g_mx = g - ge + ge_mx
     # per-class device time of the ERI gradient launches
     per_cls = {}
     st = torch.cuda.current_stream()
@@ -761,7 +773,7 @@ def run_gradient(args, rank, world):
     ncoord = min(args.fd_coords, 3 * len(mol.symbols))
     pick = rng.choice(3 * len(mol.symbols), size=ncoord, replace=False)
     h = 1e-4
-    err = 0.0
+    err = err_mx = 0.0
     for k in pick:
         a, x = divmod(int(k), 3)
         cp, cm = mol.coords.copy(), mol.coords.copy()
@@ -769,7 +781,9 @@ def run_gradient(args, rank, world):
         cm[a, x] -= h
         ep = gradient.rhf_energy_gradient(molecules.Molecule(mol.symbols, cp), basis, want_gradient=False)[0]
         em = gradient.rhf_energy_gradient(molecules.Molecule(mol.symbols, cm), basis, want_gradient=False)[0]
-        err = max(err, abs((ep - em) / (2 * h) - g[a, x]))
+        fd = (ep - em) / (2 * h)
+        err = max(err, abs(fd - g[a, x]))
+        err_mx = max(err_mx, abs(fd - g_mx[a, x]))
     line = {
         "metric": METRIC, "value": (t_eri_grad + t_one_grad) / t_fock,
         "unit": "gradient time / one Fock build", "n_gpus": world, "steps": 1, "warmup": 1,
@@ -779,6 +793,12 @@ def run_gradient(args, rank, world):
                    "fd_coordinates_checked": int(ncoord), "fd_step_bohr": h},
         "energy": e, "max_abs_grad_minus_fd": err,
         "eri_gradient_ms": t_eri_grad * 1e3, "one_electron_gradient_ms": t_one_grad * 1e3,
+        "screened_mixed": {
+            "screen_thr": 1e-12, "mixed_cut": args.grad_mixed_cut,
+            "eri_gradient_ms": t_eri_grad_mx * 1e3,
+            "gradient_over_fock_build": (t_eri_grad_mx + t_one_grad) / t_fock,
+            "max_abs_grad_minus_fd": err_mx,
+            "max_abs_minus_fp64_gradient": float(np.max(np.abs(g_mx - g)))},
         "eri_gradient_ms_per_class": per_cls, "gradient_kernel_forms_autotuned": forms,
         "fock_kernel_forms_autotuned": fock_forms,
         "fock_build_ms": t_fock * 1e3, "scf_plus_gradient_s": t_total,

@@ -47,6 +47,7 @@ _SIGS = {
     "gs_eri_grad_contract": (I, [I, P, P, P, P, P, P, P, I, P, P, P]),
     "gs_eri_grad": (I, [I, I, I, I, P, P, P, P, P, I, P, I, I, P, P, P]),
     "gs_eri_grad_form": (I, [I, I, I, I, I, P, P, P, P, P, I, P, I, I, P, P, P]),
+    "gs_eri_grad_band": (I, [I, I, I, I, I, I, P, P, P, P, P, I, P, I, I, P, I, P, D, D, D, P, P]),
     "gs_eri_grad_class_form": (I, [I, I, I, I]),
     "gs_eri_grad_variants": (I, [I, I, I, I]),
     "gs_set_eri_grad_variant": (I, [I, I, I, I, I]),

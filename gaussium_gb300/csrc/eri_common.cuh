@@ -374,7 +374,9 @@ GS_HD GS_INLINE PrimRec<float> prim_pair32(const PrimRec<double>& r) {
     f.p = (float)r.p; f.i2p = (float)r.i2p;
     f.Px = (float)r.Px; f.Py = (float)r.Py; f.Pz = (float)r.Pz;
     f.PAx = (float)r.PAx; f.PAy = (float)r.PAy; f.PAz = (float)r.PAz;
-    f.Kp = (float)r.Kp; f.pad0 = f.pad1 = f.pad2 = 0.0f;
+    f.Kp = (float)r.Kp;
+    f.pad0 = (float)r.pad;      // exponent of the first shell (FP32 derivative weights)
+    f.pad1 = f.pad2 = 0.0f;
     return f;
 }
 

@@ -25,7 +25,34 @@ struct GradArgs {
     const double* P;
     double* grad;
     int natom;
+    // FP32 evaluation (thread and split forms): recursion and accumulation in FP32 from the
+    // FP32 records (pad0 holds the first shell's exponent), HRR and contraction in FP64
+    const PrimRec<float>* prims32;
+    bool fp32;
+    // density-weighted screening: a quartet is evaluated when its Schwarz bound times the
+    // largest |P| of its six shell blocks (shell_dmax, nshell x nshell) is at least
+    // screen_thr and lies in [prec_lo, prec_hi); screen_thr <= 0 evaluates every quartet
+    const double* shell_dmax;
+    int nshell;
+    double screen_thr, prec_lo, prec_hi;
 };
+
+__device__ __forceinline__ bool grad_keep(const GradArgs& a, const PairRec& B, const PairRec& K) {
+    if (a.screen_thr <= 0.0) return true;
+    const int ns = a.nshell;
+    const double* d = a.shell_dmax;
+    double dm = d[B.sa * ns + B.sb];
+    dm = fmax(dm, d[K.sa * ns + K.sb]);
+    dm = fmax(dm, d[B.sa * ns + K.sa]);
+    dm = fmax(dm, d[B.sa * ns + K.sb]);
+    dm = fmax(dm, d[B.sb * ns + K.sa]);
+    dm = fmax(dm, d[B.sb * ns + K.sb]);
+    const double est = (double)B.qmax * (double)K.qmax * dm;
+    return !(est < a.screen_thr || est < a.prec_lo || est >= a.prec_hi);
+}
+
+__device__ __forceinline__ double prim_expo(const PrimRec<double>& r) { return r.pad; }
+__device__ __forceinline__ float prim_expo(const PrimRec<float>& r) { return r.pad0; }
 
 constexpr int kGradWarps = 2;        // warps per block, unless the class's buffer is too large
 constexpr int kNCoefG = 36;
@@ -103,6 +130,7 @@ __global__ void __launch_bounds__(32 * kGradWarps) k_eri_grad(const GradArgs a) 
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
+    if (!grad_keep(a, B, K)) return;               // warp-uniform
     double acc[NACCW];
     int accs[NACCW], acck[NACCW];
 #pragma unroll
@@ -367,12 +395,40 @@ __device__ __forceinline__ void grad_finish(const GradArgs& a, const int2 task, 
     }
 }
 
-template <int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs a) {
+// Weighted contraction sets of primitive quartets start, start + stride, ... of the quartet
+// into H[0 .. NACC), the recursion in T.
+template <int LA, int LB, int LC, int LD, typename T>
+__device__ __forceinline__ void grad_accumulate(const GradArgs& a, const PairRec& B,
+                                                const PairRec& K, double* H, int start,
+                                                int stride) {
     using W = GradThread<LA, LB, LC, LD>;
     constexpr int L = W::L;
-    constexpr int NA = (LA + 1) * (LA + 2) / 2, NB = (LB + 1) * (LB + 2) / 2;
-    constexpr int NC = (LC + 1) * (LC + 2) / 2, ND = (LD + 1) * (LD + 2) / 2;
+    const PrimRec<T>* __restrict__ prims;
+    if constexpr (sizeof(T) == 8) prims = a.prims;
+    else prims = a.prims32;
+    T acc[W::NACC];
+#pragma unroll
+    for (int k = 0; k < W::NACC; ++k) acc[k] = T(0);
+    const int nK = K.nprim, ntot = B.nprim * nK;
+    for (int i = start; i < ntot; i += stride) {
+        const PrimRec<T> P = prims[B.prim_off + i / nK];
+        const PrimRec<T> Q = prims[K.prim_off + i % nK];
+        T c[kNCoefG], n[W::NVSLOT];
+        wide_setup_m<L, T>(P, Q, c, n);
+        const T ea = prim_expo(P);
+        c[32] = T(2) * ea;                  // 2 alpha (first bra shell)
+        c[33] = T(2) * (P.p - ea);          // 2 beta
+        c[34] = T(2) * prim_expo(Q);        // 2 gamma (first ket shell)
+        c[35] = T(5) * c[28];               // 5/(2(p+q)), raised (dd|..) classes
+        W::template prim<T>(c, n, acc);
+    }
+#pragma unroll
+    for (int k = 0; k < W::NACC; ++k) H[k] = (double)acc[k];
+}
+
+template <int LA, int LB, int LC, int LD, typename T>
+__global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs a) {
+    using W = GradThread<LA, LB, LC, LD>;
     extern __shared__ double sg[];
     const bool shared_sum = a.natom > 0 && a.natom <= kGradSmemAtoms;
     if (shared_sum) {
@@ -384,22 +440,11 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
         const int2 task = a.tasks[t];
         const PairRec B = a.pairs[task.x];
         const PairRec K = a.pairs[task.y];
-        double H[W::HSIZE];
-#pragma unroll
-        for (int k = 0; k < W::NACC; ++k) H[k] = 0.0;
-        const int nK = K.nprim, ntot = B.nprim * nK;
-        for (int i = 0; i < ntot; ++i) {
-            const PrimRec<double> P = a.prims[B.prim_off + i / nK];
-            const PrimRec<double> Q = a.prims[K.prim_off + i % nK];
-            double c[kNCoefG], n[W::NVSLOT];
-            wide_setup_m<L, double>(P, Q, c, n);
-            c[32] = 2.0 * P.pad;               // 2 alpha (first bra shell)
-            c[33] = 2.0 * (P.p - P.pad);       // 2 beta
-            c[34] = 2.0 * Q.pad;               // 2 gamma (first ket shell)
-            c[35] = 5.0 * c[28];               // 5/(2(p+q)), raised (dd|..) classes
-            W::prim(c, n, H);
+        if (grad_keep(a, B, K)) {
+            double H[W::HSIZE];
+            grad_accumulate<LA, LB, LC, LD, T>(a, B, K, H, 0, 1);
+            grad_finish<LA, LB, LC, LD>(a, task, B, K, H, shared_sum ? sg : a.grad, true);
         }
-        grad_finish<LA, LB, LC, LD>(a, task, B, K, H, shared_sum ? sg : a.grad, true);
     }
     if (shared_sum) {
         __syncthreads();
@@ -408,15 +453,21 @@ __global__ void __launch_bounds__(kGradThreads) k_eri_grad_thread(const GradArgs
     }
 }
 
+template <int LA, int LB, int LC, int LD, typename T>
+int launch_grad_thread_t(const GradArgs& a, cudaStream_t st) {
+    const size_t sh = (a.natom > 0 && a.natom <= kGradSmemAtoms) ? 3 * sizeof(double) * a.natom : 0;
+    if (set_smem<k_eri_grad_thread<LA, LB, LC, LD, T>>(3 * sizeof(double) * kGradSmemAtoms))
+        return GS_ERR_CUDA;
+    k_eri_grad_thread<LA, LB, LC, LD, T><<<(a.ntask + kGradThreads - 1) / kGradThreads,
+                                           kGradThreads, sh, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+}
+
 template <int LA, int LB, int LC, int LD>
 int launch_grad_thread(const GradArgs& a, cudaStream_t st) {
     if (a.ntask <= 0) return 0;
-    const size_t sh = (a.natom > 0 && a.natom <= kGradSmemAtoms) ? 3 * sizeof(double) * a.natom : 0;
-    if (set_smem<k_eri_grad_thread<LA, LB, LC, LD>>(3 * sizeof(double) * kGradSmemAtoms))
-        return GS_ERR_CUDA;
-    k_eri_grad_thread<LA, LB, LC, LD><<<(a.ntask + kGradThreads - 1) / kGradThreads, kGradThreads,
-                                        sh, st>>>(a);
-    return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
+    return a.fp32 ? launch_grad_thread_t<LA, LB, LC, LD, float>(a, st)
+                  : launch_grad_thread_t<LA, LB, LC, LD, double>(a, st);
 }
 
 // Split form of the thread kernel, for quartets with many primitive quartets (the heavy
@@ -425,31 +476,18 @@ int launch_grad_thread(const GradArgs& a, cudaStream_t st) {
 // a butterfly sum of the weighted contraction sets, then lane 0 finishes the quartet.
 constexpr int kGradSplitWarps = 4;
 
-template <int LA, int LB, int LC, int LD>
+template <int LA, int LB, int LC, int LD, typename T>
 __global__ void __launch_bounds__(32 * kGradSplitWarps) k_eri_grad_split(const GradArgs a) {
     using W = GradThread<LA, LB, LC, LD>;
-    constexpr int L = W::L;
     const int lane = threadIdx.x & 31;
     const int t = blockIdx.x * kGradSplitWarps + (threadIdx.x >> 5);
     if (t >= a.ntask) return;                      // warp-uniform
     const int2 task = a.tasks[t];
     const PairRec B = a.pairs[task.x];
     const PairRec K = a.pairs[task.y];
+    if (!grad_keep(a, B, K)) return;               // warp-uniform
     double H[W::HSIZE];
-#pragma unroll
-    for (int k = 0; k < W::NACC; ++k) H[k] = 0.0;
-    const int nK = K.nprim, ntot = B.nprim * nK;
-    for (int i = lane; i < ntot; i += 32) {
-        const PrimRec<double> P = a.prims[B.prim_off + i / nK];
-        const PrimRec<double> Q = a.prims[K.prim_off + i % nK];
-        double c[kNCoefG], n[W::NVSLOT];
-        wide_setup_m<L, double>(P, Q, c, n);
-        c[32] = 2.0 * P.pad;
-        c[33] = 2.0 * (P.p - P.pad);
-        c[34] = 2.0 * Q.pad;
-        c[35] = 5.0 * c[28];
-        W::prim(c, n, H);
-    }
+    grad_accumulate<LA, LB, LC, LD, T>(a, B, K, H, lane, 32);
 #pragma unroll
     for (int k = 0; k < W::NACC; ++k)
 #pragma unroll
@@ -460,8 +498,11 @@ __global__ void __launch_bounds__(32 * kGradSplitWarps) k_eri_grad_split(const G
 template <int LA, int LB, int LC, int LD>
 int launch_grad_split(const GradArgs& a, cudaStream_t st) {
     if (a.ntask <= 0) return 0;
-    k_eri_grad_split<LA, LB, LC, LD><<<(a.ntask + kGradSplitWarps - 1) / kGradSplitWarps,
-                                       32 * kGradSplitWarps, 0, st>>>(a);
+    const int grid = (a.ntask + kGradSplitWarps - 1) / kGradSplitWarps;
+    if (a.fp32)
+        k_eri_grad_split<LA, LB, LC, LD, float><<<grid, 32 * kGradSplitWarps, 0, st>>>(a);
+    else
+        k_eri_grad_split<LA, LB, LC, LD, double><<<grid, 32 * kGradSplitWarps, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : GS_ERR_CUDA;
 }
 

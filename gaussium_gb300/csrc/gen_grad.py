@@ -322,7 +322,8 @@ def emit_grad_thread(cls, p=None):
              "#pragma once", "namespace gs {",
              f"template <> struct GradThread<{la}, {lb}, {lc}, {ld}> {{",
              f"  static constexpr int L = {L}, NACC = {nacc}, NVSLOT = {p['nvslot']}, HSIZE = {p['hsize']};",
-             "  static __device__ __forceinline__ void prim(const double* __restrict__ c, double* n, double* H) {",
+             "  template <typename T>",
+             "  static __device__ __forceinline__ void prim(const T* __restrict__ c, T* n, T* H) {",
              *body, *acc, "  }",
              "  static __device__ __forceinline__ void hrr(double* H, const double* dv) {",
              *hrr, "  }",

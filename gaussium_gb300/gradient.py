@@ -173,35 +173,47 @@ def _check_atoms(shell_atom, natom):
         raise ValueError("shell_atom holds an atom index outside [0, natom)")
 
 
-def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom, classes=None, host=True):
-    """Two-electron gradient through the fused adjoint kernel (gs_eri_grad), one launch per
-    class over the engine's Schwarz-screened unique quartets (``classes``: only those).
+def eri_gradient(sb, engine: JKEngine, shell_atom, P, natom, classes=None, host=True,
+                 screen_thr=0.0, mixed_cut=None):
+    """Two-electron gradient through the fused adjoint kernels, launched per class over the
+    engine's Schwarz-screened unique quartets (``classes``: only those).  ``screen_thr``
+    skips quartets whose Schwarz bound times the largest |P| of their six shell blocks is
+    below it; with ``mixed_cut``, the quartets of the thread-form classes whose such bound
+    is below the cut run their recursion in FP32 (FP64 HRR, contraction and sums).
     Returns natom x 3 (host numpy, or the device tensor with ``host=False``)."""
     _check_atoms(shell_atom, natom)
     dev = engine.dev
     grad = torch.zeros(natom * 3, dtype=torch.float64, device=dev)
     pt = torch.as_tensor(np.ascontiguousarray(P)).to(dev)
     sa = torch.as_tensor(np.ascontiguousarray(shell_atom, dtype=np.int32)).to(dev)
+    dmax, thr = None, 0.0
+    if screen_thr > 0 or mixed_cut is not None:
+        dmax = engine.shell_dmax([pt])
+        thr = screen_thr if screen_thr > 0 else 1e-300
     L = _lib.lib()
     base = engine.tasks.data_ptr()
     lane = HeavyLane(dev)
+    inf = float("inf")
     for (cls, s, e), heavy in zip(engine.segments, engine.heavy):
         if classes is not None and cls not in classes:
             continue
+        thread = L.gs_eri_grad_class_form(*cls) == 1
         # a thread-form class's quartets with many primitive quartets (the task list's
         # prefix) in the split form, on the side stream beside the other launches
-        h = heavy[0] if GRAD_SPLIT and L.gs_eri_grad_class_form(*cls) == 1 else 0
-        for form, first, count, st in ((3, 0, h, "side"), (0, h, e - s - h, "main")):
-            if count <= 0:
-                continue
-            _lib.check(L.gs_eri_grad_form(*cls, form, _lib.ptr(engine.pairs.rec),
-                                          _lib.ptr(engine.pairs.p64),
-                                          _lib.ptr(engine.ds.comp_scale),
-                                          _lib.ptr(engine.ds.func_off), _lib.ptr(sa), count,
-                                          base + (s + first) * 8, sb.nbf, natom, _lib.ptr(pt),
-                                          _lib.ptr(grad),
-                                          lane.stream() if st == "side" else _lib.stream()),
-                       f"gs_eri_grad_form{cls}")
+        h = heavy[0] if GRAD_SPLIT and thread else 0
+        bands = [(64, mixed_cut, inf), (32, 0.0, mixed_cut)] \
+            if (mixed_cut is not None and thread) else [(64, 0.0, inf)]
+        for prec, lo, hi in bands:
+            prims = engine.pairs.p64 if prec == 64 else engine.pairs.p32
+            for form, first, count, side in ((3, 0, h, True), (0, h, e - s - h, False)):
+                if count <= 0:
+                    continue
+                _lib.check(L.gs_eri_grad_band(
+                    *cls, form, prec, _lib.ptr(engine.pairs.rec), _lib.ptr(prims),
+                    _lib.ptr(engine.ds.comp_scale), _lib.ptr(engine.ds.func_off), _lib.ptr(sa),
+                    count, base + (s + first) * 8, sb.nbf, natom, _lib.ptr(pt), sb.nshell,
+                    _lib.ptr(dmax), thr, lo, hi, _lib.ptr(grad),
+                    lane.stream() if side else _lib.stream()), f"gs_eri_grad_band{cls}")
     lane.join()
     return grad.view(natom, 3).cpu().numpy() if host else grad.view(natom, 3)
 
@@ -287,24 +299,27 @@ def rhf_state(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14):
     return RHFState(mol, sb, eng, res.energy + mol.nuclear_repulsion(), res, P, W)
 
 
-def gradient_from_state(st: RHFState):
+def gradient_from_state(st: RHFState, screen_thr=0.0, mixed_cut=None):
     """dE/dR (natom x 3, Eh/bohr) from a converged state: the one-electron derivative
     kernel (P dH/dR - W dS/dR), the fused ERI adjoint kernels contracting d(ab|cd)/dR with
-    the density-weighted quartet weights Gamma(P), and the nuclear repulsion."""
+    the density-weighted quartet weights Gamma(P), and the nuclear repulsion.
+    ``screen_thr`` / ``mixed_cut``: density screening and FP32 recursions for the quartets
+    with small density-weighted bounds (eri_gradient)."""
     sa = shell_atoms(st.mol, st.sb)
     g = one_electron_gradient_kernel(st.sb, st.mol, sa, st.P, st.W)
-    g += eri_gradient(st.sb, st.engine, sa, st.P, len(st.mol.symbols))
+    g += eri_gradient(st.sb, st.engine, sa, st.P, len(st.mol.symbols), screen_thr=screen_thr,
+                      mixed_cut=mixed_cut)
     g += nuclear_repulsion_gradient(st.mol)
     return g
 
 
 def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
-                        want_gradient=True):
+                        want_gradient=True, screen_thr=0.0, mixed_cut=None):
     """Converged RHF energy and analytic gradient (Eh, Eh/bohr)."""
     st = rhf_state(mol, basis, threshold, schwarz_thr)
     if not want_gradient:
         return st.energy, None, st.scf
-    return st.energy, gradient_from_state(st), st.scf
+    return st.energy, gradient_from_state(st, screen_thr, mixed_cut), st.scf
 
 
 class EnergyGradient(torch.autograd.Function):

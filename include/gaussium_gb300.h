@@ -272,6 +272,20 @@ int gs_eri_grad_form(int la, int lb, int lc, int ld, int form, const void* pair_
                      const int* shell_atom, int ntask, const int* tasks, int nbf, int natom,
                      const double* density, double* grad, void* stream);
 
+/* gs_eri_grad_form restricted to a band of the density-weighted bound, in a chosen
+ * precision: a quartet is evaluated when q_ab q_cd max|P| over its six shell blocks
+ * (shell_dmax, nshell x nshell, device) is at least screen_thr and in [prec_lo, prec_hi)
+ * (screen_thr <= 0: every quartet).  precision 32 evaluates the recursion and the weighted
+ * contraction in FP32 from FP32 records (thread and split forms only; the Boys function
+ * below its asymptotic threshold stays FP64), the HRR, contraction with the density and
+ * the gradient sums in FP64.  No reference counterpart (see gs_eri_grad_contract). */
+int gs_eri_grad_band(int la, int lb, int lc, int ld, int form, int precision,
+                     const void* pair_rec, const void* prim, const double* comp_scale,
+                     const int* func_off, const int* shell_atom, int ntask, const int* tasks,
+                     int nbf, int natom, const double* density, int nshell,
+                     const double* shell_dmax, double screen_thr, double prec_lo,
+                     double prec_hi, double* grad, void* stream);
+
 /* The form (1 thread, 2 warp) a gs_eri_grad launch of that class uses: the configured
  * variant or the default; negative status on a class without gradient kernels.  No
  * reference counterpart. */
