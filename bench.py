@@ -705,7 +705,7 @@ def run_gradient(args, rank, world):
     gradient.rhf_energy_gradient(molecules.water_cluster(1, seed=1), basis)      # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e, g, res = gradient.rhf_energy_gradient(mol, basis)
+    e, g, res = gradient.rhf_energy_gradient(mol, basis, screen_thr=0.0, mixed_cut=None)
     torch.cuda.synchronize()
     t_total = time.perf_counter() - t0
     # gradient part alone, and one full Fock build, on the converged state
@@ -743,7 +743,7 @@ def run_gradient(args, rank, world):
     ge = gradient.eri_gradient(sb, eng, sa, P, natom)
     torch.cuda.synchronize()
     t_eri_grad = time.perf_counter() - t0
-    # the same with density screening (1e-12) and FP32 recursions below the mixed cut
+    # the default: density screening (1e-12) and FP32 recursions below the mixed cut
     mx = dict(screen_thr=1e-12, mixed_cut=args.grad_mixed_cut)
     gradient.eri_gradient(sb, eng, sa, P, natom, **mx)
     torch.cuda.synchronize()
@@ -785,20 +785,19 @@ def run_gradient(args, rank, world):
         err = max(err, abs(fd - g[a, x]))
         err_mx = max(err_mx, abs(fd - g_mx[a, x]))
     line = {
-        "metric": METRIC, "value": (t_eri_grad + t_one_grad) / t_fock,
+        "metric": METRIC, "value": (t_eri_grad_mx + t_one_grad) / t_fock,
         "unit": "gradient time / one Fock build", "n_gpus": world, "steps": 1, "warmup": 1,
-        "ms_per_step": (t_eri_grad + t_one_grad) * 1e3, "higher_is_better": False,
+        "ms_per_step": (t_eri_grad_mx + t_one_grad) * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": f"RHF gradient (H2O)8/{basis}, {sb.nbf} functions",
                    "fd_coordinates_checked": int(ncoord), "fd_step_bohr": h},
-        "energy": e, "max_abs_grad_minus_fd": err,
-        "eri_gradient_ms": t_eri_grad * 1e3, "one_electron_gradient_ms": t_one_grad * 1e3,
-        "screened_mixed": {
-            "screen_thr": 1e-12, "mixed_cut": args.grad_mixed_cut,
-            "eri_gradient_ms": t_eri_grad_mx * 1e3,
-            "gradient_over_fock_build": (t_eri_grad_mx + t_one_grad) / t_fock,
-            "max_abs_grad_minus_fd": err_mx,
-            "max_abs_minus_fp64_gradient": float(np.max(np.abs(g_mx - g)))},
+        "energy": e, "max_abs_grad_minus_fd": err_mx,
+        "eri_gradient_ms": t_eri_grad_mx * 1e3, "one_electron_gradient_ms": t_one_grad * 1e3,
+        "eri_gradient": {"screen_thr": 1e-12, "mixed_cut": args.grad_mixed_cut,
+                         "max_abs_minus_fp64_gradient": float(np.max(np.abs(g_mx - g)))},
+        "fp64_adjoint": {"eri_gradient_ms": t_eri_grad * 1e3,
+                         "gradient_over_fock_build": (t_eri_grad + t_one_grad) / t_fock,
+                         "max_abs_grad_minus_fd": err},
         "eri_gradient_ms_per_class": per_cls, "gradient_kernel_forms_autotuned": forms,
         "fock_kernel_forms_autotuned": fock_forms,
         "fock_build_ms": t_fock * 1e3, "scf_plus_gradient_s": t_total,

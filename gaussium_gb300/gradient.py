@@ -299,12 +299,19 @@ def rhf_state(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14):
     return RHFState(mol, sb, eng, res.energy + mol.nuclear_repulsion(), res, P, W)
 
 
-def gradient_from_state(st: RHFState, screen_thr=0.0, mixed_cut=None):
+# the adjoint's defaults: quartets whose Schwarz bound times max |P| is below 1e-12 are
+# skipped, and those below 1e-3 run their recursion in FP32 (FP64 Boys function at small T,
+# HRR, contraction and sums); on (H2O)8 this moves the gradient by < 4e-9 Eh/bohr
+GRAD_SCREEN_THR = 1e-12
+GRAD_MIXED_CUT = 1e-3
+
+
+def gradient_from_state(st: RHFState, screen_thr=GRAD_SCREEN_THR, mixed_cut=GRAD_MIXED_CUT):
     """dE/dR (natom x 3, Eh/bohr) from a converged state: the one-electron derivative
     kernel (P dH/dR - W dS/dR), the fused ERI adjoint kernels contracting d(ab|cd)/dR with
     the density-weighted quartet weights Gamma(P), and the nuclear repulsion.
     ``screen_thr`` / ``mixed_cut``: density screening and FP32 recursions for the quartets
-    with small density-weighted bounds (eri_gradient)."""
+    with small density-weighted bounds (eri_gradient; 0.0 / None: every quartet in FP64)."""
     sa = shell_atoms(st.mol, st.sb)
     g = one_electron_gradient_kernel(st.sb, st.mol, sa, st.P, st.W)
     g += eri_gradient(st.sb, st.engine, sa, st.P, len(st.mol.symbols), screen_thr=screen_thr,
@@ -314,7 +321,7 @@ def gradient_from_state(st: RHFState, screen_thr=0.0, mixed_cut=None):
 
 
 def rhf_energy_gradient(mol, basis="6-31G", threshold=1e-12, schwarz_thr=1e-14,
-                        want_gradient=True, screen_thr=0.0, mixed_cut=None):
+                        want_gradient=True, screen_thr=GRAD_SCREEN_THR, mixed_cut=GRAD_MIXED_CUT):
     """Converged RHF energy and analytic gradient (Eh, Eh/bohr)."""
     st = rhf_state(mol, basis, threshold, schwarz_thr)
     if not want_gradient:
