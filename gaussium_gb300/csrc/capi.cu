@@ -125,82 +125,157 @@ __global__ void __launch_bounds__(256) k_pairs_build(gs::ShellView sv, int npair
     build_pair(sv, pi, pair_shells, pair_prim_off, pairs, p64, p32, max_exp, kept, lane);
 }
 
-// K0, packed form: warp g builds the shell pairs [group_start[g], group_start[g+1]) whose
-// primitive pairs fit one warp together (a group of one pair may have more; it runs the
-// one-pair loop).  Lane l takes primitive pair k of the pair whose lanes contain l, so the
-// FP64 work of small pairs (a K = 1-6 basis has 12 primitive pairs per shell pair on
-// average) is not issued with most lanes idle.  Records and counts as k_pairs_build.
-__global__ void __launch_bounds__(256) k_pairs_build_packed(
+// K0 for grouped pairs.  A group is a run of consecutive shell pairs whose primitive pairs
+// fit one warp together (lane l takes primitive pair k of the pair whose lanes contain l),
+// or a single larger pair taken 32 candidates at a time.  A warp walks kPairGroupsPerWarp
+// groups but only tests the primitive-pair screen per lane there; the kept primitive
+// pairs (about a third on a K = 1-6 basis with exponents over five decades) go to a
+// per-warp queue in shared memory with their record positions, and are evaluated 32 at a
+// time, so the FP64 division and exponential of prim_pair run on full warps.  Records
+// and counts are those of k_pairs_build (each record goes to the position its ballot
+// rank fixed).
+struct PairCand {
+    double ab2;
+    int pi, i, j, r;
+};
+constexpr int kPairGroupsPerWarp = 8;
+constexpr int kPairWarps = 8;                  // warps per block
+constexpr int kPairQueue = 64;                 // a batch of 32 plus one chunk's kept pairs
+
+__device__ __forceinline__ void pair_eval(const gs::ShellView& sv,
+                                          const int* __restrict__ pair_shells,
+                                          const PairCand& c, gs::PrimRec<double>* p64,
+                                          gs::PrimRec<float>* p32) {
+    const double* A = sv.centre + 3 * pair_shells[2 * c.pi];
+    const double* B = sv.centre + 3 * pair_shells[2 * c.pi + 1];
+    const gs::PrimRec<double> rec =
+        gs::prim_pair(A, B, sv.expo[c.i], sv.expo[c.j], c.ab2, sv.coef[c.i], sv.coef[c.j]);
+    p64[c.r] = rec;
+    if (p32) p32[c.r] = gs::prim_pair32(rec);
+}
+
+// Append this lane's candidate if kept (m = the warp's ballot of keep); a full batch of 32
+// is taken off the front and evaluated.  len is warp-uniform and stays below 32 on return.
+__device__ __forceinline__ void pair_push(PairCand* q, int& len, bool keep, const PairCand& c,
+                                          unsigned m, int lane, const gs::ShellView& sv,
+                                          const int* __restrict__ pair_shells,
+                                          gs::PrimRec<double>* p64, gs::PrimRec<float>* p32) {
+    if (keep) q[len + __popc(m & ((1u << lane) - 1u))] = c;
+    len += __popc(m);
+    __syncwarp();
+    if (len >= 32) {
+        const PairCand e = q[lane];
+        __syncwarp();
+        if (lane < len - 32) q[lane] = q[lane + 32];
+        __syncwarp();
+        len -= 32;
+        pair_eval(sv, pair_shells, e, p64, p32);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kPairWarps) k_pairs_build_compact(
     gs::ShellView sv, int ngroups, const int* __restrict__ group_start,
     const int* __restrict__ pair_shells, const int* __restrict__ pair_prim_off,
     gs::PairRec* pairs, gs::PrimRec<double>* p64, gs::PrimRec<float>* p32, double max_exp,
     int* __restrict__ kept) {
-    const int lane = threadIdx.x & 31;
-    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (g >= ngroups) return;
-    const int first = group_start[g], np = group_start[g + 1] - first;
-    if (np == 1) {                                    // one pair (possibly > 32 primitive pairs)
-        build_pair(sv, first, pair_shells, pair_prim_off, pairs, p64, p32, max_exp, kept, lane);
-        return;
+    __shared__ PairCand queue[kPairWarps][kPairQueue];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    PairCand* q = queue[warp];
+    int len = 0;
+    const long long g0 = ((long long)blockIdx.x * kPairWarps + warp) * kPairGroupsPerWarp;
+    for (long long g = g0; g < g0 + kPairGroupsPerWarp && g < ngroups; ++g) {   // warp-uniform
+        const int first = group_start[g], np = group_start[g + 1] - first;
+        if (np == 1) {                                // one pair, chunks of 32 candidates
+            const int pi = first;
+            const int sa = pair_shells[2 * pi], sb = pair_shells[2 * pi + 1];
+            const double* A = sv.centre + 3 * sa;
+            const double* B = sv.centre + 3 * sb;
+            const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
+            const double ab2 = ABx * ABx + ABy * ABy + ABz * ABz;
+            const int a0 = sv.prim_off[sa], b0 = sv.prim_off[sb];
+            const int nb = sv.prim_off[sb + 1] - b0;
+            const int ntot = (sv.prim_off[sa + 1] - a0) * nb;
+            const int base = pair_prim_off[pi];
+            int n = 0;
+            for (int k0 = 0; k0 < ntot; k0 += 32) {
+                const int k = k0 + lane;
+                bool keep = false;
+                int i = 0, j = 0;
+                if (k < ntot) {
+                    i = a0 + k / nb;
+                    j = b0 + k % nb;
+                    keep = gs::prim_pair_kept(sv.expo[i], sv.expo[j], ab2, max_exp);
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                const PairCand c{ab2, pi, i, j, base + n + __popc(m & ((1u << lane) - 1u))};
+                pair_push(q, len, keep, c, m, lane, sv, pair_shells, p64, p32);
+                n += __popc(m);
+            }
+            if (lane == 0) {
+                gs::PairRec pr;
+                pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
+                pr.prim_off = base;
+                pr.nprim = n;
+                pr.sa = sa; pr.sb = sb;
+                pr.qmax = 0.0f; pr.pad = 0;
+                pairs[pi] = pr;
+                if (kept) kept[pi] = n;
+            }
+            continue;
+        }
+        // several pairs in one warp: lanes [off_j, off_j + size_j) belong to pair j
+        int size = 0;
+        if (lane < np) {
+            const int sa = pair_shells[2 * (first + lane)], sb = pair_shells[2 * (first + lane) + 1];
+            size = (sv.prim_off[sa + 1] - sv.prim_off[sa]) * (sv.prim_off[sb + 1] - sv.prim_off[sb]);
+        }
+        int off = size;                               // inclusive scan of the pair sizes
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += y;
+        }
+        off -= size;
+        const int total = __shfl_sync(0xffffffffu, off + size, 31);
+        int jp = 0;
+        for (int p = 1; p < np; ++p)
+            if (__shfl_sync(0xffffffffu, off, p) <= lane) jp = p;
+        const int my_off = __shfl_sync(0xffffffffu, off, jp);
+        const int my_size = __shfl_sync(0xffffffffu, size, jp);
+        const int pi = first + jp;
+        const bool in = lane < total;
+        const int sa = pair_shells[2 * pi], sb = pair_shells[2 * pi + 1];
+        const double* A = sv.centre + 3 * sa;
+        const double* B = sv.centre + 3 * sb;
+        const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
+        const double ab2 = ABx * ABx + ABy * ABy + ABz * ABz;
+        const int a0 = sv.prim_off[sa], b0 = sv.prim_off[sb];
+        const int nb = sv.prim_off[sb + 1] - b0;
+        const int k = lane - my_off;
+        bool keep = false;
+        int i = 0, jj = 0;
+        if (in) {
+            i = a0 + k / nb;
+            jj = b0 + k % nb;
+            keep = gs::prim_pair_kept(sv.expo[i], sv.expo[jj], ab2, max_exp);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        const unsigned pair_mask = (my_size >= 32 ? 0xffffffffu : ((1u << my_size) - 1u)) << my_off;
+        const unsigned mine = m & pair_mask;
+        const int base = pair_prim_off[pi];
+        const PairCand c{ab2, pi, i, jj, base + __popc(mine & ((1u << lane) - 1u))};
+        pair_push(q, len, keep, c, m, lane, sv, pair_shells, p64, p32);
+        if (in && lane == my_off) {
+            gs::PairRec pr;
+            pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
+            pr.prim_off = base;
+            pr.nprim = __popc(mine);
+            pr.sa = sa; pr.sb = sb;
+            pr.qmax = 0.0f; pr.pad = 0;
+            pairs[pi] = pr;
+            if (kept) kept[pi] = pr.nprim;
+        }
     }
-    // this lane's pair (lanes [off_j, off_j + size_j) belong to pair j of the group)
-    int size = 0;
-    if (lane < np) {
-        const int sa = pair_shells[2 * (first + lane)], sb = pair_shells[2 * (first + lane) + 1];
-        size = (sv.prim_off[sa + 1] - sv.prim_off[sa]) * (sv.prim_off[sb + 1] - sv.prim_off[sb]);
-    }
-    int off = size;                                   // inclusive scan of the pair sizes
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, off, o);
-        if (lane >= o) off += y;
-    }
-    off -= size;                                      // exclusive: first lane of pair j
-    const int total = __shfl_sync(0xffffffffu, off + size, 31);
-    int j = 0;
-    for (int q = 1; q < np; ++q)
-        if (__shfl_sync(0xffffffffu, off, q) <= lane) j = q;
-    const int my_off = __shfl_sync(0xffffffffu, off, j);
-    const int my_size = __shfl_sync(0xffffffffu, size, j);
-    const int pi = first + j;
-    const bool in = lane < total;
-    const int sa = pair_shells[2 * pi], sb = pair_shells[2 * pi + 1];
-    const double* A = sv.centre + 3 * sa;
-    const double* B = sv.centre + 3 * sb;
-    const double ABx = A[0] - B[0], ABy = A[1] - B[1], ABz = A[2] - B[2];
-    const double ab2 = ABx * ABx + ABy * ABy + ABz * ABz;
-    const int a0 = sv.prim_off[sa], b0 = sv.prim_off[sb];
-    const int nb = sv.prim_off[sb + 1] - b0;
-    const int k = lane - my_off;
-    bool keep = false;
-    double a = 0.0, b = 0.0;
-    int i = 0, jj = 0;
-    if (in) {
-        i = a0 + k / nb;
-        jj = b0 + k % nb;
-        a = sv.expo[i];
-        b = sv.expo[jj];
-        keep = gs::prim_pair_kept(a, b, ab2, max_exp);
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    const unsigned pair_mask = (my_size >= 32 ? 0xffffffffu : ((1u << my_size) - 1u)) << my_off;
-    const unsigned mine = m & pair_mask;
-    const int base = pair_prim_off[pi];
-    if (keep) {
-        const int r = base + __popc(mine & ((1u << lane) - 1u));
-        const gs::PrimRec<double> rec = gs::prim_pair(A, B, a, b, ab2, sv.coef[i], sv.coef[jj]);
-        p64[r] = rec;
-        if (p32) p32[r] = gs::prim_pair32(rec);
-    }
-    if (in && lane == my_off) {
-        gs::PairRec pr;
-        pr.ABx = ABx; pr.ABy = ABy; pr.ABz = ABz;
-        pr.prim_off = base;
-        pr.nprim = __popc(mine);
-        pr.sa = sa; pr.sb = sb;
-        pr.qmax = 0.0f; pr.pad = 0;
-        pairs[pi] = pr;
-        if (kept) kept[pi] = pr.nprim;
-    }
+    if (lane < len) pair_eval(sv, pair_shells, q[lane], p64, p32);    // the last partial batch
 }
 
 __global__ void k_set_qmax(gs::PairRec* pairs, const double* __restrict__ q, int npairs) {
@@ -368,7 +443,9 @@ int gs_pairs_build(const double* centre, const int* l, const int* prim_off, cons
     if (npairs == 0) return GS_OK;
     gs::ShellView sv{centre, l, prim_off, expo, coef};
     if (ngroups > 0) {
-        k_pairs_build_packed<<<(unsigned)(((long long)ngroups * 32 + 255) / 256), 256, 0, S(stream)>>>(
+        const long long warps = ((long long)ngroups + kPairGroupsPerWarp - 1) / kPairGroupsPerWarp;
+        k_pairs_build_compact<<<(unsigned)((warps + kPairWarps - 1) / kPairWarps), 32 * kPairWarps,
+                                0, S(stream)>>>(
             sv, ngroups, group_start, pair_shells, pair_prim_off, (gs::PairRec*)pair_rec,
             (gs::PrimRec<double>*)prim64, (gs::PrimRec<float>*)prim32, max_exp, kept);
         return check_launch();

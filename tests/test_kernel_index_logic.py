@@ -143,8 +143,32 @@ def test_symmetry_kernel_element_decomposition():
     assert np.array_equal(~zero[keys[:, 0], keys[:, 1], keys[:, 2], keys[:, 3]], g["o2_nonzero"])
 
 
+def test_pair_queue_compaction():
+    """k_pairs_build_compact's queue restated: a warp pushes each chunk's kept candidates
+    (ballot-ranked) and evaluates full batches of 32 off the front, then the rest; every
+    kept candidate is evaluated exactly once, at its own record slot, and the queue never
+    holds more than its 64 entries."""
+    rng = np.random.default_rng(11)
+    for trial in range(200):
+        chunks = [rng.random(32) < rng.uniform(0.05, 0.95) for _ in range(rng.integers(1, 12))]
+        q, evaluated, slot, peak = [], [], 0, 0
+        for keep in chunks:
+            for lane in range(32):           # q[len + rank] = candidate, for kept lanes
+                if keep[lane]:
+                    q.append(slot)
+                    slot += 1
+            peak = max(peak, len(q))
+            if len(q) >= 32:                 # lane l evaluates q[l]; q[l] = q[l + 32]
+                evaluated += q[:32]
+                q = q[32:]
+            assert len(q) < 32
+        evaluated += q                       # the last partial batch
+        assert sorted(evaluated) == list(range(slot))
+        assert peak <= 64
+
+
 def test_packed_pair_build_lane_mapping():
-    """k_pairs_build_packed restated lane by lane: every primitive pair of every shell pair
+    """The grouped pair build's lane mapping restated lane by lane: every primitive pair of every shell pair
     is taken by exactly one lane, and the kept ones land at the same record slots, in the
     same order, as the one-pair-per-warp form (rank among the pair's kept lanes)."""
     from gaussium_gb300.engine import pair_groups
