@@ -15,8 +15,8 @@
  *     the caller's next synchronisation.
  *   - Records (sizes from gs_record_sizes):
  *       PairRec  48 B  {double AB[3]; int prim_off, nprim, sa, sb; float qmax; int pad;}
- *       Prim64   80 B  {double p, 1/(2p), P[3], PA[3], Kp, pad;}
- *       Prim32   48 B  {float  p, 1/(2p), P[3], PA[3], Kp, pad[3];}
+ *       Prim64   80 B  {double p, 1/(2p), P[3], PA[3], Kp, pad;}   pad = first shell's exponent
+ *       Prim32   48 B  {float  p, 1/(2p), P[3], PA[3], Kp, pad[3];}   pad[0] = the same
  *       WriteTask 24 B {int bra, ket, code, pad; long long off;}
  *   - Shells: l <= 2, Cartesian components in the reference order
  *     (s; x,y,z; xx,yy,zz,xy,xz,yz -- factory/primitive_basis_factory.py:5-86), effective
