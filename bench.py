@@ -361,15 +361,17 @@ def run_gpu(args, rank, world):
                            "before the timed steps (e2e_with_planning builds it per step)"}
         del pipe, host_out
         torch.cuda.empty_cache()
-        # the same batch as a caller with new quartets every step sees it: shells in,
-        # QuartetBatch planning (canonical order, class sort, primitive-pair records), the
-        # kernels and the blocks out, one step after another, nothing overlapped
+        # the same batch as a caller with new quartets every step sees it: shells and
+        # quartets in, QuartetBatch planning on the device (canonical order, class sort,
+        # primitive-pair records), the kernels and the blocks out, one step after another,
+        # nothing overlapped
         host_blk = torch.empty(batch.total, dtype=torch.float64).pin_memory()
         nplan = max(1, min(args.steps, 3))
 
         def planned_step():
             dsn = engine.DeviceShells(sb)
-            bn = engine.QuartetBatch(dsn, quartets, want32=False, max_exp=args.prim_screen)
+            bn = engine.QuartetBatch(dsn, quartets, want32=False, max_exp=args.prim_screen,
+                                     plan="device")
             on = torch.empty(bn.total, dtype=torch.float64, device="cuda")
             bn.run(on, 64)
             host_blk.copy_(on)
@@ -386,10 +388,10 @@ def run_gpu(args, rank, world):
             "ms_per_step": plan_ms, "steps": nplan,
             "h2d_bytes_per_step": int(sum(getattr(sb, k).nbytes for k in
                                           ("centre", "l", "prim_off", "expo", "coef",
-                                           "comp_scale", "func_off")) + bn.tasks.numel()),
+                                           "comp_scale", "func_off", "nprim")) + quartets.nbytes),
             "d2h_bytes_per_step": int(batch.total * 8),
-            "api": "gaussium_gb300.engine.DeviceShells + QuartetBatch(quartets) + run, "
-                   "blocks copied to pinned host memory"}
+            "api": "gaussium_gb300.engine.DeviceShells + QuartetBatch(quartets, "
+                   "plan='device') + run, blocks copied to pinned host memory"}
         del host_blk, bn
         torch.cuda.empty_cache()
 

@@ -195,6 +195,7 @@ class DeviceShells:
         self.coef = t(sb.coef, torch.float64)
         self.comp_scale = t(sb.comp_scale, torch.float64)
         self.func_off = t(sb.func_off, torch.int32)
+        self.nprim = t(sb.nprim, torch.int64)          # primitives per shell (device planning)
         self.nshell = sb.nshell
         self.nbf = sb.nbf
 
@@ -216,6 +217,23 @@ def pair_groups(sizes, lanes=32):
     start = (r == 0) | ((r == 2) & ~quad) | ((r & 1).astype(bool) & ~quad & ~half)
     out = np.flatnonzero(start[:n]).astype(np.int32)
     return np.concatenate([out, np.array([n], dtype=np.int32)])
+
+
+def pair_groups_device(sizes, lanes=32):
+    """pair_groups on a device tensor of sizes (the same groups; int32 device tensor)."""
+    dev = sizes.device
+    n = sizes.numel()
+    if n == 0:
+        return torch.zeros(1, dtype=torch.int32, device=dev)
+    m = -(-n // 4) * 4
+    sz = torch.zeros(m, dtype=torch.int64, device=dev)
+    sz[:n] = sizes
+    quad = (sz.view(-1, 4).sum(1) <= lanes).repeat_interleave(4)
+    half = (sz.view(-1, 2).sum(1) <= lanes).repeat_interleave(2)
+    r = torch.arange(m, device=dev) % 4
+    start = (r == 0) | ((r == 2) & ~quad) | (((r & 1) == 1) & ~quad & ~half)
+    out = torch.nonzero(start[:n]).flatten().to(torch.int32)
+    return torch.cat([out, torch.tensor([n], dtype=torch.int32, device=dev)])
 
 
 def check_shell_indices(idx, nshell, what):
@@ -279,6 +297,70 @@ class PairSet:
         return self.p64 if precision == 64 else self.p32
 
 
+class DevicePairSet(PairSet):
+    """A PairSet planned on the device from a device tensor of shell pairs (m, 2) int32,
+    l[first] >= l[second] (as canonical quartets give them): the same records, groups and
+    kept counts; the host copies of the pair list and counts are made when first read."""
+
+    def __init__(self, ds: DeviceShells, pair_shells, want32=True, stream=None, max_exp=0.0):
+        dev = ds.device
+        ps = pair_shells.to(device=dev, dtype=torch.int32).reshape(-1, 2).contiguous()
+        m = ps.shape[0]
+        npp = ds.nprim[ps[:, 0].long()] * ds.nprim[ps[:, 1].long()]
+        off = torch.cumsum(npp, 0)
+        total = int(off[-1]) if m else 0
+        if total >= 2 ** 31:
+            raise ValueError("too many primitive pairs for one PairSet")
+        self.ds = ds
+        self.n = m
+        self.shells = ps
+        self.prim_start = (off - npp).to(torch.int32)
+        self.rec = torch.empty(max(1, m) * PAIR_REC, dtype=torch.uint8, device=dev)
+        t = max(1, total)
+        self.p64 = torch.empty(t * PRIM64, dtype=torch.uint8, device=dev)
+        self.p32 = torch.empty(t * PRIM32, dtype=torch.uint8, device=dev) if want32 else None
+        self.nprim_pairs = total
+        self.max_exp = max_exp
+        self.groups = pair_groups_device(npp, 32)
+        self.ngroups = int(self.groups.numel()) - 1
+        self.kept = torch.zeros(max(1, m), dtype=torch.int32, device=dev)
+        self.build(stream)
+        self.nprim_dev = self.kept[:m].long()
+
+    def __getattr__(self, name):
+        # host copies, made on first use
+        if name == "host_shells":
+            v = self.shells.cpu().numpy()
+        elif name == "nprim":
+            v = self.nprim_dev.cpu().numpy()
+        elif name in ("la", "lb"):
+            k = 0 if name == "la" else 1
+            v = self.ds.host.l[self.shells[:, k].cpu().numpy()]
+        else:
+            raise AttributeError(name)
+        setattr(self, name, v)
+        return v
+
+
+_DEVICE_LUTS = {}
+
+
+def _device_luts(dev):
+    """The canonicalisation and block-size tables (and each pair-class combination's
+    heavy threshold) on a device."""
+    if dev not in _DEVICE_LUTS:
+        pos, code, pcb, pck = _CANON_LUT
+        thr = [heavy_threshold(PAIR_ORDER[c // 6] + PAIR_ORDER[c % 6]) for c in range(36)]
+        _DEVICE_LUTS[dev] = {
+            "pos": torch.as_tensor(np.asarray(pos, dtype=np.int64)).to(dev),
+            "code": torch.as_tensor(np.asarray(code, dtype=np.int32)).to(dev),
+            "cls": torch.as_tensor(np.asarray(pcb * 6 + pck, dtype=np.int64)).to(dev),
+            "size": torch.as_tensor(np.asarray(_SIZE_LUT, dtype=np.int64)).to(dev),
+            "thr": torch.as_tensor(np.asarray(thr, dtype=np.int64)).to(dev),
+        }
+    return _DEVICE_LUTS[dev]
+
+
 # ---------------------------------------------------------------------- shell-quartet blocks
 def _canonicalize_rows(l4):
     """canonicalize, evaluated row by row from the rule (the table below is built from it)."""
@@ -325,7 +407,16 @@ class QuartetBatch:
     (a,b,c,d) order, row-major.  Host preparation sorts the quartets by class and
     primitive counts; ``run`` launches one kernel per class."""
 
-    def __init__(self, ds: DeviceShells, quartets, want32=True, max_exp=0.0):
+    def __init__(self, ds: DeviceShells, quartets, want32=True, max_exp=0.0, plan="host"):
+        """``plan="device"``: the same planning with torch on the device (quartets may be a
+        host array or a device tensor); only the class histogram and heavy counts come back
+        to the host, and the host copies of offsets and primitive counts are made when
+        first read."""
+        if plan == "device":
+            self._plan_device(ds, quartets, want32, max_exp)
+            return
+        if plan != "host":
+            raise ValueError(f"plan must be 'host' or 'device', not {plan!r}")
         q = np.ascontiguousarray(quartets, dtype=np.int64).reshape(-1, 4)
         sb = ds.host
         check_shell_indices(q, sb.nshell, "shell quartets")
@@ -386,6 +477,78 @@ class QuartetBatch:
         self.sorted_ket_nprim = nk[order]
         work = self.sorted_bra_nprim * self.sorted_ket_nprim
         self.heavy = [heavy_counts(cls, work[s:e]) for cls, s, e in self.segments]
+
+    def _plan_device(self, ds, quartets, want32, max_exp):
+        dev = ds.device
+        sb = ds.host
+        q = torch.as_tensor(quartets).to(device=dev, dtype=torch.int64).reshape(-1, 4)
+        n = q.shape[0]
+        if n and (int(q.min()) < 0 or int(q.max()) >= sb.nshell):
+            raise ValueError(f"shell quartets hold a shell index outside [0, {sb.nshell})")
+        lut = _device_luts(dev)
+        l4 = ds.l.long()[q]
+        li = ((l4[:, 0] * 3 + l4[:, 1]) * 3 + l4[:, 2]) * 3 + l4[:, 3]
+        qc = torch.gather(q, 1, lut["pos"][li])             # canonical shells
+        off = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        off[1:] = torch.cumsum(lut["size"][li], 0)
+        self.n = n
+        self._offsets_dev = off
+        self.total = int(off[-1])
+        self.pairs = DevicePairSet(ds, torch.cat([qc[:, 0:2], qc[:, 2:4]], 0), want32=want32,
+                                   max_exp=max_exp)
+        npr = ds.nprim
+        self.full_prim_quartets = int((npr[qc[:, 0]] * npr[qc[:, 1]] * npr[qc[:, 2]] *
+                                       npr[qc[:, 3]]).sum()) if n else 0
+        nb = self.pairs.nprim_dev[:n]
+        nk = self.pairs.nprim_dev[n:]
+        w = nb * nk
+        cls = lut["cls"][li]
+        self.prim_quartets = int(w.sum()) if n else 0
+        # the host form's order: class, then descending nb*nk, nb, nk; ties in input order
+        wb = int(nb.max()).bit_length() if n else 1
+        wk = int(nk.max()).bit_length() if n else 1
+        ww = int(w.max()).bit_length() if n else 1
+        key = (cls << ww) | ((1 << ww) - 1 - w)
+        key = (key << wb) | ((1 << wb) - 1 - nb)
+        key = (key << wk) | ((1 << wk) - 1 - nk)
+        order = torch.sort(key, stable=True).indices
+        tasks = torch.zeros((n, 6), dtype=torch.int32, device=dev)   # WRITE_TASK layout
+        tasks[:, 0] = order.to(torch.int32)
+        tasks[:, 1] = (order + n).to(torch.int32)
+        tasks[:, 2] = lut["code"][li][order]
+        tasks[:, 4:6] = off[:-1][order].contiguous().view(torch.int32).view(n, 2)
+        self.tasks = tasks.view(torch.uint8).reshape(-1)
+        self.ds = ds
+        scls = cls[order]
+        ws = w[order]
+        nper = torch.bincount(scls, minlength=36).cpu().numpy()
+        hs = torch.zeros(36, dtype=torch.int64, device=dev).index_add_(
+            0, scls, (ws >= lut["thr"][scls]).long())
+        hc = torch.zeros(36, dtype=torch.int64, device=dev).index_add_(
+            0, scls, (ws >= COOP_PRIM_QUARTETS).long())
+        hs, hc = hs.cpu().numpy(), hc.cpu().numpy()
+        self.segments, self.heavy = [], []
+        start = 0
+        for c in range(36):
+            if nper[c]:
+                (la, lb), (lc, ld) = PAIR_ORDER[c // 6], PAIR_ORDER[c % 6]
+                self.segments.append(((la, lb, lc, ld), start, start + int(nper[c])))
+                self.heavy.append((int(hs[c]), int(hc[c])))
+                start += int(nper[c])
+        self._sorted_dev = (nb[order], nk[order])
+
+    def __getattr__(self, name):
+        # host copies of a device-planned batch, made on first use
+        if name == "offsets" and "_offsets_dev" in self.__dict__:
+            v = self._offsets_dev.cpu().numpy()
+        elif name in ("sorted_bra_nprim", "sorted_ket_nprim") and "_sorted_dev" in self.__dict__:
+            v = self._sorted_dev[0 if name == "sorted_bra_nprim" else 1].cpu().numpy()
+        elif name == "tasks_host" and "_sorted_dev" in self.__dict__:
+            v = self.tasks.cpu().numpy().view(WRITE_TASK_DTYPE)
+        else:
+            raise AttributeError(name)
+        setattr(self, name, v)
+        return v
 
     def class_counts(self):
         return {cls: e - s for cls, s, e in self.segments}

@@ -232,3 +232,25 @@ def test_cooperative_jk_matches_plain_forms(gpu_lib):
     finally:
         engine.SPLIT_OFF.clear()
         autotune.reset(eng.segments)
+
+
+def test_device_planning_matches_host_planning_gpu(gpu_lib):
+    """QuartetBatch planned on the device against the host planning, with the real pair
+    build and screen: the same task bytes, segments, heavy counts and offsets, and
+    bit-identical blocks."""
+    import torch
+    from gaussium_gb300 import engine
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(20000, seed=8)
+    ds = engine.DeviceShells(sb)
+    bh = engine.QuartetBatch(ds, q, want32=True, max_exp=engine.PRIM_SCREEN)
+    bd = engine.QuartetBatch(ds, q, want32=True, max_exp=engine.PRIM_SCREEN, plan="device")
+    assert torch.equal(bd.tasks, bh.tasks)
+    assert bd.segments == bh.segments and bd.heavy == bh.heavy
+    assert np.array_equal(bd.offsets, bh.offsets)
+    for prec in (64, 32):
+        oh = torch.zeros(bh.total, dtype=torch.float64, device="cuda")
+        od = torch.zeros_like(oh)
+        bh.run(oh, prec)
+        bd.run(od, prec)
+        assert torch.equal(od, oh), prec

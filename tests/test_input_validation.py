@@ -174,3 +174,40 @@ def test_split_forms_by_class_form(monkeypatch):
     assert engine.split_forms(cls, 64, (5, 0)) == [(0, 0, None)]
     w = np.array([600, 300, 200, 128, 127, 40, 1])
     assert engine.heavy_counts(cls, w) == (int(np.count_nonzero(w >= engine.heavy_threshold(cls))), 4)
+
+
+def test_device_planning_matches_host_planning(monkeypatch):
+    """QuartetBatch(plan="device") restated with torch on the CPU (the pair records
+    stubbed: every primitive pair kept): the same task list byte for byte, the same class
+    segments, heavy counts, block offsets and primitive-quartet totals as the host
+    planning."""
+    import torch
+    from gaussium_gb300.workloads import random_shell_quartets
+    sb, q, _ = random_shell_quartets(5000, seed=3)
+
+    class StubPairs:
+        def __init__(self, ds, pairs, want32=True, max_exp=0.0):
+            self.nprim = (sb.nprim[pairs[:, 0]].astype(np.int64) * sb.nprim[pairs[:, 1]])
+
+    def stub_build(self, stream=None, want32=True):
+        self.kept[:self.n] = (self.ds.nprim[self.shells[:, 0].long()] *
+                              self.ds.nprim[self.shells[:, 1].long()]).to(torch.int32)
+
+    ds = _host_only(sb)
+    ds.device = torch.device("cpu")
+    ds.l = torch.as_tensor(sb.l.astype(np.int32))
+    ds.nprim = torch.as_tensor(sb.nprim.astype(np.int64))
+    monkeypatch.setattr(engine, "PairSet", StubPairs)
+    monkeypatch.setattr(engine.DevicePairSet, "build", stub_build)
+    monkeypatch.setattr(engine.torch.Tensor, "to", lambda self, *a, **k: self)
+    host = engine.QuartetBatch(ds, q)
+    dev = engine.QuartetBatch(ds, q, plan="device")
+    assert np.array_equal(dev.tasks.numpy(), host.tasks.numpy())
+    assert dev.segments == host.segments
+    assert dev.heavy == host.heavy
+    assert np.array_equal(dev.offsets, host.offsets) and dev.total == host.total
+    assert np.array_equal(dev.sorted_bra_nprim, host.sorted_bra_nprim)
+    assert (dev.prim_quartets, dev.full_prim_quartets) == (host.prim_quartets,
+                                                           host.full_prim_quartets)
+    with pytest.raises(ValueError):
+        engine.QuartetBatch(ds, np.array([[0, 1, 2, sb.nshell]]), plan="device")
