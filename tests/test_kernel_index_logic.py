@@ -229,3 +229,14 @@ def test_heavy_threshold_every_class():
         v = gen_eri.VrrGen(cls)
         nacc = len(v.e_targets) * len(v.f_targets)
         assert engine.heavy_threshold(cls) == max(engine.HEAVY_PRIM_QUARTETS, 2 * nacc)
+
+
+def test_device_pair_groups_match_host():
+    """pair_groups_device (torch, here on the CPU) gives the host pair_groups' starts."""
+    import torch
+    from gaussium_gb300.engine import pair_groups, pair_groups_device
+    rng = np.random.default_rng(13)
+    for n in (0, 1, 2, 3, 4, 5, 7, 8, 1001, 40000):
+        s = rng.integers(1, 40, n)
+        got = pair_groups_device(torch.as_tensor(s)).numpy()
+        assert np.array_equal(got, pair_groups(s)), n
