@@ -111,3 +111,36 @@ def test_wide_program_matches_generated_code(cls, grouped):
         if done == 2:
             break
     assert done > 0
+
+
+@pytest.mark.parametrize("cls", [(2, 1, 2, 1), (2, 2, 2, 1), (2, 2, 2, 2)])
+def test_bank_spread_keeps_slots_and_cuts_conflicts(cls):
+    """The slot renaming of the ungrouped program keeps the Boys value slots and the slot
+    count, maps slots one to one, and lowers the shared-memory wavefronts of the operand
+    loads (FP32: 1 ideal; FP64: 2)."""
+    real = gen_eri.bank_spread
+    try:
+        gen_eri.bank_spread = lambda vrec, vseg, vtgt, nvslot, L: (vrec, vtgt, nvslot)
+        p0 = gen_eri.wide_program(cls)
+    finally:
+        gen_eri.bank_spread = real
+    p1 = gen_eri.wide_program(cls)
+    assert p1["nvslot"] == p0["nvslot"]
+    L = p1["L"]
+    ren = {}
+    for r in range(len(p0["vrec"]) // 8):
+        w0, w1 = p0["vrec"][8 * r: 8 * r + 8], p1["vrec"][8 * r: 8 * r + 8]
+        assert w0[0] >> 16 == w1[0] >> 16
+        for t in range(1 + (w0[0] >> 16)):
+            a, b = w0[t] & 0xffff, w1[t] & 0xffff
+            assert ren.setdefault(a, b) == b
+            assert w0[t] >> 16 == w1[t] >> 16
+    for a, b in zip(p0["vtgt"], p1["vtgt"]):
+        assert ren.setdefault(a, b) == b
+    assert len(set(ren.values())) == len(ren)              # one to one
+    assert all(ren.get(m, m) == m for m in range(L + 1))   # Boys values stay put
+    assert max(ren.values()) < p1["nvslot"]
+    for eb in (4, 8):
+        w0 = gen_eri.bank_wavefronts(p0["vrec"], p0["vseg"], eb)
+        w1 = gen_eri.bank_wavefronts(p1["vrec"], p1["vseg"], eb)
+        assert w1 < 0.85 * w0, (eb, w0, w1)
