@@ -644,18 +644,12 @@ int gs_fock_jk_mixed(int la, int lb, int lc, int ld, const void* pair_rec, const
 static __device__ __align__(256) unsigned char g_noalloc_ws[256 + 2 * (size_t)GS_NOALLOC_MAX_TASKS * 8];
 
 namespace {
-constexpr int kMaxDevices = 64;
-void* g_noalloc_ptr[kMaxDevices] = {nullptr};
-
+// looked up on every call: a cached address would go stale when a device reset reloads
+// the module
 int noalloc_workspace(void** ptr) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GS_ERR_CUDA;
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_ws) != cudaSuccess || !p) return GS_ERR_CUDA;
-        g_noalloc_ptr[dev] = p;
-    }
-    *ptr = g_noalloc_ptr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_ws) != cudaSuccess || !p) return GS_ERR_CUDA;
+    *ptr = p;
     return GS_OK;
 }
 }  // namespace
