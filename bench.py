@@ -366,7 +366,7 @@ def run_gpu(args, rank, world):
         # primitive-pair records), the kernels and the blocks out, one step after another,
         # nothing overlapped
         host_blk = torch.empty(batch.total, dtype=torch.float64).pin_memory()
-        nplan = max(1, min(args.steps, 3))
+        nplan = max(1, min(args.steps, 5))
 
         def planned_step():
             dsn = engine.DeviceShells(sb)
@@ -376,7 +376,10 @@ def run_gpu(args, rank, world):
             bn.run(on, 64)
             host_blk.copy_(on)
             return bn
-        planned_step()
+        # warm-up as in the other arms: the first two steps are slower (block download
+        # 55 ms and shell upload up to 240 ms, against 10 ms and 8 ms after)
+        for _ in range(max(3, args.warmup)):
+            planned_step()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(nplan):
@@ -385,7 +388,7 @@ def run_gpu(args, rank, world):
         plan_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / nplan, world)
         e2e["e2e_with_planning"] = {
             "value": args.quartets * world / (plan_ms * 1e-3), "unit": UNIT,
-            "ms_per_step": plan_ms, "steps": nplan,
+            "ms_per_step": plan_ms, "steps": nplan, "warmup": max(3, args.warmup),
             "h2d_bytes_per_step": int(sum(getattr(sb, k).nbytes for k in
                                           ("centre", "l", "prim_off", "expo", "coef",
                                            "comp_scale", "func_off", "nprim")) + quartets.nbytes),
