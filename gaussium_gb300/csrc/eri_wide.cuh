@@ -53,12 +53,13 @@ template <int LA, int LB, int LC, int LD, typename T, int VG = 1, int RQ = 1> st
     // node slots of the program this form runs (the grouped form has its own schedule)
     static constexpr int NVS = VG == 1 ? W::NVSLOT : W::NVSLOT_G;
     // primitive quartets set up per round: 32, or 16 for a form whose node buffers are
-    // large -- grouped with more than 1024 slots, or an ungrouped class of total angular
+    // large -- grouped with more than 1088 slots (above (pp|pp)'s 8 x 132, its slot count
+    // padded for the banks), or an ungrouped class of total angular
     // momentum 7 or more whose VRR buffers would outgrow the HRR's (measured: (dd|dp)
     // 17.7 -> 16.0 ms at 2,000,000 quartets; the smaller classes lose setup parallelism)
     static constexpr int VRR32 = 32 * kNCoef + 32 * (G::L + 1) + VG * RQ * NVS;
     static constexpr int HRR_W = W::HSIZE + G::NA * G::NB + G::NC * G::ND;
-    static constexpr int SB = kSetupBatch > 16 && ((VG * RQ > 1 && VG * RQ * NVS > 1024) ||
+    static constexpr int SB = kSetupBatch > 16 && ((VG * RQ > 1 && VG * RQ * NVS > 1088) ||
                                                    (VG * RQ == 1 && G::L >= 7 && VRR32 > HRR_W))
                                   ? 16 : kSetupBatch;
     static_assert(SB % RQ == 0, "setup rounds hold whole stacks");

@@ -474,28 +474,38 @@ def vrr_waves(nodes, L, target_slots, wave=32):
     return vrec, vseg, phys, top
 
 
-def bank_spread(vrec, vseg, vtgt, nvslot, L):
-    """Rename the node slots of an ungrouped (waves of 32) program so that the slots one
-    instruction touches across the warp fall in different shared-memory banks: each wave's
-    operands of one term, its outputs, and each run of 32 targets.  A slot s sits in bank
-    s mod 32 (FP32 words; an FP64 slot spans banks 2s, 2s+1, so FP64 lanes of one half-warp
-    conflict when their slots agree mod 16).  Greedy colouring: slots in order of the
-    weight of their groups take the bank (with room left) least shared with the slots
-    already placed in their groups, FP64 half-warp pairs counted too; then bank b's slots
-    become b, b + 32, b + 64, ...  The Boys value slots 0..L stay where the kernel writes
-    them.  A renaming changes no value's lifetime, so the schedule's hazard rules hold."""
+def bank_spread(vrec, vseg, vtgt, nvslot, L, wave=32):
+    """Rename the node slots of a program so that the slots one instruction touches across
+    the warp fall in different shared-memory banks.
+
+    Waves of 32 (the ungrouped program): each wave's operands of one term, its outputs,
+    and each run of 32 targets.  A slot s sits in bank s mod 32 (FP32 words; an FP64 slot
+    spans banks 2s, 2s+1, so FP64 lanes of one half-warp conflict when their slots agree
+    mod 16).  Waves of 32/VG (the grouped program): lane g*wave + j runs record j on group
+    g's buffer, at g*NVS + slot.  With the wave's slots distinct mod ``wave`` and NVS = wave
+    (mod 32), the groups' copies land ``wave`` banks apart, so the warp (FP32) and each
+    half-warp (FP64) read distinct banks; the slot count is padded to that residue.
+
+    Greedy colouring: slots in order of the weight of their groups take the class (with
+    room left) least shared with the slots already placed in their groups, FP64 half-warp
+    pairs counted too for waves of 32; then class b's slots become b, b + M, b + 2M, ...
+    (M = 32 or ``wave``).  The Boys value slots 0..L stay where the kernel writes them.  A
+    renaming changes no value's lifetime, so the schedule's hazard rules hold.  Returns
+    (vrec, vtgt, nvslot)."""
     import collections
-    groups = []                                   # (slots, half) ; half: lanes 0-15 / 16-31
+    M = 32 if wave == 32 else wave
+    groups = []
     for noff, _, cnt, _, _, _ in vseg:
-        for w0 in range(0, cnt, 32):
-            recs = [vrec[8 * (noff + n): 8 * (noff + n) + 8] for n in range(w0, min(cnt, w0 + 32))]
+        for w0 in range(0, cnt, wave):
+            recs = [vrec[8 * (noff + n): 8 * (noff + n) + 8] for n in range(w0, min(cnt, w0 + wave))]
             nt = recs[0][0] >> 16
             groups.append([r[0] & 0xffff for r in recs])
             for t in range(nt):
                 groups.append([r[1 + t] & 0xffff for r in recs])
-    for k in range(0, len(vtgt), 32):
-        groups.append(list(vtgt[k:k + 32]))
-    w32 = collections.defaultdict(collections.Counter)      # same warp: avoid equal mod 32
+    if wave == 32:
+        for k in range(0, len(vtgt), 32):
+            groups.append(list(vtgt[k:k + 32]))
+    w32 = collections.defaultdict(collections.Counter)      # same wave: avoid equal mod M
     w16 = collections.defaultdict(collections.Counter)      # same half-warp: equal mod 16
     for g in groups:
         u = sorted(set(g))
@@ -503,22 +513,24 @@ def bank_spread(vrec, vseg, vtgt, nvslot, L):
             for b in u[i + 1:]:
                 w32[a][b] += 1
                 w32[b][a] += 1
+        if wave < 32:
+            continue
         for half in (g[:16], g[16:]):
             u = sorted(set(half))
             for i, a in enumerate(u):
                 for b in u[i + 1:]:
                     w16[a][b] += 1
                     w16[b][a] += 1
-    cap = [len(range(b, nvslot, 32)) for b in range(32)]    # ids stay below nvslot
+    cap = [len(range(b, nvslot, M)) for b in range(M)]      # ids stay below nvslot
     bank = {}
-    fill = [0] * 32
-    for s in range(L + 1):                       # Boys slots: bank s, first row
-        bank[s] = s
-        fill[s] += 1
+    fill = [0] * M
+    for s in range(L + 1):                       # Boys slots keep their ids
+        bank[s] = s % M
+        fill[s % M] += 1
     order = sorted((s for s in range(L + 1, nvslot)),
                    key=lambda s: (-(sum(w32[s].values()) + sum(w16[s].values())), s))
     for s in order:
-        cost = [0] * 32
+        cost = [0] * M
         for n, c in w32[s].items():
             if n in bank:
                 cost[bank[n]] += 2 * c
@@ -527,14 +539,14 @@ def bank_spread(vrec, vseg, vtgt, nvslot, L):
                 b = bank[n] % 16
                 cost[b] += c
                 cost[b + 16] += c
-        best = min((b for b in range(32) if fill[b] < cap[b]), key=lambda b: (cost[b], fill[b], b))
+        best = min((b for b in range(M) if fill[b] < cap[b]), key=lambda b: (cost[b], fill[b], b))
         bank[s] = best
         fill[best] += 1
-    rank = [0] * 32
+    rank = [0] * M
     new = {}
     for s in range(nvslot):                      # Boys slots first, then in slot order
         b = bank[s]
-        new[s] = 32 * rank[b] + b
+        new[s] = M * rank[b] + b
         rank[b] += 1
     out = list(vrec)
     for r in range(len(vrec) // 8):
@@ -544,20 +556,27 @@ def bank_spread(vrec, vseg, vtgt, nvslot, L):
         for t in range(nt):
             x = w[1 + t]
             out[8 * r + 1 + t] = (x & ~0xffff) | new[x & 0xffff]
+    if wave < 32:
+        nvslot += (wave - nvslot) % 32
     return out, [new[t] for t in vtgt], nvslot
 
 
-def bank_wavefronts(vrec, vseg, elem_bytes):
+def bank_wavefronts(vrec, vseg, elem_bytes, wave=32, nvs=0):
     """Average shared-memory wavefronts per warp-wide operand load of a program (1 ideal
-    for 4-byte, 2 for 8-byte elements): the distinct slots of each bank, per warp (4 B)
-    or per half-warp (8 B)."""
+    for 4-byte, 2 for 8-byte elements): the distinct addresses of each bank, per warp
+    (4 B) or per half-warp (8 B).  Lane g*wave + j reads record j's slot in group g's
+    buffer, at g*nvs + slot (one group for waves of 32)."""
+    vg = 32 // wave
     tot = wf = 0
     for noff, _, cnt, _, _, _ in vseg:
-        for w0 in range(0, cnt, 32):
-            recs = [vrec[8 * (noff + n): 8 * (noff + n) + 8] for n in range(w0, min(cnt, w0 + 32))]
+        for w0 in range(0, cnt, wave):
+            recs = [vrec[8 * (noff + n): 8 * (noff + n) + 8] for n in range(w0, min(cnt, w0 + wave))]
             for t in range(recs[0][0] >> 16):
                 slots = [r[1 + t] & 0xffff for r in recs]
-                parts = [slots] if elem_bytes == 4 else [slots[:16], slots[16:]]
+                lanes = {g * wave + j: g * nvs + x for g in range(vg) for j, x in enumerate(slots)}
+                parts = ([list(lanes.values())] if elem_bytes == 4 else
+                         [[a for ln, a in lanes.items() if ln < 16],
+                          [a for ln, a in lanes.items() if ln >= 16]])
                 n = 0
                 for part in parts:
                     if part:
@@ -617,8 +636,7 @@ def wide_program(cls, wave=32):
            for e in v.e_targets for f in v.f_targets]
     vrec, vseg, phys, nvslot = vrr_waves(nodes, L, [slot(t) for t in tgt], wave)
     vtgt = [phys[slot(t)] for t in tgt]
-    if wave == 32:
-        vrec, vtgt, nvslot = bank_spread(vrec, vseg, vtgt, nvslot, L)
+    vrec, vtgt, nvslot = bank_spread(vrec, vseg, vtgt, nvslot, L, wave)
     vout, vdesc = [], []
     # ---- HRR: arrays, levels, liveness
     arrays = {}          # name -> (size, producer level)

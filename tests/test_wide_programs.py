@@ -113,19 +113,28 @@ def test_wide_program_matches_generated_code(cls, grouped):
     assert done > 0
 
 
-@pytest.mark.parametrize("cls", [(2, 1, 2, 1), (2, 2, 2, 1), (2, 2, 2, 2)])
-def test_bank_spread_keeps_slots_and_cuts_conflicts(cls):
-    """The slot renaming of the ungrouped program keeps the Boys value slots and the slot
-    count, maps slots one to one, and lowers the shared-memory wavefronts of the operand
-    loads (FP32: 1 ideal; FP64: 2)."""
+@pytest.mark.parametrize("grouped", [False, True])
+@pytest.mark.parametrize("cls", [(1, 1, 1, 1), (2, 0, 1, 0), (2, 1, 2, 1), (2, 2, 2, 1), (2, 2, 2, 2)])
+def test_bank_spread_keeps_slots_and_cuts_conflicts(cls, grouped):
+    """The slot renaming keeps the Boys value slots, maps slots one to one within the
+    slot count, and lowers the shared-memory wavefronts of the operand loads (FP32: 1
+    ideal; FP64: 2).  The grouped program's slot count is padded to ``wave`` mod 32, so
+    that the groups' buffers start ``wave`` banks apart."""
+    wave = 32 // gen_eri.vrr_group(cls)[0] if grouped else 32
+    if wave == 32 and grouped:
+        pytest.skip("class has no grouped form")
     real = gen_eri.bank_spread
     try:
-        gen_eri.bank_spread = lambda vrec, vseg, vtgt, nvslot, L: (vrec, vtgt, nvslot)
-        p0 = gen_eri.wide_program(cls)
+        gen_eri.bank_spread = lambda vrec, vseg, vtgt, nvslot, L, wave=32: (vrec, vtgt, nvslot)
+        p0 = gen_eri.wide_program(cls, wave)
     finally:
         gen_eri.bank_spread = real
-    p1 = gen_eri.wide_program(cls)
-    assert p1["nvslot"] == p0["nvslot"]
+    p1 = gen_eri.wide_program(cls, wave)
+    if wave == 32:
+        assert p1["nvslot"] == p0["nvslot"]
+    else:
+        assert p0["nvslot"] <= p1["nvslot"] < p0["nvslot"] + 32
+        assert p1["nvslot"] % 32 == wave % 32
     L = p1["L"]
     ren = {}
     for r in range(len(p0["vrec"]) // 8):
@@ -139,8 +148,9 @@ def test_bank_spread_keeps_slots_and_cuts_conflicts(cls):
         assert ren.setdefault(a, b) == b
     assert len(set(ren.values())) == len(ren)              # one to one
     assert all(ren.get(m, m) == m for m in range(L + 1))   # Boys values stay put
-    assert max(ren.values()) < p1["nvslot"]
+    assert max(ren.values()) < p0["nvslot"]
     for eb in (4, 8):
-        w0 = gen_eri.bank_wavefronts(p0["vrec"], p0["vseg"], eb)
-        w1 = gen_eri.bank_wavefronts(p1["vrec"], p1["vseg"], eb)
-        assert w1 < 0.85 * w0, (eb, w0, w1)
+        w0 = gen_eri.bank_wavefronts(p0["vrec"], p0["vseg"], eb, wave, p0["nvslot"])
+        w1 = gen_eri.bank_wavefronts(p1["vrec"], p1["vseg"], eb, wave, p1["nvslot"])
+        ideal = eb / 4                                     # 1 (FP32) or 2 (FP64)
+        assert w1 <= w0 and (w1 < 0.9 * w0 or w0 <= ideal + 1e-9), (eb, w0, w1)
