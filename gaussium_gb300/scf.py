@@ -1,5 +1,5 @@
 """Host-side SCF driver (FP64 numpy) with the reference's algorithm, for use where the
-reference package itself is not installed (it is not on the GPU machine).
+reference package itself is not installed (it is not a dependency of this library).
 
 Restated from the reference (file:line within the reference project):
   LinearAlgebra           hartreefock/linear_algebra.py:4-30   canonical orthogonalisation, eigh

@@ -1,8 +1,8 @@
 /*
  * ORACLE — test infrastructure only.  CPU restatement of the reference Gaussium's
- * two-electron repulsion integral path, used by tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference arm of bench.py as the checker.  Nothing in the product
- * library links, loads or calls this file.
+ * two-electron repulsion integral path.  tests/ and __graft_entry__.smoke() compare the
+ * GPU results with it; the cpu_baseline leg and reference arm of bench.py time it on the
+ * host cores.  Nothing in the product library links, loads or calls this file.
  *
  * What it restates (file:line within the reference project):
  *   boys_function            integrals/boys_function.py:4-54   -> oracle_boys_reference

@@ -3,7 +3,8 @@
 ctypes front end of ``eri_oracle.c`` (the CPU restatement of the reference's
 Obara-Saika ERI and Boys function) plus numpy restatements of the reference's Fock
 builders and SCF loop.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of
-``bench.py`` import this module, always as the checker and never as the measured path.
+``bench.py`` import this module: the tests and smoke compare the GPU results with it, the
+CPU legs time it on the host cores.  The product path never calls it.
 
 Restated reference functions (file:line within the reference project):
   FockMatrixRestricted.create            hartreefock/fock_matrix.py:12-22

@@ -3,7 +3,7 @@
 Test infrastructure, used solely by ``make_golden.py`` to produce the committed golden
 vectors under ``tests/golden/``.  The reference source tree is read in place and never
 written to (``sys.dont_write_bytecode``).  Nothing on the product path imports this file,
-and the GPU machine does not have the reference tree at all.
+and the GPU tests run without the reference tree.
 
 Shims (none of them changes the reference's arithmetic on the ERI path):
 

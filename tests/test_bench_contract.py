@@ -1,5 +1,5 @@
 """The reference arm of bench.py runs on CPU (the oracle port on the host cores) and prints
-the one JSON line the driver reads, with the keys and values its contract requires; under
+its one JSON line, with the keys and values the bench contract requires; under
 torchrun only rank 0 prints and the other ranks exit 0 without work."""
 import json
 import os

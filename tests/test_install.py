@@ -58,7 +58,7 @@ def test_install_reroutes_post_scf_transforms():
 
 def test_install_on_the_real_reference_package():
     """Acceptance on the reference itself (when its source tree is given by the
-    GAUSSIUM_REFERENCE environment variable; the GPU machine has none): install() rebinds
+    GAUSSIUM_REFERENCE environment variable; skipped without it): install() rebinds
     hartreefock/hartree_fock.py:14,39-41 and kohnsham/kohn_sham.py:1-2 of the real package,
     the reference's own HartreeFock constructor then takes the basis list instead of
     building the N^4 tensor, and uninstall() restores every original."""

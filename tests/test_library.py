@@ -90,6 +90,7 @@ def test_new_drop_ins_refuse_cpu_tensors():
 
 
 def test_every_entry_point_is_documented_for_integrators():
-    """Each C-ABI symbol the header declares has its row in INTEGRATION.md."""
+    """Each C-ABI symbol the header declares has its row in the integration guide at the
+    repository root."""
     doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     assert [n for n in declared_symbols() if n not in doc] == []
