@@ -176,17 +176,22 @@ def test_split_forms_by_class_form(monkeypatch):
     assert engine.heavy_counts(cls, w) == (int(np.count_nonzero(w >= engine.heavy_threshold(cls))), 4)
 
 
-def test_device_planning_matches_host_planning(monkeypatch):
+@pytest.mark.parametrize("case", ["random", "empty", "one", "repeated", "int32"])
+def test_device_planning_matches_host_planning(monkeypatch, case):
     """QuartetBatch(plan="device") restated with torch on the CPU (the pair records
     stubbed: every primitive pair kept): the same task list byte for byte, the same class
     segments, heavy counts, block offsets and primitive-quartet totals as the host
-    planning."""
+    planning, for 5,000 seeded quartets, none, one, one repeated 7 times, and int32
+    input."""
     import torch
     from gaussium_gb300.workloads import random_shell_quartets
     sb, q, _ = random_shell_quartets(5000, seed=3)
+    q = {"random": q, "empty": np.zeros((0, 4), dtype=np.int64), "one": q[:1],
+         "repeated": np.repeat(q[:1], 7, 0), "int32": q.astype(np.int32)}[case]
 
     class StubPairs:
         def __init__(self, ds, pairs, want32=True, max_exp=0.0):
+            pairs = np.asarray(pairs).reshape(-1, 2)
             self.nprim = (sb.nprim[pairs[:, 0]].astype(np.int64) * sb.nprim[pairs[:, 1]])
 
     def stub_build(self, stream=None, want32=True):
