@@ -587,6 +587,36 @@ def bank_wavefronts(vrec, vseg, elem_bytes, wave=32, nvs=0):
     return wf / tot if tot else 1.0
 
 
+def vrr_l1_wavefronts(cls, rq=1, elem_bytes=4):
+    """L1 wavefronts and FMAs per primitive quartet of the ungrouped VRR program run by the
+    warp form (rq = 1) or the stacked form (rq primitive quartets per record decode).
+    Counted per wave: the two 16-byte record loads of every lane (8 wavefronts, shared
+    by the rq quartets); per quartet and term, the operand load (its bank conflicts
+    included, per warp for 4-byte and per half-warp for 8-byte elements) and the
+    coefficient load (a gather from the quartet's 32 contiguous coefficients: 1
+    wavefront, or 2 for 8-byte elements); per quartet, the output store.  FMAs are the
+    nodes' terms, padding excluded.  Returns (fma, wavefronts) per primitive quartet."""
+    p = wide_program(cls)
+    vrec, vseg = p["vrec"], p["vseg"]
+    nb = 32 if elem_bytes == 4 else 16
+
+    def wf(slots):
+        parts = [slots] if elem_bytes == 4 else [slots[:16], slots[16:]]
+        return sum(max(len(v) for v in _bank_sets(x, nb).values()) for x in parts if x)
+    fma = 0
+    per_q = 0
+    rec = 0
+    for noff, _, cnt, _, _, _ in vseg:
+        for w0 in range(0, cnt, 32):
+            recs = [vrec[8 * (noff + n): 8 * (noff + n) + 8] for n in range(w0, min(cnt, w0 + 32))]
+            fma += sum(r[0] >> 16 for r in recs)
+            rec += 8
+            per_q += wf([r[0] & 0xffff for r in recs])
+            for t in range(recs[0][0] >> 16):
+                per_q += wf([r[1 + t] & 0xffff for r in recs]) + elem_bytes // 4
+    return fma, per_q + rec / rq
+
+
 def _bank_sets(slots, nbanks):
     """Distinct slots per bank (slot mod nbanks)."""
     out = {}

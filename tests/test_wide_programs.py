@@ -154,3 +154,22 @@ def test_bank_spread_keeps_slots_and_cuts_conflicts(cls, grouped):
         w1 = gen_eri.bank_wavefronts(p1["vrec"], p1["vseg"], eb, wave, p1["nvslot"])
         ideal = eb / 4                                     # 1 (FP32) or 2 (FP64)
         assert w1 <= w0 and (w1 < 0.9 * w0 or w0 <= ideal + 1e-9), (eb, w0, w1)
+
+
+@pytest.mark.parametrize("cls", [(1, 1, 1, 1), (2, 2, 2, 1)])
+def test_vrr_l1_wavefront_model(cls):
+    """The L1 model of the ungrouped VRR program: FMAs are the nodes' terms; every term of
+    a wave costs at least one operand and one coefficient wavefront per quartet (a wave
+    holds at most 32 nodes); stacking shares only the record loads, and no 8-byte load
+    takes fewer wavefronts than the 4-byte one (a bank shared within a half-warp is
+    shared within the warp)."""
+    p = gen_eri.wide_program(cls)
+    terms = sum(p["vrec"][8 * r] >> 16 for r in range(len(p["vrec"]) // 8))
+    f1, w1 = gen_eri.vrr_l1_wavefronts(cls, 1, 4)
+    f4, w4 = gen_eri.vrr_l1_wavefronts(cls, 4, 4)
+    _, w8 = gen_eri.vrr_l1_wavefronts(cls, 1, 8)
+    assert f1 == f4 == terms
+    assert w4 >= 2 * terms / 32
+    nwaves = sum(-(-s[2] // 32) for s in p["vseg"])
+    assert w1 - w4 == pytest.approx(8 * nwaves * (1 - 1 / 4))
+    assert w8 >= w1
