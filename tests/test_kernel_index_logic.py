@@ -240,3 +240,45 @@ def test_device_pair_groups_match_host():
         s = rng.integers(1, 40, n)
         got = pair_groups_device(torch.as_tensor(s)).numpy()
         assert np.array_equal(got, pair_groups(s)), n
+
+
+def _dense_expand_sources(l, quartets):
+    """k_dense_expand (csrc/dense.cu) on the CPU, each block element standing for its own
+    function quartet: per tensor position, the set of source elements written there."""
+    ncart = lambda x: (x + 1) * (x + 2) // 2
+    func_off = np.concatenate([[0], np.cumsum([ncart(x) for x in l])])
+    n = int(func_off[-1])
+    src = {}
+    for s in quartets:
+        A, B, C, D = (int(x) for x in s)
+        na, nb, nc, nd = (ncart(l[x]) for x in (A, B, C, D))
+        for e in range(na * nb * nc * nd):
+            id_, ic = e % nd, (e // nd) % nc
+            ib, ia = (e // (nd * nc)) % nb, e // (nd * nc * nb)
+            a, b, c, d = func_off[A] + ia, func_off[B] + ib, func_off[C] + ic, func_off[D] + id_
+            if (A == B and a < b) or (C == D and c < d) or \
+                    (A == C and B == D and (a < c or (a == c and b < d))):
+                continue
+            for p in ((a, b, c, d), (b, a, c, d), (a, b, d, c), (b, a, d, c),
+                      (c, d, a, b), (d, c, a, b), (c, d, b, a), (d, c, b, a)):
+                src.setdefault(tuple(int(x) for x in p), set()).add((a, b, c, d))
+    return n, src
+
+
+def test_dense_expand_one_writer_per_index_orbit():
+    """The 8-fold fill of the dense tensor (the reference's create_repulsion_matrix fills
+    every position from its canonical key, Symmetry.sort_index, common/symmetry.py:186-197):
+    over the unique shell quartets of shells with repeated angular momenta, every position
+    is written, by one source element only, from the position's own orbit, and all
+    positions of an orbit by the same element."""
+    from gaussium_gb300.dropin import unique_shell_quartets
+    l = [0, 1, 2, 1, 0]
+    n, src = _dense_expand_sources(l, unique_shell_quartets(len(l)))
+    assert len(src) == n ** 4
+    writer = {}
+    for pos, s in src.items():
+        assert len(s) == 1, (pos, s)
+        (e,) = s
+        key = oracle.sort_index(*pos)
+        assert oracle.sort_index(*e) == key
+        assert writer.setdefault(key, e) == e

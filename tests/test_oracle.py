@@ -167,3 +167,15 @@ def test_symmetry_screen_restatement_matches_reference():
             a, b, c, d = keys[t]
             for perm in ((b, a, c, d), (a, b, d, c), (c, d, a, b), (d, c, b, a)):
                 assert oracle.symmetry_nonzero(table, flip, cid, par, perm) == ref[t]
+
+
+def test_sort_index_known_answers():
+    """oracle.sort_index against the reference's own cases
+    (tests/testsfast/common/test_symmetry.py:14-48 within the reference project)."""
+    cases = [((6, 2, 1, 0), (0, 1, 2, 6)), ((0, 0, 1, 0), (0, 0, 0, 1)),
+             ((1, 0, 0, 0), (0, 0, 0, 1)), ((1, 0, 1, 0), (0, 1, 0, 1)),
+             ((2, 2, 1, 0), (0, 1, 2, 2)), ((2, 1, 1, 0), (0, 1, 1, 2)),
+             ((1, 1, 1, 0), (0, 1, 1, 1)), ((2, 1, 2, 0), (0, 2, 1, 2)),
+             ((1, 1, 0, 2), (0, 2, 1, 1))]
+    for key, want in cases:
+        assert tuple(oracle.sort_index(*key)) == want, key
