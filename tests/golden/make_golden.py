@@ -33,6 +33,9 @@ Each file records what produced it:
 * ``energies.npz``   reference total energies of test_start.py systems run without
                      point-group symmetry (HeH+ STO-3G RHF, O2 UHF/GUHF STO-3G).
 * ``heh_sto3g.npz``, ``o2_sto3g.npz``  their basis functions and S, T, V matrices.
+* ``heh_6311pgss.npz``, ``ethene_321g.npz``  the other RHF systems of test_start.py:15-25
+                     (HeH+ in 6-311+G**, ethene in 3-21G): reference RHF total energy and
+                     SCF iteration count, basis functions, and S, T, V.
 """
 import argparse
 import contextlib
@@ -485,6 +488,22 @@ def make_energies(procs):
     np.savez_compressed(os.path.join(HERE, "energies.npz"), **out)
 
 
+def make_start_rhf(procs):
+    ref_harness.load()
+    d = f"{ref_harness.reference_root()}/tests/testslow/start"
+    for tag, mol, gbs in (("heh_6311pgss", "HeH+.mol", "6-311+GPP.gbs"),
+                          ("ethene_321g", "C2H4.mol", "3-21G.gbs")):
+        nuclei, electrons, mult, basis = load_molecule(f"{d}/{mol}", f"{d}/{gbs}")
+        energy, iterations = run_rhf(nuclei, electrons, basis, procs)
+        np.savez_compressed(os.path.join(HERE, f"{tag}.npz"), energy=energy,
+                            iterations=iterations, electrons=electrons, multiplicity=mult,
+                            coords=np.array([x.coordinates for x in nuclei]),
+                            charges=np.array([x.charge for x in nuclei]),
+                            **one_electron(nuclei, basis), **basis_arrays(basis))
+        print(f"{tag}: {len(basis)} functions, E = {energy:.10f} in {iterations} iterations",
+              flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
@@ -498,7 +517,8 @@ def main():
              "synthetic": lambda: make_synthetic(args.procs, args.quick),
              "synthetic_k6": lambda: make_synthetic_k6(args.procs),
              "gradient_fd": lambda: make_gradient_fd(args.procs),
-             "energies": lambda: make_energies(args.procs)}
+             "energies": lambda: make_energies(args.procs),
+             "start_rhf": lambda: make_start_rhf(args.procs)}
     for name, fn in steps.items():
         if args.only and name not in args.only.split(","):
             continue

@@ -93,7 +93,8 @@ def _rhf(name, **kw):
     return res.energy + scf.nuclear_repulsion(g["charges"], g["coords"]), res, g
 
 
-@pytest.mark.parametrize("name", ["h2o_sto3g", "h2o_631gs", "heh_sto3g"])
+@pytest.mark.parametrize("name", ["h2o_sto3g", "h2o_631gs", "heh_sto3g", "heh_6311pgss",
+                                  "ethene_321g"])
 def test_rhf_energy_matches_reference(gpu_lib, name):
     e, res, g = _rhf(name)
     ref = float(golden("energies")["heh_sto3g_rhf"]) if name == "heh_sto3g" else float(g["energy"])

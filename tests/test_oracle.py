@@ -179,3 +179,25 @@ def test_sort_index_known_answers():
              ((1, 1, 0, 2), (0, 2, 1, 1))]
     for key, want in cases:
         assert tuple(oracle.sort_index(*key)) == want, key
+
+
+@pytest.mark.parametrize("name", ["heh_6311pgss", "ethene_321g"])
+def test_start_rhf_energies_through_the_oracle(name):
+    """HeH+/6-311+G** and ethene/3-21G (the reference's test_start.py:15-25 systems): the
+    restated SCF loop over the oracle's ERI tensor and Fock builder reproduces the
+    reference's RHF total energy to 1e-8 Eh."""
+    from molecules import load
+    from gaussium_gb300 import scf
+    g, _, table = load(name)
+    eri = oracle.dense_tensor(table, boys_mode=1)
+    hcore = g["kinetic"] + g["nuclear"]
+
+    class Fock:
+        core_hamiltonian = hcore
+
+        def create(self, p):
+            return oracle.fock_restricted(hcore, eri, p)
+    res = scf.restricted_scf(g["overlap"], hcore, int(g["electrons"]), Fock(), threshold=1e-12)
+    e = res.energy + scf.nuclear_repulsion(g["charges"], g["coords"])
+    assert res.converged
+    assert abs(e - float(g["energy"])) < 1e-8, (e, float(g["energy"]))
