@@ -13,6 +13,8 @@ Restated reference functions (file:line within the reference project):
   RestrictedKohnShamHamiltonian J part   kohnsham/kohn_sham_hamiltonian.py:15-19
   TwoElectronRepulsion.create_repulsion_matrix  matrixelements/electron_repulsion_matrix.py:28-47
   Symmetry.sort_index                    common/symmetry.py:186-197
+  MoellerPlesset.second_order            moellerplesset/moeller_plesset.py:14-22
+                                         (index loops: common/indices.py:30-32, 70-80)
 """
 import ctypes
 import itertools
@@ -290,6 +292,19 @@ def spin_basis_anti_physicist(repulsion):
                     b = (r % 2 == u % 2) * (s % 2 == t % 2) * repulsion[r // 2, u // 2, s // 2, t // 2]
                     out[r, s, t, u] = a - b
     return out
+
+
+def mp2_correlation(mo, orbital_energies, occupied):
+    """MoellerPlesset.second_order: for occupied i, j and unoccupied a, b, the sum of
+    [2 (ia|jb)^2 - (ia|jb)(ib|ja)] / (e_i + e_j - e_a - e_b) over the MO tensor in
+    chemists' order (the reference's molecular_orbitals)."""
+    e = np.asarray(orbital_energies, dtype=np.float64)
+    o, v = slice(0, occupied), slice(occupied, len(e))
+    iajb = np.asarray(mo)[o, v, o, v]
+    ibja = iajb.transpose(0, 3, 2, 1)
+    denom = (e[o, None, None, None] + e[None, None, o, None]
+             - e[None, v, None, None] - e[None, None, None, v])
+    return float(np.sum((2.0 * iajb * iajb - iajb * ibja) / denom))
 
 
 # ---------------------------------------------------------------------- LDA exchange-correlation

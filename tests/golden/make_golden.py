@@ -36,6 +36,9 @@ Each file records what produced it:
 * ``heh_6311pgss.npz``, ``ethene_321g.npz``  the other RHF systems of test_start.py:15-25
                      (HeH+ in 6-311+G**, ethene in 3-21G): reference RHF total energy and
                      SCF iteration count, basis functions, and S, T, V.
+* ``co_sto3g.npz``   carbon monoxide in STO-3G (test_start.py:45-49): reference RHF and MP2
+                     total energies (their difference is the MP2 correlation energy of
+                     moellerplesset/moeller_plesset.py), basis functions, and S, T, V.
 """
 import argparse
 import contextlib
@@ -504,6 +507,24 @@ def make_start_rhf(procs):
               flush=True)
 
 
+def make_start_mp2(procs):
+    g = ref_harness.load()
+    from gaussium.energy import Energy
+    d = f"{ref_harness.reference_root()}/tests/testslow/start"
+    nuclei, electrons, mult, basis = load_molecule(f"{d}/CO.mol", f"{d}/STO-3G.gbs")
+    energy_rhf, iterations = run_rhf(nuclei, electrons, basis, procs)
+    energy = Energy(electrons, mult, procs, "MP2")
+    energy.symmetry_object = ref_harness.c1_symmetry(basis)
+    energy_mp2 = float(quiet(energy.calculate_energy, nuclei, basis))
+    np.savez_compressed(os.path.join(HERE, "co_sto3g.npz"), energy_rhf=energy_rhf,
+                        energy_mp2=energy_mp2, iterations=iterations, electrons=electrons,
+                        multiplicity=mult, coords=np.array([x.coordinates for x in nuclei]),
+                        charges=np.array([x.charge for x in nuclei]),
+                        **one_electron(nuclei, basis), **basis_arrays(basis))
+    print(f"co_sto3g: {len(basis)} functions, RHF {energy_rhf:.10f}, MP2 {energy_mp2:.10f}",
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
@@ -518,7 +539,8 @@ def main():
              "synthetic_k6": lambda: make_synthetic_k6(args.procs),
              "gradient_fd": lambda: make_gradient_fd(args.procs),
              "energies": lambda: make_energies(args.procs),
-             "start_rhf": lambda: make_start_rhf(args.procs)}
+             "start_rhf": lambda: make_start_rhf(args.procs),
+             "start_mp2": lambda: make_start_mp2(args.procs)}
     for name, fn in steps.items():
         if args.only and name not in args.only.split(","):
             continue

@@ -201,3 +201,27 @@ def test_start_rhf_energies_through_the_oracle(name):
     e = res.energy + scf.nuclear_repulsion(g["charges"], g["coords"])
     assert res.converged
     assert abs(e - float(g["energy"])) < 1e-8, (e, float(g["energy"]))
+
+
+def test_co_mp2_energy_through_the_oracle():
+    """Carbon monoxide / STO-3G (the reference's test_start.py:45-49): the restated SCF
+    over the oracle's ERI tensor, the oracle's AO->MO transform and its MP2 sum reproduce
+    the reference's RHF and MP2 total energies to 1e-8 Eh."""
+    from molecules import load
+    from gaussium_gb300 import scf
+    g, _, table = load("co_sto3g")
+    eri = oracle.dense_tensor(table, boys_mode=1)
+    hcore = g["kinetic"] + g["nuclear"]
+
+    class Fock:
+        core_hamiltonian = hcore
+
+        def create(self, p):
+            return oracle.fock_restricted(hcore, eri, p)
+    res = scf.restricted_scf(g["overlap"], hcore, int(g["electrons"]), Fock(), threshold=1e-12)
+    e_nuc = scf.nuclear_repulsion(g["charges"], g["coords"])
+    assert res.converged
+    assert abs(res.energy + e_nuc - float(g["energy_rhf"])) < 1e-8
+    mo = oracle.molecular_orbitals(eri, res.coefficients)
+    corr = oracle.mp2_correlation(mo, res.orbital_energies, int(g["electrons"]) // 2)
+    assert abs(res.energy + e_nuc + corr - float(g["energy_mp2"])) < 1e-8

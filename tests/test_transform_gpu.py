@@ -161,3 +161,24 @@ def test_spin_expand_limits(gpu_lib):
     assert gpu_lib.gs_spin_expand(None, 0, 0, None, _lib.stream()) == 0
     with pytest.raises(ValueError):
         transform.spin_expand_device(torch.zeros((2, 3, 2, 2), dtype=torch.float64, device="cuda"), 0)
+
+
+def test_co_mp2_energy_matches_reference(gpu_lib):
+    """Carbon monoxide / STO-3G (the reference's test_start.py:45-49) end to end: RHF on the
+    GPU Fock builder, the AO tensor from the GPU ERI-matrix drop-in, the AO->MO transform on
+    the GPU, and the MP2 sum of moellerplesset/moeller_plesset.py:14-22 (restated in the
+    oracle) give the reference's RHF and MP2 total energies to 1e-8 Eh."""
+    from gaussium_gb300 import scf, transform
+    from gaussium_gb300.dropin import TwoElectronRepulsionGPU
+    from gaussium_gb300.fock import FockMatrixRestrictedGPU
+    g, funcs, _ = load("co_sto3g")
+    hcore = g["kinetic"] + g["nuclear"]
+    res = scf.restricted_scf(g["overlap"], hcore, int(g["electrons"]),
+                             FockMatrixRestrictedGPU(hcore, funcs), threshold=1e-12)
+    e_nuc = scf.nuclear_repulsion(g["charges"], g["coords"])
+    assert res.converged
+    assert abs(res.energy + e_nuc - float(g["energy_rhf"])) < 1e-8
+    ao = TwoElectronRepulsionGPU(funcs, None, None, 1).create_repulsion_matrix()
+    mo = transform.molecular_orbitals(ao, res.coefficients)
+    corr = oracle.mp2_correlation(mo, res.orbital_energies, int(g["electrons"]) // 2)
+    assert abs(res.energy + e_nuc + corr - float(g["energy_mp2"])) < 1e-8
