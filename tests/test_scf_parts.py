@@ -43,3 +43,16 @@ def test_density_matrix_restricted():
     g = golden("scf_parts")
     d = scf.density_matrix_restricted(g["C"], 2)
     assert np.max(np.abs(d - g["D"])) < 1e-13
+
+
+def test_nuclear_repulsion_two_nuclei():
+    """common/nuclear_repulsion.py:5-24 on the two pairs of the reference's
+    tests/testsfast/common/test_nuclear_repulsion.py:9-21 (H2 and HeH at +-z, bohr): the
+    sum over pairs equals the one pair's Z_a Z_b / r, which the reference pins to 4 and 7
+    figures."""
+    for z, half, want, digits in (((1.0, 1.0), (0.70, -0.70), 0.7143, 4),
+                                  ((1.0, 2.0), (0.7316, -0.7316), 1.366867, 7)):
+        coords = np.array([[0.0, 0.0, half[0]], [0.0, 0.0, half[1]]])
+        e = scf.nuclear_repulsion(np.array(z), coords)
+        assert abs(e - z[0] * z[1] / (half[0] - half[1])) < 1e-15
+        assert abs(e - want) <= 0.5 * 10.0 ** (np.floor(np.log10(abs(want))) - digits + 1)
