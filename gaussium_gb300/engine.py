@@ -148,11 +148,14 @@ class HeavyLane:
                 self.forked[k] = False
 
 
-def _check_sizes():
+def check_record_sizes(lib=None):
+    """The library's pair, primitive-pair and task record sizes (``gs_record_sizes``, a host
+    call) must equal the layouts this module packs; raises GsError on a mismatch."""
     sizes = np.zeros(4, dtype=np.int32)
-    _lib.check(_lib.lib().gs_record_sizes(sizes.ctypes.data), "gs_record_sizes")
-    if tuple(sizes) != (PAIR_REC, PRIM64, PRIM32, WRITE_TASK):
-        raise _lib.GsError(f"record sizes mismatch: library {tuple(sizes)}")
+    _lib.check((lib or _lib.lib()).gs_record_sizes(sizes.ctypes.data), "gs_record_sizes")
+    if tuple(int(x) for x in sizes) != (PAIR_REC, PRIM64, PRIM32, WRITE_TASK):
+        raise _lib.GsError(f"record sizes mismatch: library {tuple(sizes)}, host "
+                           f"{(PAIR_REC, PRIM64, PRIM32, WRITE_TASK)}")
 
 
 def indexed_device(device):

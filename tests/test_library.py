@@ -42,6 +42,8 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, name), name
     assert L.gs_version() == 1
     assert L.gs_status_string(0) == b"ok"
+    from gaussium_gb300 import engine
+    engine.check_record_sizes(L)              # host record layouts equal the library's
     limit = L.gs_status_string(6)
     assert b"no-allocation" in limit and b"gs_spin_expand_max_orbitals" in limit
 
@@ -94,3 +96,12 @@ def test_every_entry_point_is_documented_for_integrators():
     repository root."""
     doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     assert [n for n in declared_symbols() if n not in doc] == []
+
+
+def test_record_size_mismatch_is_refused(monkeypatch):
+    """A host record layout that differs from the library's is refused, not packed."""
+    from gaussium_gb300 import build, engine, _lib
+    L = _lib.load_library(build.build())
+    monkeypatch.setattr(engine, "PRIM64", engine.PRIM64 + 8)
+    with pytest.raises(_lib.GsError):
+        engine.check_record_sizes(L)
