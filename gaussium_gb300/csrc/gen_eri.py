@@ -26,7 +26,6 @@ are the algorithmic FLOP figures the roofline uses.
 
 Usage: python gen_eri.py OUTDIR [LMAX]
 """
-import itertools
 import json
 import os
 import sys

@@ -4,7 +4,6 @@ hartreefock/hartree_fock.py:20-84) with the ERI tensor replaced by the integral-
 Fock builder.  Records the wall time of every Fock build (CUDA-synchronised)."""
 import time
 
-import numpy as np
 import torch
 
 from . import scf

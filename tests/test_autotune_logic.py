@@ -2,7 +2,6 @@
 class with several forms is timed in each and left on its fastest; every class is then
 timed with and without its heavy form (split or cooperative) and keeps the faster; empty
 segments are skipped."""
-import pytest
 
 from gaussium_gb300 import autotune
 

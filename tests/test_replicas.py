@@ -3,7 +3,6 @@ workloads, meet only at barriers, and the whole-job time is the max over ranks."
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
